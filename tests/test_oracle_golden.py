@@ -1,0 +1,97 @@
+"""Pins the CPU oracle to the reference's own known answers.
+
+* Gauss-Hermite nodes/weights against Internal_data/HermQuadra (the files
+  sub_quadra_herm.f90 reads).
+* Henon-Heiles SG4 levels (6-D L=3, 21-D L=2; Working_tests/MPI_tests/*_S0/
+  benchmark) from a dense diagonalisation of the oracle's H.psi.  The
+  reference's Davidson converged to a residual of 5e-4 au, which bounds its
+  eigenvalue error near 1e-7 au; the tolerance below is 2e-7 au.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle.oracle import OracleSG4, gauss_hermite
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def test_hermquadra_bitwise():
+    d = json.load(open(os.path.join(GOLD, "hermquadra.json")))["nq"]
+    worst, exact, tot = 0.0, 0, 0
+    for nq_s, ref in d.items():
+        nq = int(nq_s)
+        x, w, wr = gauss_hermite(nq)
+        for a, b in ((x, ref["x"]), (wr, ref["wrho"]), (w, ref["w"])):
+            b = np.array(b)
+            err = np.abs(a - b) / np.maximum(np.abs(b), 1e-300)
+            worst = max(worst, float(err.max()))
+            exact += int(np.sum(a == b))
+            tot += nq
+    # nodes and weights are correctly rounded doubles of the 50-digit tables,
+    # except for rare 1-ulp ties
+    assert worst <= 2.3e-16, worst
+    assert exact >= tot - 8, (exact, tot)
+
+
+def hh_potential(Q, lam):
+    """Henon-Heiles V of Working_tests/MPI_tests/*/sub_system_HenonHeiles.f."""
+    V = 0.5 * np.sum(Q ** 2, axis=1)
+    for i in range(Q.shape[1] - 1):
+        V += lam * (Q[:, i] ** 2 * Q[:, i + 1] - Q[:, i + 1] ** 3 / 3.0)
+    return V
+
+
+@pytest.mark.parametrize("case", ["6D_Davidson_S0", "21D_Davidson_S0"])
+def test_henon_heiles_levels(case):
+    c = json.load(open(os.path.join(GOLD, "hh_levels.json")))["cases"][case]
+    D, L, B = c["D"], c["L"], c["L_TO_nq_B"]
+    o = OracleSG4(D, L, c["LB"], A_nb=c["L_TO_nq_A"], B_nb=B, A_nq=c["L_TO_nq_A"], B_nq=B)
+    V = hh_potential(o.grid_points(), c["lambda"])
+    H = o.hpsi(np.eye(o.N), type_op=1, V=V, F2=(-0.5 * np.eye(D)).ravel())
+    assert np.max(np.abs(H - H.T)) < 1e-12
+    ev = np.sort(np.linalg.eigvalsh(0.5 * (H + H.T)))
+    ref = np.array(c["levels_au"])
+    assert np.max(np.abs(ev[: len(ref)] - ref)) < 2e-7
+
+
+def test_sizes_match_index_set_formulas():
+    # N = C(L+D, D) and term counts for nb(l)=l+1, nq(l)=l+2
+    from math import comb
+    for D, L, nsg in ((3, 6, 64), (6, 8, 2975), (4, 7, 295)):
+        o = OracleSG4(D, L, L, 1, 1, 2, 1)
+        assert o.N == comb(L + D, D)
+        assert o.nb_SG == nsg
+        tab_l, w, m, p = o.tables()
+        assert abs(w.sum() - 1.0) < 1e-12
+        assert np.all((m >= 0) & (m <= o.N))
+        # every packed function is reached by at least one term
+        assert set(m[m > 0]) == set(range(1, o.N + 1))
+
+
+def test_type10_invariances():
+    # constant Jac and rho cancel in the type-10 formula
+    o = OracleSG4(3, 3, 3, 1, 1, 2, 1)
+    rng = np.random.default_rng(1)
+    V = rng.normal(size=o.sum_nq)
+    psi = rng.normal(size=(o.N, 2))
+    h0 = o.hpsi(psi, type_op=10, V=V)
+    c = np.full(o.sum_nq, 2.5)
+    h1 = o.hpsi(psi, type_op=10, V=V, Jac=c, sqRho=np.ones(o.sum_nq))
+    assert np.max(np.abs(h1 - h0)) <= 1e-13 * np.max(np.abs(h0))
+    G = np.zeros(o.sum_nq * 9)
+    oq = 0
+    for t in range(o.nb_SG):
+        pass
+    # identity G given explicitly equals G=None
+    tab_l = o.tables()[0]
+    off = 0
+    for t in range(o.nb_SG):
+        nq = int(np.prod(tab_l[t] + 2))
+        for i in range(3):
+            G[off * 9 + nq * (i + 3 * i): off * 9 + nq * (i + 3 * i) + nq] = 1.0
+        off += nq
+    h2 = o.hpsi(psi, type_op=10, V=V, G=G)
+    assert np.max(np.abs(h2 - h0)) <= 1e-14 * np.max(np.abs(h0))
