@@ -1,0 +1,318 @@
+"""Benchmark: batched SG4 H.psi (FP64) on the 6-D L=8 workload, one GB300.
+
+A step is one H.psi over the block of 20 right-hand sides of the 6-D, L=8,
+Q-dependent-G (type 10) SG4 Hamiltonian (seeded synthetic data, see
+elvibrot_gb300/configs.py).  value = right-hand-side H.psi applications per
+second with psi resident in HBM; e2e = the same through the host-pointer C
+ABI (pinned host psi copied in and H.psi copied out every step).  L2 is
+flushed (256 MB write) before every timed step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the reference algorithm's CPU implementation of the
+path (the C/OpenMP restatement in oracle/, the reference itself being
+Fortran that cannot be compiled here) on all host cores, same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SG4 H·psi/s FP64 (≤1e-12 rel) batched vs plain on 1 GB300"
+UNIT = "Hpsi/s"
+CONFIG_INDEX = 1
+WORKLOAD = "6-D SG4 (HO modes, L=LB=8, nb=l+1, nq=l+2), type-10 KEO with Q-dependent G, 20 real RHS"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def build_oracle_inputs(model):
+    from oracle.oracle import OracleSG4
+    O = OracleSG4(model.D, model.L, model.L, 1, 1, 2, 1, scaleQ=model.scaleQ)
+    Q = O.grid_points()
+    kw = dict(V=model.V(Q))
+    if model.type_op == 1:
+        kw.update(type_op=1, F2=model.F2.ravel())
+    else:
+        nq = np.prod(O.tables()[0] + 2, axis=1)
+        kw.update(type_op=10, G=model.G_grid(Q, nq))
+    return O, kw
+
+
+def time_oracle(model, nrhs, min_seconds, min_steps, max_steps, seed):
+    """Times the CPU restatement on all host threads; returns (Hpsi/s, steps, seconds, threads)."""
+    from elvibrot_gb300.configs import random_psi
+    O, kw = build_oracle_inputs(model)
+    psi = random_psi(O.N, nrhs, seed)
+    threads = os.cpu_count() or 1
+    O.hpsi(psi[:, :1], nthreads=threads, **kw)  # warm
+    t0 = time.perf_counter()
+    steps = 0
+    while steps < min_steps or (time.perf_counter() - t0 < min_seconds and steps < max_steps):
+        O.hpsi(psi, nthreads=threads, **kw)
+        steps += 1
+    dt = time.perf_counter() - t0
+    return steps * nrhs / dt, steps, dt, threads
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if not self.path or not os.path.exists(self.path):
+            return out
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        if sm:
+            out.update(sm_mhz=statistics.median(sm), sm_max_mhz=max(mx), reasons=sorted(reasons), samples=len(sm))
+        return out
+
+
+def profile_traffic():
+    """Per-launch DRAM traffic of the batched kernel from the committed ncu summary, if present."""
+    p = os.path.join(ROOT, "profiles", "hpsi_batched_6d_l8_20rhs.txt")
+    if not os.path.exists(p):
+        return None
+    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", open(p).read())
+    return float(m.group(1)) if m else None
+
+
+def run_ours(args, ws, rank, local):
+    import torch
+    import torch.distributed as dist
+    from elvibrot_gb300 import fp64_peak_tflops, lib
+    from elvibrot_gb300.configs import config, random_psi
+
+    torch.cuda.set_device(local)
+    cfg = config(CONFIG_INDEX)
+    model, nrhs = cfg["model"], cfg["nrhs"]
+    op = model.operator()
+    N = op.basis.N
+    psi_np = random_psi(N, nrhs, cfg["seed"])
+    psi = torch.from_numpy(np.ascontiguousarray(psi_np.T)).cuda()
+    out = torch.empty_like(psi)
+    flush = torch.empty(32 * 1024 * 1024, dtype=torch.float64, device="cuda")  # 256 MB > L2
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+
+    def step():
+        op.hpsi_dev(psi, out, stream=sh)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    peak = fp64_peak_tflops()
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            ev[k][0].record(stream)
+            step()
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+    launches = op.last_launches * args.steps
+    ms = [a.elapsed_time(b) for a, b in ev]
+    t_tot = sum(ms) / 1e3
+    if ws > 1:
+        t = torch.tensor([t_tot], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_tot = float(t.item())
+        dist.barrier()
+    ms_step = 1e3 * t_tot / args.steps
+    value = ws * args.steps * nrhs / t_tot
+
+    # end to end through the host-pointer C ABI: pinned psi in, H.psi out, every step
+    ph = torch.from_numpy(np.ascontiguousarray(psi_np.T)).pin_memory()
+    hh = torch.empty_like(ph).pin_memory()
+    L = lib()
+    import ctypes
+    for _ in range(2):
+        L.evr_sg4_hpsi_host(op._h, nrhs, ctypes.c_void_p(ph.data_ptr()), N, ctypes.c_void_p(hh.data_ptr()), N, 0.0, 1.0)
+    e2e_t = 0.0
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rc = L.evr_sg4_hpsi_host(op._h, nrhs, ctypes.c_void_p(ph.data_ptr()), N, ctypes.c_void_p(hh.data_ptr()), N,
+                                 0.0, 1.0)
+        e2e_t += time.perf_counter() - t0
+        assert rc == 0, L.evr_sg4_last_error().decode()
+    np.testing.assert_allclose(hh.numpy(), out.cpu().numpy(), rtol=0, atol=1e-12 * float(out.abs().max()))
+    e2e_value = ws * args.steps * nrhs / e2e_t
+
+    # plain per-term path (one launch per Smolyak term) on the same workload
+    plain_steps = max(2, min(5, args.steps))
+    op.hpsi_dev(psi, out, plain=True)
+    torch.cuda.synchronize()
+    pt = 0.0
+    for k in range(plain_steps):
+        flush.fill_(float(k))
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        op.hpsi_dev(psi, out, stream=sh, plain=True)
+        b.record(stream)
+        torch.cuda.synchronize()
+        pt += a.elapsed_time(b) / 1e3
+    plain_value = plain_steps * nrhs / pt
+
+    flops = op.flops_per_rhs * nrhs
+    achieved = flops / (ms_step / 1e3) / 1e12
+    b = op.basis
+    D = model.D
+    alg_bytes = 8.0 * 2 * N * nrhs + 8.0 * b.sum_nq * (1 + D * D)
+    hbm_peak = None
+    try:
+        hbm_peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get("hbm_gbs")
+    except (OSError, ValueError):
+        pass
+    hbm_peak = hbm_peak or 6800.0
+    result = None
+    if rank == 0:
+        cpu_v, cpu_steps, cpu_dt, cpu_threads = time_oracle(model, nrhs, min_seconds=1.5, min_steps=1,
+                                                            max_steps=50, seed=cfg["seed"])
+        clocks = clk.summary()
+        result = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded PCG64, configs[1] shapes)",
+            "config": {"workload": WORKLOAD, "D": D, "L": model.L, "nrhs": nrhs, "N": N, "nb_SG": b.nb_SG,
+                       "sum_nq": b.sum_nq, "type_op": 10, "l2": "flushed (256 MB write) before every timed step",
+                       "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * N * nrhs,
+                    "d2h_bytes_per_step": 8 * N * nrhs},
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": profile_traffic(),
+                         "peak_source": "in-run DFMA probe (evr_probe_fp64_peak); MEASURED_PEAKS.json has no FP64 entry",
+                         "flops_per_launch": flops,
+                         "hbm": {"achieved": alg_bytes / (ms_step / 1e3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                                 "frac": alg_bytes / (ms_step / 1e3) / 1e9 / hbm_peak,
+                                 "alg_bytes_per_launch": alg_bytes}},
+            "plain": {"value": plain_value, "unit": UNIT, "steps": plain_steps,
+                      "launches_per_step": 1 + b.nb_SG, "batched_over_plain": value / ws / plain_value},
+            "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cpu_threads, "kind": "port",
+                             "sample": f"{cpu_steps} full 20-RHS H.psi of the same workload in {cpu_dt:.2f} s "
+                                       f"(C/OpenMP restatement, OpenMP static over Smolyak terms)"},
+            "clocks": {"sm_mhz": clocks["sm_mhz"], "sm_max_mhz": clocks["sm_max_mhz"], "reasons": clocks["reasons"]},
+            "gpu_launches": launches,
+        }
+    return result
+
+
+def run_reference(args, ws, rank):
+    from elvibrot_gb300.configs import config
+    if rank != 0:
+        return None
+    cfg = config(CONFIG_INDEX)
+    model, nrhs = cfg["model"], cfg["nrhs"]
+    from oracle.oracle import OracleSG4  # noqa: F401
+    O, kw = build_oracle_inputs(model)
+    from elvibrot_gb300.configs import random_psi
+    psi = random_psi(O.N, nrhs, cfg["seed"])
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        O.hpsi(psi[:, :2], nthreads=threads, **kw)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        O.hpsi(psi, nthreads=threads, **kw)
+    dt = time.perf_counter() - t0
+    v = args.steps * nrhs / dt
+    return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded PCG64, configs[1] shapes)", "impl": "reference",
+            "config": {"workload": WORKLOAD, "D": model.D, "L": model.L, "nrhs": nrhs, "N": O.N},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} full 20-RHS H.psi steps (the reference is Fortran with no "
+                                       f"compiler on this image; timed: its C/OpenMP restatement)"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        import torch
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    if args.impl == "reference":
+        res = run_reference(args, ws, rank)
+    else:
+        res = run_ours(args, ws, rank, local)
+    if rank == 0 and res is not None:
+        print(json.dumps(res))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

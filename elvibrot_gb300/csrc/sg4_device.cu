@@ -1,0 +1,993 @@
+// sg4_device.cu -- GB300 (sm_103a) SG4 H.psi: context, operator fields and
+// the FP64 kernels behind include/evr_sg4.h.
+//
+// The reference computes, for every Smolyak term l (sub_TabOpPsi_FOR_SGtype4,
+// SRC/sub_Operator/sub_OpPsi_SG4.f90:681-977):
+//   gather (tabPackedBasis_TO_tabR_AT_iG) -> sum-factorised basis->grid
+//   (BDP_TO_GDP_OF_SmolyakRep) -> operator on the grid (CASE 0/1/10 of
+//   sub_TabOpPsi_OF_ONEDP_FOR_SGtype4) -> grid->basis (GDP_TO_BDP) ->
+//   weighted atomic scatter (tabR_AT_iG_TO_tabPackedBasis).
+// Here one persistent kernel runs every (term, block of right-hand sides)
+// work item of one H.psi: CTAs pull items from a cost-sorted list through a
+// global atomic counter, keep the whole term in shared memory (a per-CTA
+// slab of global scratch when a term does not fit), apply the 1-D matrices
+// mode by mode with one thread per fibre, and scatter with FP64 atomics.
+// GB300's FP64 pipe (~1.2 TFLOP/s measured) is the binding resource, so the
+// kernel is organised to keep it busy: two CTAs per SM so one computes while
+// the other gathers/synchronises, right-hand sides batched per item so the
+// 1-D matrices and the operator fields are loaded once per point, and no
+// FP64 work spent on anything but the algorithm's own multiply-adds.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "evr_sg4.h"
+#include "sg4_internal.h"
+
+namespace evr {
+
+static thread_local std::string g_err;
+
+int set_error(int code, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CUDA_TRY(call)                                                                          \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess)                                                                      \
+      return set_error(EVR_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+int desc_sizes(const evr_sg4_desc* d, DescSizes* z) {
+  if (!d) return set_error(EVR_ERR_ARG, "descriptor is NULL");
+  if (d->D < 1 || d->D > EVR_MAXD) return set_error(EVR_ERR_ARG, "D=%d outside [1,%d]", d->D, EVR_MAXD);
+  if (d->L < 0) return set_error(EVR_ERR_ARG, "L < 0");
+  if (d->nb0 != 1) return set_error(EVR_ERR_ARG, "nb0=%d: only nb0=1 is supported", d->nb0);
+  if (d->nb_SG < 1 || d->N < 1) return set_error(EVR_ERR_ARG, "empty basis (nb_SG=%lld, N=%lld)", d->nb_SG, d->N);
+  if (!d->nb_of_l || !d->nq_of_l || !d->tab_l || !d->weight || !d->map)
+    return set_error(EVR_ERR_ARG, "descriptor has NULL tables");
+  for (int k = 0; k < d->D * (d->L + 1); ++k) {
+    int nb = d->nb_of_l[k], nq = d->nq_of_l[k];
+    if (nb < 1 || nq < 1 || nb > EVR_MAXN || nq > EVR_MAXN)
+      return set_error(EVR_ERR_ARG, "nb/nq of (mode,level) %d = %d/%d outside [1,%d]", k, nb, nq, EVR_MAXN);
+    if (nb > nq)  // sub_read_data.f90:804: the basis may not outgrow its grid
+      return set_error(EVR_ERR_ARG, "nb=%d > nq=%d at (mode,level) %d", nb, nq, k);
+  }
+  z->sum_nb = z->sum_nq = z->max_nb = z->max_nq = 0;
+  for (long long t = 0; t < d->nb_SG; ++t) {
+    long long nb = 1, nq = 1;
+    for (int i = 0; i < d->D; ++i) {
+      int l = d->tab_l[t * d->D + i];
+      if (l < 0 || l > d->L) return set_error(EVR_ERR_ARG, "term %lld has level %d outside [0,L]", t, l);
+      nb *= d->nb_of_l[i * (d->L + 1) + l];
+      nq *= d->nq_of_l[i * (d->L + 1) + l];
+    }
+    z->sum_nb += nb;
+    z->sum_nq += nq;
+    z->max_nb = std::max(z->max_nb, nb);
+    z->max_nq = std::max(z->max_nq, nq);
+  }
+  return EVR_OK;
+}
+
+// ------------------------------------------------------------------ device
+struct TermInfo {
+  long long off_nb;   // into map
+  long long off_nq;   // into the operator fields
+  int nb, nq;
+  int r;              // right-hand sides per work item for this term
+  float cost;
+  double w;           // WeightSG
+  unsigned char l[EVR_MAXD];
+};
+
+struct Item {
+  int term;
+  int rhs0;
+};
+
+// 1-D matrices of (mode, level), row-major [nout][nin] for the kernel.
+enum { M_BG = 0, M_GB = 1, M_D1 = 2, M_D2 = 3 };
+
+struct OpFields {
+  int type;
+  const double* V;     // [sum_nq] or NULL
+  const double* G;     // [sum_nq*D*D] (GGiq per term) or NULL = identity
+  const double* Jac;   // [sum_nq] or NULL
+  const double* sqRho; // [sum_nq] or NULL
+  double F2[EVR_MAXD * EVR_MAXD];
+  double F1[EVR_MAXD];
+};
+
+struct KParams {
+  int D, Lp1;
+  int nrhs_v;                // virtual right-hand sides (2*nrhs for complex)
+  int cshift;                // 1 for interleaved complex, else 0
+  const TermInfo* terms;
+  const Item* items;
+  int n_items;
+  int item_base;             // plain path: items [item_base, item_base+gridDim.x)
+  unsigned int* counter;     // batched path: global work counter
+  const int* map;
+  const double* mats;
+  const int* mat_off;        // [D*Lp1*4]
+  const int* nb_of_l;
+  const int* nq_of_l;
+  const double* psi;
+  long long ldpsi;           // in doubles, already scaled for complex
+  double* hpsi;
+  long long ldh;
+  double scale;              // 1/Esc
+  const double* V;
+  const double* G;
+  const double* Jac;
+  const double* sqRho;
+  const double* F2;          // device [D*D]
+  const double* F1;          // device [D]
+  int type;
+  int nbuf;                  // work arrays per item
+  int smem_doubles;
+  double* gscratch;
+  long long scratch_per_cta; // doubles
+};
+
+struct ItemShared {
+  int nb[EVR_MAXD], nq[EVR_MAXD];
+  int mo[EVR_MAXD][4];
+  long long off_nb, off_nq;
+  int nb_t, nq_t, r, rhs0, term;
+  double w;
+  double* base;
+};
+
+__device__ __forceinline__ long long vaddr(const KParams& p, int v, int n, long long ld) {
+  // element n (0-based, packed index) of virtual right-hand side v
+  return (long long)(v >> p.cshift) * ld + ((long long)n << p.cshift) + (v & p.cshift);
+}
+
+// out[a + S*(k + nout*b)] (+)= scale * sum_m M[k*NIN+m] in[a + S*(m + NIN*b)]
+template <int NIN>
+__device__ __forceinline__ void mode_pass_t(const double* __restrict__ M, int nout, long long S,
+                                            long long R, const double* in, double* out, bool acc,
+                                            double scale) {
+  const long long nf = S * R;
+  for (long long f = threadIdx.x; f < nf; f += blockDim.x) {
+    long long b = f / S, a = f - b * S;
+    const double* fi = in + a + S * NIN * b;
+    double v[NIN];
+#pragma unroll
+    for (int m = 0; m < NIN; ++m) v[m] = fi[S * m];
+    double* fo = out + a + S * (long long)nout * b;
+    for (int k = 0; k < nout; ++k) {
+      const double* Mk = M + k * NIN;
+      double s = 0.0;
+#pragma unroll
+      for (int m = 0; m < NIN; ++m) s = fma(__ldg(Mk + m), v[m], s);
+      fo[S * k] = acc ? fma(scale, s, fo[S * k]) : (scale == 1.0 ? s : scale * s);
+    }
+  }
+}
+
+__device__ void mode_pass(const double* M, int nin, int nout, long long S, long long R,
+                          const double* in, double* out, bool acc, double scale) {
+  switch (nin) {
+#define EVR_CASE(n) \
+  case n:           \
+    mode_pass_t<n>(M, nout, S, R, in, out, acc, scale); break;
+    EVR_CASE(1) EVR_CASE(2) EVR_CASE(3) EVR_CASE(4) EVR_CASE(5) EVR_CASE(6) EVR_CASE(7) EVR_CASE(8)
+    EVR_CASE(9) EVR_CASE(10) EVR_CASE(11) EVR_CASE(12) EVR_CASE(13) EVR_CASE(14) EVR_CASE(15) EVR_CASE(16)
+#undef EVR_CASE
+    default: break;
+  }
+}
+
+// Derivative pass along mode i on the grid (DerivOp_TO_RDP_OF_SmolaykRep).
+__device__ void grid_deriv(const KParams& p, const ItemShared& it, int i, int which, const double* in,
+                           double* out, bool acc, double scale) {
+  long long S = 1, R = it.r;
+  for (int j = 0; j < p.D; ++j) {
+    if (j < i) S *= it.nq[j];
+    else if (j > i) R *= it.nq[j];
+  }
+  mode_pass(p.mats + it.mo[i][which], it.nq[i], it.nq[i], S, R, in, out, acc, scale);
+}
+
+// basis->grid (to_grid = true, BDP_TO_GDP) or grid->basis (GDP_TO_BDP), modes 1..D
+__device__ double* transform(const KParams& p, const ItemShared& it, bool to_grid, double* a, double* b) {
+  long long S = 1, R = it.r;
+  for (int j = 0; j < p.D; ++j) R *= to_grid ? it.nb[j] : it.nq[j];
+  for (int i = 0; i < p.D; ++i) {
+    int nin = to_grid ? it.nb[i] : it.nq[i];
+    int nout = to_grid ? it.nq[i] : it.nb[i];
+    R /= nin;
+    mode_pass(p.mats + it.mo[i][to_grid ? M_BG : M_GB], nin, nout, S, R, a, b, false, 1.0);
+    S *= nout;
+    __syncthreads();
+    double* t = a;
+    a = b;
+    b = t;
+  }
+  return a;
+}
+
+__device__ void run_item(const KParams& p, ItemShared& it, double* smem, int item_idx) {
+  if (threadIdx.x == 0) {
+    const Item itm = p.items[item_idx];
+    const TermInfo& T = p.terms[itm.term];
+    it.term = itm.term;
+    it.rhs0 = itm.rhs0;
+    it.r = min(T.r, p.nrhs_v - itm.rhs0);
+    it.off_nb = T.off_nb;
+    it.off_nq = T.off_nq;
+    it.nb_t = T.nb;
+    it.nq_t = T.nq;
+    it.w = T.w;
+    long long need = (long long)p.nbuf * T.nq * it.r;
+    it.base = (need <= p.smem_doubles) ? smem : p.gscratch + (long long)blockIdx.x * p.scratch_per_cta;
+  }
+  if (threadIdx.x < p.D) {
+    const int i = threadIdx.x;
+    const int l = p.terms[p.items[item_idx].term].l[i];
+    const int k = i * p.Lp1 + l;
+    it.nb[i] = p.nb_of_l[k];
+    it.nq[i] = p.nq_of_l[k];
+    for (int q = 0; q < 4; ++q) it.mo[i][q] = p.mat_off[k * 4 + q];
+  }
+  __syncthreads();
+  const int D = p.D, r = it.r, nbt = it.nb_t, nqt = it.nq_t;
+  const long long NQR = (long long)nqt * r;
+  double* buf = it.base;
+  double* X = buf;
+  double* T = buf + NQR;
+  const int* map = p.map + it.off_nb;
+
+  // gather (tabPackedBasis_TO_tabR_AT_iG)
+  for (long long e = threadIdx.x; e < (long long)nbt * r; e += blockDim.x) {
+    int j = (int)(e / nbt), k = (int)(e - (long long)j * nbt);
+    int n = __ldg(map + k);
+    X[e] = n > 0 ? p.psi[vaddr(p, it.rhs0 + j, n - 1, p.ldpsi)] : 0.0;
+  }
+  __syncthreads();
+  double* x = transform(p, it, true, X, T);
+  double* y;
+  const long long oq = it.off_nq;
+
+  if (p.type == 0) {
+    // CASE 0: y = V.x
+    for (long long e = threadIdx.x; e < NQR; e += blockDim.x) {
+      long long q = e % nqt;
+      x[e] = (p.V ? __ldg(p.V + oq + q) : 0.0) * x[e];
+    }
+    y = x;
+    __syncthreads();
+  } else if (p.type == 1) {
+    // CASE 1: y = V.x + sum F2_ij d_i d_j x + sum F1_i d_i x
+    double* other = (x == X) ? T : X;
+    double* Y = buf + 2 * NQR;
+    double* C = buf + 3 * NQR;
+    for (long long e = threadIdx.x; e < NQR; e += blockDim.x) {
+      long long q = e % nqt;
+      Y[e] = p.V ? __ldg(p.V + oq + q) * x[e] : 0.0;
+    }
+    __syncthreads();
+    for (int i = 0; i < D; ++i)
+      for (int j = i; j < D; ++j) {
+        double f = p.F2[i * D + j];
+        if (f == 0.0) continue;
+        if (i == j) {
+          grid_deriv(p, it, i, M_D2, x, Y, true, f);
+        } else {
+          grid_deriv(p, it, i, M_D1, x, C, false, 1.0);
+          __syncthreads();
+          grid_deriv(p, it, j, M_D1, C, Y, true, f);
+        }
+        __syncthreads();
+      }
+    for (int i = 0; i < D; ++i) {
+      double f = p.F1[i];
+      if (f == 0.0) continue;
+      grid_deriv(p, it, i, M_D1, x, Y, true, f);
+      __syncthreads();
+    }
+    (void)other;
+    y = Y;
+  } else {
+    // CASE 10: -1/2 sum_i d_i(Jac sum_j G_ji d_j(s x)) / (Jac s) + V x
+    double* VX = buf + 2 * NQR;
+    double* O = buf + 3 * NQR;
+    double* Phi = buf + 4 * NQR;
+    for (long long e = threadIdx.x; e < NQR; e += blockDim.x) {
+      long long q = e % nqt;
+      double xv = x[e];
+      VX[e] = p.V ? __ldg(p.V + oq + q) * xv : 0.0;
+      if (p.sqRho) x[e] = xv * __ldg(p.sqRho + oq + q);
+    }
+    __syncthreads();
+    for (int j = 0; j < D; ++j) grid_deriv(p, it, j, M_D1, x, Phi + (long long)j * NQR, false, 1.0);
+    __syncthreads();
+    double* U = x;  // s.x is no longer needed
+    const long long GD = (long long)D * D;
+    for (int i = 0; i < D; ++i) {
+      for (long long e = threadIdx.x; e < NQR; e += blockDim.x) {
+        long long q = e % nqt;
+        double u = 0.0;
+        if (p.G) {
+          const double* g = p.G + oq * GD + (long long)nqt * ((long long)D * i) + q;
+          for (int j = 0; j < D; ++j) u = fma(__ldg(g + (long long)nqt * j), Phi[(long long)j * NQR + e], u);
+        } else {
+          u = Phi[(long long)i * NQR + e];
+        }
+        if (p.Jac) u *= __ldg(p.Jac + oq + q);
+        U[e] = u;
+      }
+      __syncthreads();
+      grid_deriv(p, it, i, M_D1, U, O, i > 0, 1.0);
+      __syncthreads();
+    }
+    for (long long e = threadIdx.x; e < NQR; e += blockDim.x) {
+      long long q = e % nqt;
+      double jac = p.Jac ? __ldg(p.Jac + oq + q) : 1.0;
+      double s = p.sqRho ? __ldg(p.sqRho + oq + q) : 1.0;
+      O[e] = -0.5 * O[e] / (jac * s) + VX[e];
+    }
+    __syncthreads();
+    y = O;
+    // G->B ping-pongs between O and U
+    double* yb = transform(p, it, false, O, U);
+    const double wt = it.w * p.scale;
+    for (long long e = threadIdx.x; e < (long long)nbt * r; e += blockDim.x) {
+      int j = (int)(e / nbt), k = (int)(e - (long long)j * nbt);
+      int n = __ldg(map + k);
+      if (n > 0) atomicAdd(p.hpsi + vaddr(p, it.rhs0 + j, n - 1, p.ldh), wt * yb[e]);
+    }
+    __syncthreads();
+    return;
+  }
+  double* other = (y == X) ? T : X;
+  if (p.type == 1) other = (x == X) ? X : T;  // x is free after the operator
+  double* yb = transform(p, it, false, y, other);
+  const double wt = it.w * p.scale;
+  for (long long e = threadIdx.x; e < (long long)nbt * r; e += blockDim.x) {
+    int j = (int)(e / nbt), k = (int)(e - (long long)j * nbt);
+    int n = __ldg(map + k);
+    if (n > 0) atomicAdd(p.hpsi + vaddr(p, it.rhs0 + j, n - 1, p.ldh), wt * yb[e]);
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(256, 2) hpsi_batched_kernel(KParams p) {
+  extern __shared__ double smem[];
+  __shared__ ItemShared it;
+  __shared__ int next;
+  for (;;) {
+    if (threadIdx.x == 0) next = (int)atomicAdd(p.counter, 1u);
+    __syncthreads();
+    int idx = next;
+    __syncthreads();
+    if (idx >= p.n_items) break;
+    run_item(p, it, smem, idx);
+  }
+}
+
+__global__ void __launch_bounds__(256, 2) hpsi_plain_kernel(KParams p) {
+  extern __shared__ double smem[];
+  __shared__ ItemShared it;
+  run_item(p, it, smem, p.item_base + blockIdx.x);
+}
+
+// hpsi(:,v) = -(E0/Esc) psi(:,v) over the packed vectors; also resets the
+// work counter of the batched kernel that follows on the same stream.
+__global__ void hpsi_init_kernel(double* hpsi, const double* psi, long long N, int nrhs_v, int cshift,
+                                 long long ldpsi, long long ldh, double a, unsigned int* counter) {
+  if (blockIdx.x == 0 && threadIdx.x == 0 && counter) *counter = 0u;
+  long long total = N * nrhs_v;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    int v = (int)(e / N);
+    long long n = e - (long long)v * N;
+    long long oh = (long long)(v >> cshift) * ldh + (n << cshift) + (v & cshift);
+    long long op = (long long)(v >> cshift) * ldpsi + (n << cshift) + (v & cshift);
+    hpsi[oh] = (a == 0.0) ? 0.0 : a * psi[op];
+  }
+}
+
+// Operator fields on the term grids: V from a polynomial, G from the affine
+// form (get_OpGrid_type10_OF_ONEDP_FOR_SG4 evaluates them point by point).
+__device__ void point_coords(const int* nq_of_l, const double* xcat, const int* x_off, int D, int Lp1,
+                             const TermInfo& T, long long q, double* Q) {
+  for (int i = 0; i < D; ++i) {
+    int k = i * Lp1 + T.l[i];
+    int nqi = nq_of_l[k];
+    long long iq = q % nqi;
+    q /= nqi;
+    Q[i] = xcat[x_off[k] + iq];
+  }
+}
+
+__global__ void fields_kernel(const TermInfo* terms, long long nb_SG, const long long* pt_term_start,
+                              const int* nq_of_l, const double* xcat, const int* x_off, int D, int Lp1,
+                              int V_nterms, const double* V_coef, const int* V_expo, double* V,
+                              const double* G0, const double* G1, double* G, long long sum_nq) {
+  for (long long gp = blockIdx.x * (long long)blockDim.x + threadIdx.x; gp < sum_nq;
+       gp += (long long)gridDim.x * blockDim.x) {
+    // binary search of the term owning global point gp
+    long long lo = 0, hi = nb_SG - 1;
+    while (lo < hi) {
+      long long mid = (lo + hi + 1) / 2;
+      if (pt_term_start[mid] <= gp) lo = mid; else hi = mid - 1;
+    }
+    const TermInfo& T = terms[lo];
+    long long q = gp - T.off_nq;
+    double Q[EVR_MAXD];
+    point_coords(nq_of_l, xcat, x_off, D, Lp1, T, q, Q);
+    if (V) {
+      double v = 0.0;
+      for (int t = 0; t < V_nterms; ++t) {
+        double m = V_coef[t];
+        for (int i = 0; i < D; ++i) {
+          int e = V_expo[t * D + i];
+          for (int k = 0; k < e; ++k) m *= Q[i];
+        }
+        v += m;
+      }
+      V[gp] = v;
+    }
+    if (G) {
+      const long long nqt = T.nq;
+      for (int i = 0; i < D; ++i)
+        for (int j = 0; j < D; ++j) {
+          double g = G0 ? G0[i * D + j] : (i == j ? 1.0 : 0.0);
+          if (G1)
+            for (int k = 0; k < D; ++k) g = fma(G1[((long long)i * D + j) * D + k], Q[k], g);
+          // GGiq(iq, j, i) of the term
+          G[T.off_nq * D * D + nqt * ((long long)D * i + j) + q] = g;
+        }
+    }
+  }
+}
+
+// In-bounds DFMA loop used to measure the FP64 peak.
+__global__ void dfma_peak_kernel(double* out, int iters, double a, double b) {
+  double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6,
+         x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+}  // namespace evr
+
+using namespace evr;
+
+// ----------------------------------------------------------------- context
+struct evr_sg4_ctx {
+  int D = 0, L = 0, LB = 0;
+  long long N = 0, nb_SG = 0;
+  DescSizes z;
+  int device = 0, num_sms = 0;
+  std::vector<int> nb_of_l, nq_of_l, mat_off, x_off;
+  std::vector<TermInfo> terms;  // host copy (r filled per nrhs)
+  // device
+  int* d_map = nullptr;
+  double* d_mats = nullptr;
+  int* d_mat_off = nullptr;
+  int* d_nb_of_l = nullptr;
+  int* d_nq_of_l = nullptr;
+  double* d_x = nullptr;
+  int* d_x_off = nullptr;
+  TermInfo* d_terms = nullptr;
+  Item* d_items = nullptr;
+  size_t items_cap = 0;
+  int items_nrhs = -1;           // items built for this virtual nrhs
+  int n_items = 0;
+  std::vector<int> term_item_start;  // plain path
+  unsigned int* d_counter = nullptr;
+  double* d_scratch = nullptr;
+  long long scratch_per_cta = 0;
+  int grid = 0;
+  int smem_doubles = 0;
+  // operator
+  bool have_op = false;
+  int type = -1;
+  double* d_V = nullptr;
+  double* d_G = nullptr;
+  double* d_Jac = nullptr;
+  double* d_sqRho = nullptr;
+  double* d_F2 = nullptr;
+  double* d_F1 = nullptr;
+  double F2[EVR_MAXD * EVR_MAXD] = {0};
+  double F1[EVR_MAXD] = {0};
+  // host-pointer path buffers
+  double* d_io = nullptr;
+  size_t io_cap = 0;
+  long long last_launches = 0;
+};
+
+static int nbuf_for(int type, int D) { return type == 0 ? 2 : (type == 1 ? 4 : D + 4); }
+
+static void free_ctx(evr_sg4_ctx* c) {
+  void* ptrs[] = {c->d_map, c->d_mats, c->d_mat_off, c->d_nb_of_l, c->d_nq_of_l, c->d_x, c->d_x_off,
+                  c->d_terms, c->d_items, c->d_counter, c->d_scratch, c->d_V, c->d_G, c->d_Jac,
+                  c->d_sqRho, c->d_F2, c->d_F1, c->d_io};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  delete c;
+}
+
+template <class T>
+static int upload(T** dst, const T* src, size_t n) {
+  if (n == 0) n = 1;
+  CUDA_TRY(cudaMalloc((void**)dst, n * sizeof(T)));
+  if (src) CUDA_TRY(cudaMemcpy(*dst, src, n * sizeof(T), cudaMemcpyHostToDevice));
+  return EVR_OK;
+}
+
+extern "C" const char* evr_sg4_last_error(void) { return g_err.c_str(); }
+
+extern "C" int evr_sg4_create(const evr_sg4_desc* d, evr_sg4_ctx** out) {
+  if (!out) return set_error(EVR_ERR_ARG, "evr_sg4_create: out is NULL");
+  *out = nullptr;
+  DescSizes z;
+  int rc = desc_sizes(d, &z);
+  if (rc) return rc;
+  if (!d->RGB || !d->RBGwrho || !d->d1GG || !d->d2GG || !d->x)
+    return set_error(EVR_ERR_ARG, "evr_sg4_create: descriptor has NULL matrices");
+  if (d->N > 2147483647LL) return set_error(EVR_ERR_ARG, "evr_sg4_create: N exceeds int32");
+  for (long long k = 0; k < z.sum_nb; ++k)
+    if (d->map[k] < 0 || d->map[k] > d->N)
+      return set_error(EVR_ERR_ARG, "evr_sg4_create: map[%lld]=%d outside [0,N]", k, d->map[k]);
+  evr_sg4_ctx* c = new evr_sg4_ctx();
+  c->D = d->D;
+  c->L = d->L;
+  c->LB = d->LB;
+  c->N = d->N;
+  c->nb_SG = d->nb_SG;
+  c->z = z;
+  const int D = d->D, Lp1 = d->L + 1;
+  cudaError_t e = cudaGetDevice(&c->device);
+  if (e != cudaSuccess) {
+    free_ctx(c);
+    return set_error(EVR_ERR_CUDA, "evr_sg4_create: no CUDA device (%s)", cudaGetErrorString(e));
+  }
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
+  c->nb_of_l.assign(d->nb_of_l, d->nb_of_l + D * Lp1);
+  c->nq_of_l.assign(d->nq_of_l, d->nq_of_l + D * Lp1);
+  // matrices, re-laid out row-major [nout][nin]
+  std::vector<double> mats;
+  c->mat_off.resize((size_t)D * Lp1 * 4);
+  c->x_off.resize((size_t)D * Lp1);
+  size_t o_rgb = 0, o_gb = 0, o_gg = 0, o_x = 0;
+  for (int k = 0; k < D * Lp1; ++k) {
+    int nb = c->nb_of_l[k], nq = c->nq_of_l[k];
+    c->x_off[k] = (int)o_x;
+    o_x += nq;
+    c->mat_off[k * 4 + M_BG] = (int)mats.size();
+    for (int q = 0; q < nq; ++q)
+      for (int b = 0; b < nb; ++b) mats.push_back(d->RGB[o_rgb + q + (size_t)nq * b]);
+    c->mat_off[k * 4 + M_GB] = (int)mats.size();
+    for (int b = 0; b < nb; ++b)
+      for (int q = 0; q < nq; ++q) mats.push_back(d->RBGwrho[o_gb + b + (size_t)nb * q]);
+    c->mat_off[k * 4 + M_D1] = (int)mats.size();
+    for (int r = 0; r < nq; ++r)
+      for (int s = 0; s < nq; ++s) mats.push_back(d->d1GG[o_gg + r + (size_t)nq * s]);
+    c->mat_off[k * 4 + M_D2] = (int)mats.size();
+    for (int r = 0; r < nq; ++r)
+      for (int s = 0; s < nq; ++s) mats.push_back(d->d2GG[o_gg + r + (size_t)nq * s]);
+    o_rgb += (size_t)nq * nb;
+    o_gb += (size_t)nq * nb;
+    o_gg += (size_t)nq * nq;
+  }
+  c->terms.resize(d->nb_SG);
+  long long onb = 0, onq = 0;
+  for (long long t = 0; t < d->nb_SG; ++t) {
+    TermInfo& T = c->terms[t];
+    memset(&T, 0, sizeof(T));
+    long long nb = 1, nq = 1;
+    for (int i = 0; i < D; ++i) {
+      int l = d->tab_l[t * D + i];
+      T.l[i] = (unsigned char)l;
+      nb *= c->nb_of_l[i * Lp1 + l];
+      nq *= c->nq_of_l[i * Lp1 + l];
+    }
+    T.off_nb = onb;
+    T.off_nq = onq;
+    T.nb = (int)nb;
+    T.nq = (int)nq;
+    T.w = d->weight[t];
+    onb += nb;
+    onq += nq;
+  }
+  // launch geometry: two 256-thread CTAs per SM, ~110 KB of shared memory each
+  c->smem_doubles = 110 * 1024 / 8;
+  c->grid = 2 * c->num_sms;
+  if ((rc = upload(&c->d_map, d->map, (size_t)z.sum_nb)) ||
+      (rc = upload(&c->d_mats, mats.data(), mats.size())) ||
+      (rc = upload(&c->d_mat_off, c->mat_off.data(), c->mat_off.size())) ||
+      (rc = upload(&c->d_nb_of_l, c->nb_of_l.data(), c->nb_of_l.size())) ||
+      (rc = upload(&c->d_nq_of_l, c->nq_of_l.data(), c->nq_of_l.size())) ||
+      (rc = upload(&c->d_x, d->x, o_x)) ||
+      (rc = upload(&c->d_x_off, c->x_off.data(), c->x_off.size())) ||
+      (rc = upload<TermInfo>(&c->d_terms, nullptr, c->terms.size())) ||
+      (rc = upload<unsigned int>(&c->d_counter, nullptr, 1))) {
+    free_ctx(c);
+    return rc;
+  }
+  e = cudaFuncSetAttribute(hpsi_batched_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, c->smem_doubles * 8);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(hpsi_plain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, c->smem_doubles * 8);
+  if (e != cudaSuccess) {
+    free_ctx(c);
+    return set_error(EVR_ERR_CUDA, "evr_sg4_create: shared-memory attribute: %s", cudaGetErrorString(e));
+  }
+  *out = c;
+  return EVR_OK;
+}
+
+extern "C" int evr_sg4_destroy(evr_sg4_ctx* c) {
+  if (!c) return set_error(EVR_ERR_ARG, "evr_sg4_destroy: NULL context");
+  cudaDeviceSynchronize();
+  free_ctx(c);
+  return EVR_OK;
+}
+
+extern "C" int evr_sg4_set_operator(evr_sg4_ctx* c, const evr_sg4_op_desc* op) {
+  if (!c || !op) return set_error(EVR_ERR_ARG, "evr_sg4_set_operator: NULL argument");
+  if (op->type != 0 && op->type != 1 && op->type != 10)
+    return set_error(EVR_ERR_ARG, "evr_sg4_set_operator: type_Op=%d not in {0,1,10}", op->type);
+  const int D = c->D;
+  const long long snq = c->z.sum_nq;
+  for (double** p : {&c->d_V, &c->d_G, &c->d_Jac, &c->d_sqRho, &c->d_F2, &c->d_F1})
+    if (*p) {
+      cudaFree(*p);
+      *p = nullptr;
+    }
+  c->have_op = false;
+  c->type = op->type;
+  int rc;
+  if (op->V_grid) {
+    for (long long k = 0; k < snq; ++k)
+      if (!std::isfinite(op->V_grid[k])) return set_error(EVR_ERR_NUMERIC, "V_grid[%lld] is not finite", k);
+    if ((rc = upload(&c->d_V, op->V_grid, (size_t)snq))) return rc;
+  }
+  bool need_fields_kernel = false;
+  if (!op->V_grid && op->V_nterms > 0) {
+    if (!op->V_coef || !op->V_expo) return set_error(EVR_ERR_ARG, "V polynomial without coef/expo");
+    for (int t = 0; t < op->V_nterms * D; ++t)
+      if (op->V_expo[t] < 0 || op->V_expo[t] > 16) return set_error(EVR_ERR_ARG, "V exponent outside [0,16]");
+    CUDA_TRY(cudaMalloc(&c->d_V, (size_t)snq * 8));
+    need_fields_kernel = true;
+  }
+  if (op->type == 10) {
+    if (op->G_grid) {
+      if ((rc = upload(&c->d_G, op->G_grid, (size_t)snq * D * D))) return rc;
+    } else if (op->G0 || op->G1) {
+      CUDA_TRY(cudaMalloc(&c->d_G, (size_t)snq * D * D * 8));
+      need_fields_kernel = true;
+    }
+    if (op->Jac_grid) {
+      for (long long k = 0; k < snq; ++k)
+        if (!(op->Jac_grid[k] != 0.0) || !std::isfinite(op->Jac_grid[k]))
+          return set_error(EVR_ERR_NUMERIC, "Jac_grid[%lld] is zero or not finite", k);
+      if ((rc = upload(&c->d_Jac, op->Jac_grid, (size_t)snq))) return rc;
+    }
+    if (op->sqRho_grid) {
+      for (long long k = 0; k < snq; ++k)
+        if (!(op->sqRho_grid[k] != 0.0) || !std::isfinite(op->sqRho_grid[k]))
+          return set_error(EVR_ERR_NUMERIC, "sqRho_grid[%lld] is zero or not finite", k);
+      if ((rc = upload(&c->d_sqRho, op->sqRho_grid, (size_t)snq))) return rc;
+    }
+  }
+  memset(c->F2, 0, sizeof(c->F2));
+  memset(c->F1, 0, sizeof(c->F1));
+  if (op->type == 1) {
+    if (op->F2)
+      for (int i = 0; i < D; ++i)
+        for (int j = i; j < D; ++j) c->F2[i * D + j] = op->F2[i * D + j];
+    if (op->F1)
+      for (int i = 0; i < D; ++i) c->F1[i] = op->F1[i];
+  }
+  if ((rc = upload(&c->d_F2, c->F2, (size_t)D * D)) || (rc = upload(&c->d_F1, c->F1, (size_t)D))) return rc;
+  if (need_fields_kernel) {
+    std::vector<long long> start(c->nb_SG);
+    for (long long t = 0; t < c->nb_SG; ++t) start[t] = c->terms[t].off_nq;
+    long long* d_start = nullptr;
+    double *d_coef = nullptr, *d_G0 = nullptr, *d_G1 = nullptr;
+    int* d_expo = nullptr;
+    TermInfo* d_terms = c->d_terms;
+    CUDA_TRY(cudaMemcpy(d_terms, c->terms.data(), c->terms.size() * sizeof(TermInfo), cudaMemcpyHostToDevice));
+    if ((rc = upload(&d_start, start.data(), start.size()))) return rc;
+    bool polyV = !op->V_grid && op->V_nterms > 0;
+    if (polyV && ((rc = upload(&d_coef, op->V_coef, (size_t)op->V_nterms)) ||
+                  (rc = upload(&d_expo, op->V_expo, (size_t)op->V_nterms * D))))
+      return rc;
+    bool affG = op->type == 10 && !op->G_grid && (op->G0 || op->G1);
+    if (affG && op->G0 && (rc = upload(&d_G0, op->G0, (size_t)D * D))) return rc;
+    if (affG && op->G1 && (rc = upload(&d_G1, op->G1, (size_t)D * D * D))) return rc;
+    fields_kernel<<<4 * c->num_sms, 256>>>(c->d_terms, c->nb_SG, d_start, c->d_nq_of_l, c->d_x, c->d_x_off, D,
+                                           c->L + 1, polyV ? op->V_nterms : 0, d_coef, d_expo,
+                                           polyV ? c->d_V : nullptr, d_G0, d_G1, affG ? c->d_G : nullptr, snq);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaDeviceSynchronize());
+    cudaFree(d_start);
+    if (d_coef) cudaFree(d_coef);
+    if (d_expo) cudaFree(d_expo);
+    if (d_G0) cudaFree(d_G0);
+    if (d_G1) cudaFree(d_G1);
+  }
+  c->have_op = true;
+  c->items_nrhs = -1;  // work split depends on the operator's buffer count
+  return EVR_OK;
+}
+
+// Builds the (term, rhs block) work list for nrhs_v virtual right-hand sides,
+// sorted by decreasing cost so the persistent kernel balances well.
+static int build_items(evr_sg4_ctx* c, int nrhs_v) {
+  if (c->items_nrhs == nrhs_v) return EVR_OK;
+  const int nbuf = nbuf_for(c->type, c->D);
+  const int Rmax = 32;
+  long long max_need = 0;
+  std::vector<Item> items;
+  std::vector<float> cost;
+  for (long long t = 0; t < c->nb_SG; ++t) {
+    TermInfo& T = c->terms[t];
+    long long per = (long long)nbuf * T.nq;
+    int r = (int)std::min<long long>(std::min(nrhs_v, Rmax), std::max<long long>(1, c->smem_doubles / per));
+    T.r = r;
+    max_need = std::max(max_need, per * r);
+    double fl = 0;  // cost ~ grid size times the 1-D lengths
+    for (int i = 0; i < c->D; ++i) fl += c->nq_of_l[i * (c->L + 1) + T.l[i]];
+    T.cost = (float)(fl * T.nq);
+    for (int r0 = 0; r0 < nrhs_v; r0 += r) {
+      items.push_back(Item{(int)t, r0});
+      cost.push_back(T.cost * std::min(r, nrhs_v - r0));
+    }
+  }
+  // plain path keeps the term order; the batched path gets a sorted copy
+  std::vector<int> order(items.size());
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+  std::vector<Item> sorted(items.size());
+  for (size_t k = 0; k < order.size(); ++k) sorted[k] = items[order[k]];
+  c->term_item_start.assign(c->nb_SG + 1, 0);
+  for (size_t k = 0; k < items.size(); ++k) c->term_item_start[items[k].term + 1]++;
+  for (long long t = 0; t < c->nb_SG; ++t) c->term_item_start[t + 1] += c->term_item_start[t];
+  size_t need = items.size() * 2;
+  if (need > c->items_cap) {
+    if (c->d_items) cudaFree(c->d_items);
+    c->d_items = nullptr;
+    CUDA_TRY(cudaMalloc(&c->d_items, need * sizeof(Item)));
+    c->items_cap = need;
+  }
+  CUDA_TRY(cudaMemcpy(c->d_items, sorted.data(), sorted.size() * sizeof(Item), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(c->d_items + items.size(), items.data(), items.size() * sizeof(Item), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(c->d_terms, c->terms.data(), c->terms.size() * sizeof(TermInfo), cudaMemcpyHostToDevice));
+  c->n_items = (int)items.size();
+  // global scratch for terms that do not fit in shared memory
+  long long per_cta = max_need > c->smem_doubles ? max_need : 0;
+  if (per_cta > c->scratch_per_cta) {
+    if (c->d_scratch) cudaFree(c->d_scratch);
+    c->d_scratch = nullptr;
+    CUDA_TRY(cudaMalloc(&c->d_scratch, (size_t)per_cta * c->grid * 8));
+    c->scratch_per_cta = per_cta;
+  }
+  c->items_nrhs = nrhs_v;
+  return EVR_OK;
+}
+
+static KParams make_params(evr_sg4_ctx* c, int nrhs_v, int cshift, const double* psi, long long ldpsi,
+                           double* hpsi, long long ldh, double scale) {
+  KParams p;
+  memset(&p, 0, sizeof(p));
+  p.D = c->D;
+  p.Lp1 = c->L + 1;
+  p.nrhs_v = nrhs_v;
+  p.cshift = cshift;
+  p.terms = c->d_terms;
+  p.n_items = c->n_items;
+  p.counter = c->d_counter;
+  p.map = c->d_map;
+  p.mats = c->d_mats;
+  p.mat_off = c->d_mat_off;
+  p.nb_of_l = c->d_nb_of_l;
+  p.nq_of_l = c->d_nq_of_l;
+  p.psi = psi;
+  p.ldpsi = ldpsi;
+  p.hpsi = hpsi;
+  p.ldh = ldh;
+  p.scale = scale;
+  p.V = c->d_V;
+  p.G = c->d_G;
+  p.Jac = c->d_Jac;
+  p.sqRho = c->d_sqRho;
+  p.F2 = c->d_F2;
+  p.F1 = c->d_F1;
+  p.type = c->type;
+  p.nbuf = nbuf_for(c->type, c->D);
+  p.smem_doubles = c->smem_doubles;
+  p.gscratch = c->d_scratch;
+  p.scratch_per_cta = c->scratch_per_cta;
+  return p;
+}
+
+static int hpsi_common(evr_sg4_ctx* c, int nrhs, int cshift, const double* psi, long long ldpsi,
+                       double* hpsi, long long ldh, double E0, double Esc, void* stream, bool plain) {
+  if (!c) return set_error(EVR_ERR_ARG, "hpsi: NULL context");
+  if (!c->have_op) return set_error(EVR_ERR_STATE, "hpsi: set_operator was not called");
+  if (nrhs < 1) return set_error(EVR_ERR_ARG, "hpsi: nrhs=%d (size(Psi)=0 stops the reference)", nrhs);
+  if (!psi || !hpsi) return set_error(EVR_ERR_ARG, "hpsi: NULL vector");
+  if (ldpsi < c->N || ldh < c->N) return set_error(EVR_ERR_ARG, "hpsi: leading dimension < N=%lld", c->N);
+  if (!(Esc != 0.0) || !std::isfinite(Esc) || !std::isfinite(E0))
+    return set_error(EVR_ERR_ARG, "hpsi: Esc must be finite and non-zero");
+  cudaPointerAttributes a1, a2;
+  if (cudaPointerGetAttributes(&a1, psi) != cudaSuccess || cudaPointerGetAttributes(&a2, hpsi) != cudaSuccess ||
+      a1.type != cudaMemoryTypeDevice || a2.type != cudaMemoryTypeDevice) {
+    cudaGetLastError();
+    return set_error(EVR_ERR_ARG, "hpsi: psi and hpsi must be device pointers (use evr_sg4_hpsi_host)");
+  }
+  const int nrhs_v = nrhs << cshift;
+  int rc = build_items(c, nrhs_v);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  const long long ldv_psi = ldpsi << cshift, ldv_h = ldh << cshift;
+  hpsi_init_kernel<<<2 * c->num_sms, 256, 0, s>>>(hpsi, psi, c->N, nrhs_v, cshift, ldv_psi, ldv_h, -E0 / Esc,
+                                                 c->d_counter);
+  CUDA_TRY(cudaGetLastError());
+  KParams p = make_params(c, nrhs_v, cshift, psi, ldv_psi, hpsi, ldv_h, 1.0 / Esc);
+  const size_t smem = (size_t)c->smem_doubles * 8;
+  if (!plain) {
+    p.items = c->d_items;
+    hpsi_batched_kernel<<<c->grid, 256, smem, s>>>(p);
+    CUDA_TRY(cudaGetLastError());
+    c->last_launches = 2;
+  } else {
+    p.items = c->d_items + c->n_items;  // term-ordered list
+    long long launches = 1;
+    for (long long t = 0; t < c->nb_SG; ++t) {
+      int n = c->term_item_start[t + 1] - c->term_item_start[t];
+      p.item_base = c->term_item_start[t];
+      hpsi_plain_kernel<<<n, 256, smem, s>>>(p);
+      ++launches;
+    }
+    CUDA_TRY(cudaGetLastError());
+    c->last_launches = launches;
+  }
+  return EVR_OK;
+}
+
+extern "C" int evr_sg4_hpsi(evr_sg4_ctx* c, int nrhs, const double* psi, long long ldpsi, double* hpsi,
+                            long long ldh, double E0, double Esc, void* stream) {
+  return hpsi_common(c, nrhs, 0, psi, ldpsi, hpsi, ldh, E0, Esc, stream, false);
+}
+
+extern "C" int evr_sg4_hpsi_plain(evr_sg4_ctx* c, int nrhs, const double* psi, long long ldpsi, double* hpsi,
+                                  long long ldh, void* stream) {
+  return hpsi_common(c, nrhs, 0, psi, ldpsi, hpsi, ldh, 0.0, 1.0, stream, true);
+}
+
+extern "C" int evr_sg4_hpsi_cplx(evr_sg4_ctx* c, int nrhs, const double* psi, long long ldpsi, double* hpsi,
+                                 long long ldh, double E0, double Esc, void* stream) {
+  return hpsi_common(c, nrhs, 1, psi, ldpsi, hpsi, ldh, E0, Esc, stream, false);
+}
+
+extern "C" int evr_sg4_hpsi_host(evr_sg4_ctx* c, int nrhs, const double* psi, long long ldpsi, double* hpsi,
+                                 long long ldh, double E0, double Esc) {
+  if (!c) return set_error(EVR_ERR_ARG, "hpsi_host: NULL context");
+  if (nrhs < 1 || !psi || !hpsi || ldpsi < c->N || ldh < c->N)
+    return set_error(EVR_ERR_ARG, "hpsi_host: bad sizes or NULL vectors");
+  size_t n = (size_t)c->N * nrhs;
+  if (2 * n > c->io_cap) {
+    if (c->d_io) cudaFree(c->d_io);
+    c->d_io = nullptr;
+    CUDA_TRY(cudaMalloc(&c->d_io, 2 * n * 8));
+    c->io_cap = 2 * n;
+  }
+  double* dpsi = c->d_io;
+  double* dh = c->d_io + n;
+  CUDA_TRY(cudaMemcpy2DAsync(dpsi, (size_t)c->N * 8, psi, (size_t)ldpsi * 8, (size_t)c->N * 8, nrhs,
+                             cudaMemcpyHostToDevice, 0));
+  int rc = evr_sg4_hpsi(c, nrhs, dpsi, c->N, dh, c->N, E0, Esc, nullptr);
+  if (rc) return rc;
+  CUDA_TRY(cudaMemcpy2DAsync(hpsi, (size_t)ldh * 8, dh, (size_t)c->N * 8, (size_t)c->N * 8, nrhs,
+                             cudaMemcpyDeviceToHost, 0));
+  CUDA_TRY(cudaStreamSynchronize(0));
+  return EVR_OK;
+}
+
+extern "C" int evr_sg4_flops_per_rhs(const evr_sg4_ctx* c, double* flops) {
+  if (!c || !flops) return set_error(EVR_ERR_ARG, "flops: NULL argument");
+  if (!c->have_op) return set_error(EVR_ERR_STATE, "flops: set_operator was not called");
+  const int D = c->D, Lp1 = c->L + 1;
+  double F = 0.0;
+  for (const TermInfo& T : c->terms) {
+    int nb[EVR_MAXD], nq[EVR_MAXD];
+    for (int i = 0; i < D; ++i) {
+      nb[i] = c->nb_of_l[i * Lp1 + T.l[i]];
+      nq[i] = c->nq_of_l[i * Lp1 + T.l[i]];
+    }
+    double f = 0.0;
+    for (int i = 0; i < D; ++i) {  // B->G and G->B
+      double a = 1.0, b = 1.0;
+      for (int j = 0; j < D; ++j) {
+        if (j < i) { a *= nq[j]; b *= nb[j]; }
+        if (j > i) { a *= nb[j]; b *= nq[j]; }
+      }
+      f += 2.0 * nq[i] * nb[i] * (a + b);
+    }
+    double sum_nqi = 0;
+    for (int i = 0; i < D; ++i) sum_nqi += nq[i];
+    const double q = T.nq;
+    if (c->type == 0) {
+      f += q;
+    } else if (c->type == 1) {
+      f += c->d_V ? q : 0.0;
+      for (int i = 0; i < D; ++i)
+        for (int j = i; j < D; ++j)
+          if (c->F2[i * D + j] != 0.0) f += 2.0 * q * (i == j ? nq[i] : nq[i] + nq[j]) + 2.0 * q;
+      for (int i = 0; i < D; ++i)
+        if (c->F1[i] != 0.0) f += 2.0 * q * nq[i] + 2.0 * q;
+    } else {
+      f += 4.0 * q * sum_nqi;                       // D derivative passes, twice
+      f += c->d_G ? 2.0 * D * D * q : 0.0;           // G contraction
+      f += (c->d_Jac ? 2.0 * D * q : 0.0) + (c->d_sqRho ? 2.0 * q : 0.0);
+      f += (c->d_V ? q : 0.0) + 4.0 * q;            // V.x and the final combination
+    }
+    f += 2.0 * T.nb;                                // weighted scatter
+    F += f;
+  }
+  *flops = F;
+  return EVR_OK;
+}
+
+extern "C" int evr_sg4_last_launches(const evr_sg4_ctx* c, long long* n) {
+  if (!c || !n) return set_error(EVR_ERR_ARG, "last_launches: NULL argument");
+  *n = c->last_launches;
+  return EVR_OK;
+}
+
+extern "C" int evr_probe_fp64_peak(double* tflops) {
+  if (!tflops) return set_error(EVR_ERR_ARG, "probe: NULL argument");
+  int dev = 0, sms = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int blocks = 4 * sms, threads = 256, iters = 2048;
+  double* d = nullptr;
+  CUDA_TRY(cudaMalloc(&d, sizeof(double) * blocks * threads));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  dfma_peak_kernel<<<blocks, threads>>>(d, 64, 1.0000001, 1e-9);
+  float best = 1e30f;
+  for (int rep = 0; rep < 3; ++rep) {
+    cudaEventRecord(e0);
+    dfma_peak_kernel<<<blocks, threads>>>(d, iters, 1.0000001, 1e-9);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    best = std::min(best, ms);
+  }
+  cudaError_t e = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(d);
+  if (e != cudaSuccess) return set_error(EVR_ERR_CUDA, "probe: %s", cudaGetErrorString(e));
+  *tflops = 2.0 * 8 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
+  return EVR_OK;
+}

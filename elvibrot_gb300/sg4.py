@@ -1,0 +1,321 @@
+"""Host-side mirror of ElVibRot's SG4 operator interface over libevrsg4.so.
+
+The names follow the reference:
+
+* :class:`SG4Basis` -- ``para_Op%BasisnD`` after ``RecSparseGrid_ForDP_type4``
+  (SRC/sub_Basis/sub_quadra_SparseBasis.f90:922) for HO/Hermite modes.
+* :class:`ParamOp` -- ``TYPE(param_Op)`` (SRC/sub_Operator/sub_module_SetOp.f90:59)
+  restricted to what the SG4 action reads: ``type_Op`` (0, 1 or 10) and the
+  cached operator grids (``OpGrid``).
+* :func:`sub_TabOpPsi`, :func:`sub_OpPsi`, :func:`sub_scaledOpPsi` -- the
+  reference's entry points (SRC/sub_Operator/sub_OpPsi.f90:705, :180, :2821)
+  for SG4 bases: they return ``OpPsi`` with the packed layout of ``RvecB``
+  (column-major N x nrhs), complex vectors going through the real operator on
+  their real and imaginary parts like ``CplxPsi_TO_RCpsi``.
+
+Vectors are torch tensors: CUDA tensors run on the device in place; host
+(numpy or CPU torch) vectors go through ``evr_sg4_hpsi_host`` (copies in and
+out).  There is no CPU fallback: without the CUDA library every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _build
+
+EVR_OK = 0
+_ERRORS = {1: "EVR_ERR_ARG", 2: "EVR_ERR_CUDA", 3: "EVR_ERR_ALLOC", 4: "EVR_ERR_STATE",
+           5: "EVR_ERR_TIMEOUT", 6: "EVR_ERR_NUMERIC"}
+
+
+class EVRError(RuntimeError):
+    """A C-ABI call returned a non-zero status (the reference would STOP)."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{_ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def lib():
+    """Loads (building if needed) the in-tree libevrsg4.so."""
+    global _lib
+    if _lib is None:
+        path = _build.LIB
+        if not os.path.exists(path) or not _build.up_to_date():
+            _build.build()
+        L = ctypes.CDLL(path)
+        _declare(L)
+        _lib = L
+    return _lib
+
+
+class Desc(ctypes.Structure):
+    _fields_ = [("D", ctypes.c_int), ("L", ctypes.c_int), ("LB", ctypes.c_int), ("nb0", ctypes.c_int),
+                ("nb_of_l", ctypes.POINTER(ctypes.c_int)), ("nq_of_l", ctypes.POINTER(ctypes.c_int)),
+                ("x", ctypes.POINTER(ctypes.c_double)), ("RGB", ctypes.POINTER(ctypes.c_double)),
+                ("RBGwrho", ctypes.POINTER(ctypes.c_double)), ("d1GG", ctypes.POINTER(ctypes.c_double)),
+                ("d2GG", ctypes.POINTER(ctypes.c_double)), ("nb_SG", ctypes.c_longlong),
+                ("tab_l", ctypes.POINTER(ctypes.c_int)), ("weight", ctypes.POINTER(ctypes.c_double)),
+                ("map", ctypes.POINTER(ctypes.c_int)), ("N", ctypes.c_longlong)]
+
+
+class OpDesc(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_int), ("V_grid", ctypes.POINTER(ctypes.c_double)),
+                ("V_nterms", ctypes.c_int), ("V_coef", ctypes.POINTER(ctypes.c_double)),
+                ("V_expo", ctypes.POINTER(ctypes.c_int)), ("G_grid", ctypes.POINTER(ctypes.c_double)),
+                ("G0", ctypes.POINTER(ctypes.c_double)), ("G1", ctypes.POINTER(ctypes.c_double)),
+                ("Jac_grid", ctypes.POINTER(ctypes.c_double)), ("sqRho_grid", ctypes.POINTER(ctypes.c_double)),
+                ("F2", ctypes.POINTER(ctypes.c_double)), ("F1", ctypes.POINTER(ctypes.c_double))]
+
+
+def _declare(L):
+    vp, ip, dp, ll = ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double), ctypes.c_longlong
+    L.evr_sg4_last_error.restype = ctypes.c_char_p
+    sig = {
+        "evr_sg4_desc_sizes": [ctypes.POINTER(Desc), ctypes.POINTER(ll)],
+        "evr_sg4_basis_build_ho": [ctypes.c_int] * 7 + [dp, dp, ctypes.POINTER(vp)],
+        "evr_sg4_basis_desc": [vp, ctypes.POINTER(Desc)],
+        "evr_sg4_basis_grid_points": [vp, dp],
+        "evr_sg4_create": [ctypes.POINTER(Desc), ctypes.POINTER(vp)],
+        "evr_sg4_destroy": [vp],
+        "evr_sg4_set_operator": [vp, ctypes.POINTER(OpDesc)],
+        "evr_sg4_hpsi": [vp, ctypes.c_int, vp, ll, vp, ll, ctypes.c_double, ctypes.c_double, vp],
+        "evr_sg4_hpsi_plain": [vp, ctypes.c_int, vp, ll, vp, ll, vp],
+        "evr_sg4_hpsi_cplx": [vp, ctypes.c_int, vp, ll, vp, ll, ctypes.c_double, ctypes.c_double, vp],
+        "evr_sg4_hpsi_host": [vp, ctypes.c_int, vp, ll, vp, ll, ctypes.c_double, ctypes.c_double],
+        "evr_sg4_flops_per_rhs": [vp, dp],
+        "evr_sg4_last_launches": [vp, ctypes.POINTER(ll)],
+        "evr_probe_fp64_peak": [dp],
+    }
+    for name, args in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = ctypes.c_int
+    L.evr_sg4_basis_free.argtypes = [vp]
+    L.evr_sg4_basis_free.restype = None
+
+
+def check(rc: int):
+    if rc != EVR_OK:
+        raise EVRError(rc, lib().evr_sg4_last_error().decode())
+
+
+def _dp(a):
+    if a is None:
+        return ctypes.cast(None, ctypes.POINTER(ctypes.c_double))
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ip(a):
+    if a is None:
+        return ctypes.cast(None, ctypes.POINTER(ctypes.c_int))
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+
+class SG4Basis:
+    """SG4 basis of D harmonic-oscillator modes (nb(l) = A_nb + B_nb l, nq(l) = A_nq + B_nq l)."""
+
+    def __init__(self, D: int, L: int, LB: Optional[int] = None, A_nb: int = 1, B_nb: int = 1,
+                 A_nq: int = 2, B_nq: int = 1, Q0: Optional[Sequence[float]] = None,
+                 scaleQ: Optional[Sequence[float]] = None):
+        self.D, self.L = int(D), int(L)
+        self.LB = self.L if LB is None else int(LB)
+        self.A_nb, self.B_nb, self.A_nq, self.B_nq = A_nb, B_nb, A_nq, B_nq
+        self.Q0 = np.zeros(D) if Q0 is None else np.ascontiguousarray(Q0, dtype=np.float64)
+        self.scaleQ = np.ones(D) if scaleQ is None else np.ascontiguousarray(scaleQ, dtype=np.float64)
+        h = ctypes.c_void_p()
+        check(lib().evr_sg4_basis_build_ho(self.D, self.L, self.LB, A_nb, B_nb, A_nq, B_nq,
+                                           _dp(self.Q0), _dp(self.scaleQ), ctypes.byref(h)))
+        self._h = h
+        self.desc = Desc()
+        check(lib().evr_sg4_basis_desc(self._h, ctypes.byref(self.desc)))
+        z = (ctypes.c_longlong * 8)()
+        check(lib().evr_sg4_desc_sizes(ctypes.byref(self.desc), z))
+        self.N, self.nb_SG, self.sum_nb, self.sum_nq, self.max_nb, self.max_nq = [int(v) for v in z[:6]]
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.evr_sg4_basis_free(self._h)
+            self._h = None
+
+    def grid_points(self) -> np.ndarray:
+        Q = np.zeros(self.sum_nq * self.D)
+        check(lib().evr_sg4_basis_grid_points(self._h, _dp(Q)))
+        return Q.reshape(self.sum_nq, self.D)
+
+    def tables(self):
+        """(tab_l[nb_SG,D], WeightSG[nb_SG], tab_iB_OF_SRep_TO_iB[sum_nb]) as numpy copies."""
+        d = self.desc
+        tab_l = np.ctypeslib.as_array(d.tab_l, shape=(self.nb_SG * self.D,)).reshape(self.nb_SG, self.D).copy()
+        w = np.ctypeslib.as_array(d.weight, shape=(self.nb_SG,)).copy()
+        m = np.ctypeslib.as_array(d.map, shape=(self.sum_nb,)).copy()
+        return tab_l, w, m
+
+    def basis1d(self, mode: int, l: int):
+        """1-D matrices of (mode, level): dict x, RGB (nq x nb), RBGwrho (nb x nq), d1GG, d2GG."""
+        d = self.desc
+        nbl = np.ctypeslib.as_array(d.nb_of_l, shape=(self.D * (self.L + 1),))
+        nql = np.ctypeslib.as_array(d.nq_of_l, shape=(self.D * (self.L + 1),))
+        k = mode * (self.L + 1) + l
+        ox = int(nql[:k].sum())
+        om = int((nql[:k] * nbl[:k]).sum())
+        og = int((nql[:k] ** 2).sum())
+        nb, nq = int(nbl[k]), int(nql[k])
+        arr = lambda p, o, n: np.ctypeslib.as_array(p, shape=(o + n,))[o:o + n].copy()
+        return dict(x=arr(d.x, ox, nq), RGB=arr(d.RGB, om, nq * nb).reshape(nb, nq).T,
+                    RBGwrho=arr(d.RBGwrho, om, nq * nb).reshape(nq, nb).T,
+                    d1GG=arr(d.d1GG, og, nq * nq).reshape(nq, nq).T,
+                    d2GG=arr(d.d2GG, og, nq * nq).reshape(nq, nq).T)
+
+
+@dataclass
+class Polynomial:
+    """sum_t coef[t] prod_i Q_i**expo[t, i] (raw coordinates Q)."""
+    coef: np.ndarray
+    expo: np.ndarray
+
+    def __call__(self, Q: np.ndarray) -> np.ndarray:
+        kmax = int(self.expo.max()) if len(self.expo) else 0
+        pw = [np.ones_like(Q)]
+        for _ in range(kmax):
+            pw.append(pw[-1] * Q)
+        out = np.zeros(Q.shape[0])
+        for c, e in zip(self.coef, self.expo):
+            t = np.full(Q.shape[0], c)
+            for i in np.nonzero(e)[0]:
+                t *= pw[e[i]][:, i]
+            out += t
+        return out
+
+
+class ParamOp:
+    """SG4 operator on the GPU (param_Op with its Save_MemGrid grids).
+
+    type_op 0 : V;  1 : V + sum F2_ij d_i d_j + sum F1_i d_i (constant F);
+    10 : -1/2 sum d_i Jac G_ji d_j s / (Jac s) + V with G grid or affine G(Q).
+    """
+
+    def __init__(self, basis: SG4Basis, type_op: int, V: Optional[np.ndarray] = None,
+                 V_poly: Optional[Polynomial] = None, G: Optional[np.ndarray] = None,
+                 G0: Optional[np.ndarray] = None, G1: Optional[np.ndarray] = None,
+                 Jac: Optional[np.ndarray] = None, sqRho: Optional[np.ndarray] = None,
+                 F2: Optional[np.ndarray] = None, F1: Optional[np.ndarray] = None):
+        self.basis = basis
+        self.type_op = int(type_op)
+        h = ctypes.c_void_p()
+        check(lib().evr_sg4_create(ctypes.byref(basis.desc), ctypes.byref(h)))
+        self._h = h
+        self.set_operator(V=V, V_poly=V_poly, G=G, G0=G0, G1=G1, Jac=Jac, sqRho=sqRho, F2=F2, F1=F1)
+
+    def set_operator(self, V=None, V_poly=None, G=None, G0=None, G1=None, Jac=None, sqRho=None, F2=None, F1=None):
+        D = self.basis.D
+        c = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float64).ravel()
+        keep = dict(V=c(V), G=c(G), G0=c(G0), G1=c(G1), Jac=c(Jac), sqRho=c(sqRho), F2=c(F2), F1=c(F1))
+        coef = expo = None
+        nterms = 0
+        if V_poly is not None and V is None:
+            coef = np.ascontiguousarray(V_poly.coef, dtype=np.float64)
+            expo = np.ascontiguousarray(V_poly.expo, dtype=np.int32).reshape(-1, D)
+            nterms = len(coef)
+        op = OpDesc(self.type_op, _dp(keep["V"]), nterms, _dp(coef), _ip(expo), _dp(keep["G"]),
+                    _dp(keep["G0"]), _dp(keep["G1"]), _dp(keep["Jac"]), _dp(keep["sqRho"]),
+                    _dp(keep["F2"]), _dp(keep["F1"]))
+        check(lib().evr_sg4_set_operator(self._h, ctypes.byref(op)))
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.evr_sg4_destroy(self._h)
+            self._h = None
+
+    @property
+    def flops_per_rhs(self) -> float:
+        f = ctypes.c_double()
+        check(lib().evr_sg4_flops_per_rhs(self._h, ctypes.byref(f)))
+        return f.value
+
+    @property
+    def last_launches(self) -> int:
+        n = ctypes.c_longlong()
+        check(lib().evr_sg4_last_launches(self._h, ctypes.byref(n)))
+        return n.value
+
+    # -- device-pointer calls (torch CUDA tensors, column-major N x nrhs) --
+    def hpsi_dev(self, psi, out, E0: float = 0.0, Esc: float = 1.0, stream: int = 0, plain: bool = False):
+        import torch
+        N = self.basis.N
+        if psi.dtype not in (torch.float64, torch.complex128) or not psi.is_cuda:
+            raise EVRError(1, "psi must be a CUDA float64/complex128 tensor")
+        cplx = psi.dtype == torch.complex128
+        P = psi if psi.dim() == 2 else psi.unsqueeze(0)   # (nrhs, N) rows = columns of RvecB
+        O = out if out.dim() == 2 else out.unsqueeze(0)
+        if P.shape[-1] != N or O.shape != P.shape or not P.is_contiguous() or not O.is_contiguous():
+            raise EVRError(1, f"psi/out must be contiguous (nrhs, {N}) tensors of equal shape")
+        nrhs = P.shape[0]
+        if plain:
+            if cplx or E0 != 0.0 or Esc != 1.0:
+                raise EVRError(1, "the plain per-term path takes real psi with E0=0, Esc=1")
+            check(lib().evr_sg4_hpsi_plain(self._h, nrhs, P.data_ptr(), N, O.data_ptr(), N, stream))
+        elif cplx:
+            check(lib().evr_sg4_hpsi_cplx(self._h, nrhs, P.data_ptr(), N, O.data_ptr(), N, E0, Esc, stream))
+        else:
+            check(lib().evr_sg4_hpsi(self._h, nrhs, P.data_ptr(), N, O.data_ptr(), N, E0, Esc, stream))
+        return out
+
+    def hpsi_host(self, psi: np.ndarray, E0: float = 0.0, Esc: float = 1.0) -> np.ndarray:
+        """psi (N,) or (N, nrhs) host float64; returns the same shape (copies in/out)."""
+        N = self.basis.N
+        a = np.asarray(psi, dtype=np.float64)
+        one = a.ndim == 1
+        P = np.asfortranarray(a.reshape(N, -1))
+        H = np.zeros_like(P, order="F")
+        check(lib().evr_sg4_hpsi_host(self._h, P.shape[1], P.ctypes.data, N, H.ctypes.data, N, E0, Esc))
+        return H[:, 0] if one else H
+
+
+def sub_TabOpPsi(Psi, para_Op: ParamOp, E0: float = 0.0, Esc: float = 1.0):
+    """OpPsi(:) for a block of vectors (sub_OpPsi.f90:705 -> sub_OpPsi_SG4.f90:681).
+
+    ``Psi``: CUDA tensor (nrhs, N) float64/complex128 -> CUDA tensor; or a host
+    array (N,) / (N, nrhs) float64 -> host array.  Raises EVRError (the
+    reference STOPs) on empty input or inconsistent sizes.
+    """
+    try:
+        import torch
+        is_t = isinstance(Psi, torch.Tensor)
+    except ImportError:
+        is_t = False
+    if is_t and Psi.is_cuda:
+        if Psi.numel() == 0:
+            raise EVRError(1, "size(Psi) = 0")
+        out = torch.empty_like(Psi)
+        return para_Op.hpsi_dev(Psi.contiguous(), out, E0=E0, Esc=Esc)
+    a = Psi.cpu().numpy() if is_t else np.asarray(Psi)
+    if a.size == 0:
+        raise EVRError(1, "size(Psi) = 0")
+    if np.iscomplexobj(a):
+        return para_Op.hpsi_host(a.real, E0, Esc) + 1j * para_Op.hpsi_host(a.imag, 0.0 if E0 == 0 else E0, Esc)
+    return para_Op.hpsi_host(a, E0, Esc)
+
+
+def sub_OpPsi(Psi, para_Op: ParamOp):
+    """OpPsi for one vector (sub_OpPsi.f90:180)."""
+    return sub_TabOpPsi(Psi, para_Op)
+
+
+def sub_scaledOpPsi(Psi, para_Op: ParamOp, E0: float, Esc: float):
+    """(H Psi - E0 Psi) / Esc (sub_OpPsi.f90:2821-2864), fused into the H.psi launch."""
+    return sub_TabOpPsi(Psi, para_Op, E0=E0, Esc=Esc)
+
+
+def fp64_peak_tflops() -> float:
+    t = ctypes.c_double()
+    check(lib().evr_probe_fp64_peak(ctypes.byref(t)))
+    return t.value

@@ -1,0 +1,184 @@
+/*
+ * evr_sg4.h -- C ABI of the GB300 (sm_103a) Smolyak type-4 (SG4) H.psi.
+ *
+ * Drop-in boundary for ElVibRot's operator action on an SG4 basis:
+ *
+ *   SUBROUTINE sub_TabOpPsi(TabPsi, TabOpPsi, para_Op, ...)
+ *       SRC/sub_Operator/sub_OpPsi.f90:705, SG4 branch :864-884
+ *   -> SUBROUTINE sub_TabOpPsi_FOR_SGtype4(Psi, OpPsi, para_Op)
+ *       SRC/sub_Operator/sub_OpPsi_SG4.f90:681-977
+ *
+ * Every entry point returns an int status (EVR_OK = 0) and never exits,
+ * aborts or traps; evr_sg4_last_error() gives the message of the last
+ * failure on the calling thread.  No CUDA or torch types appear in the
+ * signatures: streams are passed as void* (a cudaStream_t, NULL = legacy
+ * default stream).  Vectors are column-major N x nrhs (Fortran order) with a
+ * leading dimension, exactly the packed layout of param_psi%RvecB
+ * (SRC/sub_WP/sub_module_psi_set_alloc.f90:56-169): index (ib0-1)*N + nDI,
+ * nDI enumerating nDindB type 5p.  The library never frees caller memory.
+ * A context is single-stream and not thread-safe; distinct contexts are
+ * independent.
+ */
+#ifndef EVR_SG4_H
+#define EVR_SG4_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EVR_OK 0
+#define EVR_ERR_ARG 1      /* invalid argument / size (the reference STOPs) */
+#define EVR_ERR_CUDA 2     /* a CUDA runtime call failed */
+#define EVR_ERR_ALLOC 3    /* device or host allocation failed */
+#define EVR_ERR_STATE 4    /* call order (e.g. hpsi before set_operator) */
+#define EVR_ERR_TIMEOUT 5  /* a bounded device wait gave up */
+#define EVR_ERR_NUMERIC 6  /* non-finite input or diverging iteration */
+
+typedef struct evr_sg4_basis evr_sg4_basis; /* host-side tables */
+typedef struct evr_sg4_ctx evr_sg4_ctx;     /* device-side operator */
+
+/* ------------------------------------------------------------------------
+ * Basis descriptor: the SG4 tables as ElVibRot holds them after
+ * RecSparseGrid_ForDP_type4 (SRC/sub_Basis/sub_quadra_SparseBasis.f90:922).
+ * A Fortran caller fills it from para_Op%BasisnD:
+ *   nb_of_l/nq_of_l  <- tab_basisPrimSG(l,i)%nb / nq
+ *   x                <- tab_basisPrimSG(l,i)%x(1,:)
+ *   RGB              <- tab_basisPrimSG(l,i)%dnRGB%d0      (nq x nb)
+ *   RBGwrho          <- tab_basisPrimSG(l,i)%dnRBGwrho%d0  (nb x nq)
+ *   d1GG, d2GG       <- tab_basisPrimSG(l,i)%dnRGG%d1, %d2 (nq x nq)
+ *   tab_l            <- para_SGType2%nDind_SmolyakRep%Tab_nDval (transposed)
+ *   weight           <- BasisnD%WeightSG
+ *   map              <- para_SGType2%tab_iB_OF_SRep_TO_iB
+ *   N                <- BasisnD%nDindB%Max_nDI
+ * Per-(mode,level) arrays are concatenated mode-major, level-minor
+ * (i*(L+1)+l); matrices column-major.  Terms are in nDind_SmolyakRep order;
+ * inside a term the DP index runs mode 1 fastest.
+ * ---------------------------------------------------------------------- */
+typedef struct {
+  int D;                    /* number of modes */
+  int L;                    /* Smolyak grid level (L_SparseGrid) */
+  int LB;                   /* basis level (L_SparseBasis) */
+  int nb0;                  /* channels (only 1 is supported) */
+  const int* nb_of_l;       /* [D*(L+1)] */
+  const int* nq_of_l;       /* [D*(L+1)] */
+  const double* x;          /* sum over (i,l) of nq */
+  const double* RGB;        /* sum of nq*nb */
+  const double* RBGwrho;    /* sum of nb*nq */
+  const double* d1GG;       /* sum of nq*nq */
+  const double* d2GG;       /* sum of nq*nq */
+  long long nb_SG;          /* number of Smolyak terms */
+  const int* tab_l;         /* [nb_SG*D] term-major */
+  const double* weight;     /* [nb_SG] */
+  const int* map;           /* [sum_nb], 1-based packed index, 0 = skipped */
+  long long N;              /* packed basis size */
+} evr_sg4_desc;
+
+/* Sizes derived from a descriptor: out[0..7] = N, nb_SG, sum_nb, sum_nq,
+ * max_nb_term, max_nq_term, D, L. */
+int evr_sg4_desc_sizes(const evr_sg4_desc* d, long long* out);
+
+/* ------------------------------------------------------------------------
+ * Host builder for harmonic-oscillator (Hermite) primitive bases.
+ * Restates RecSparseGrid_ForDP_type4 (sub_quadra_SparseBasis.f90:922-1434)
+ * with basis "HO"/"Hm" per mode: nb(l) = A_nb + B_nb*l, nq(l) = A_nq + B_nq*l
+ * (L_TO_n_type 0, expo 1), Gauss-Hermite grids (sub_quadra_herm.f90:48),
+ * scaling x -> Q0 + x/scaleQ (sub_module_basis.f90:1499), dnRGG through the
+ * pseudo-inverse of dnRGB%d0 (sub_module_basis.f90:2048), nDindB type 5p
+ * and nDind_SmolyakRep type -5 (Ext_Lib/nDindex_loc), WeightSG
+ * (sub_module_param_SGType2.f90:770) and tab_iB_OF_SRep_TO_iB
+ * (sub_module_basis_BtoG_GtoB_SG4.f90:630).  Q0/scaleQ may be NULL (0, 1).
+ * ---------------------------------------------------------------------- */
+int evr_sg4_basis_build_ho(int D, int L, int LB, int A_nb, int B_nb, int A_nq, int B_nq,
+                           const double* Q0, const double* scaleQ, evr_sg4_basis** out);
+/* Fills *d with pointers into the basis' own storage (valid until free). */
+int evr_sg4_basis_desc(const evr_sg4_basis* b, evr_sg4_desc* d);
+/* Coordinates of every term grid point: Q[sum_nq*D], point-major
+ * (Rec_Qact_SG4_with_Tab_iq, sub_module_basis.f90:3979). */
+int evr_sg4_basis_grid_points(const evr_sg4_basis* b, double* Q);
+void evr_sg4_basis_free(evr_sg4_basis* b);
+
+/* ------------------------------------------------------------------------
+ * Device context.  Copies the descriptor's tables to the device.
+ * ---------------------------------------------------------------------- */
+int evr_sg4_create(const evr_sg4_desc* d, evr_sg4_ctx** out);
+int evr_sg4_destroy(evr_sg4_ctx* c);
+
+/* ------------------------------------------------------------------------
+ * Operator.  Replaces param_Op%type_Op with its cached grids (OpGrid,
+ * get_OpGrid_type0/1/10_OF_ONEDP_FOR_SG4, sub_OpPsi_SG4.f90:2536-3319):
+ *   type 0  : y = V.x                                           (CASE 0 :1446)
+ *   type 1  : y = V.x + sum_{i<=j} F2_ij d_i d_j x + sum_i F1_i d_i x
+ *             (d_i d_i through dnRGG%d2, others through %d1)     (CASE 1 :1488)
+ *   type 10 : y = -1/2 sum_i d_i(Jac sum_j G_ji d_j(s x)) / (Jac s) + V.x,
+ *             s = sqRhoOVERJac                                  (CASE 10 :1546)
+ * V is a grid (sum_nq values, OpGrid%Grid layout, terms concatenated) or a
+ * polynomial sum_t coef_t prod_i Q_i^expo_ti evaluated on the device.
+ * G (type 10) is a grid GGiq(iq,j,i) per term, concatenated (sum_nq*D*D),
+ * or the affine form G_ij(Q) = G0_ij + sum_k G1_ijk Q_k ([D*D], [D*D*D],
+ * row-major ijk); neither = identity.  Jac / sqRho grids: NULL = 1.
+ * F2 [D*D] row-major (entries i<=j used) and F1 [D]: constant coefficients.
+ * All pointers are host pointers; the fields are built once on the device
+ * (the equivalent of Save_MemGrid).
+ * ---------------------------------------------------------------------- */
+typedef struct {
+  int type;
+  const double* V_grid;
+  int V_nterms;
+  const double* V_coef;     /* [V_nterms] */
+  const int* V_expo;        /* [V_nterms*D] */
+  const double* G_grid;
+  const double* G0;
+  const double* G1;
+  const double* Jac_grid;
+  const double* sqRho_grid;
+  const double* F2;
+  const double* F1;
+} evr_sg4_op_desc;
+
+int evr_sg4_set_operator(evr_sg4_ctx* c, const evr_sg4_op_desc* op);
+
+/* ------------------------------------------------------------------------
+ * H.psi on device pointers (batched persistent kernel, the fast path):
+ *   hpsi(:,r) = (H psi(:,r) - E0 psi(:,r)) / Esc,  r = 1..nrhs
+ * E0 = 0, Esc = 1 is sub_TabOpPsi; other values are sub_scaledOpPsi
+ * (sub_OpPsi.f90:2821-2864).  psi and hpsi must not overlap.
+ * ---------------------------------------------------------------------- */
+int evr_sg4_hpsi(evr_sg4_ctx* c, int nrhs, const double* psi, long long ldpsi, double* hpsi,
+                 long long ldh, double E0, double Esc, void* stream);
+
+/* Same result through one kernel launch per Smolyak term (the "plain"
+ * per-term GPU path, kept as the baseline the batched kernel is measured
+ * against; it mirrors the reference's per-term loop). */
+int evr_sg4_hpsi_plain(evr_sg4_ctx* c, int nrhs, const double* psi, long long ldpsi,
+                       double* hpsi, long long ldh, void* stream);
+
+/* Complex psi, interleaved complex128 (CvecB): the real operator applied to
+ * the real and imaginary parts, as sub_PrimOpPsi's SG4 branch does with
+ * CplxPsi_TO_RCpsi (sub_OpPsi.f90:395-412). ld in complex elements. */
+int evr_sg4_hpsi_cplx(evr_sg4_ctx* c, int nrhs, const double* psi, long long ldpsi, double* hpsi,
+                      long long ldh, double E0, double Esc, void* stream);
+
+/* Host-pointer variant: copies psi to the device, runs evr_sg4_hpsi,
+ * copies the result back and synchronises (what a Fortran caller holding
+ * RvecB in host memory calls). */
+int evr_sg4_hpsi_host(evr_sg4_ctx* c, int nrhs, const double* psi, long long ldpsi, double* hpsi,
+                      long long ldh, double E0, double Esc);
+
+/* Algorithmic FP64 operation count of one H.psi per right-hand side for the
+ * current operator (flop, counted from the term sizes). */
+int evr_sg4_flops_per_rhs(const evr_sg4_ctx* c, double* flops);
+
+/* Number of kernel launches the last hpsi call issued. */
+int evr_sg4_last_launches(const evr_sg4_ctx* c, long long* n);
+
+/* Message of the last failure on the calling thread ("" if none). */
+const char* evr_sg4_last_error(void);
+
+/* Measured FP64 FMA throughput of the current device in TFLOP/s (a short
+ * in-bounds DFMA loop; used as the roofline denominator). */
+int evr_probe_fp64_peak(double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

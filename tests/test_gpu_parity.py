@@ -1,0 +1,183 @@
+"""GPU parity of the SG4 H.psi kernels (through the C ABI) against the CPU oracle.
+
+Tolerance: the benchmark's bar of 1e-12 maximum relative error, measured
+block-wise as max|H_gpu - H_oracle| / max|H_oracle| (FP64 throughout; the
+GPU reorders sums and uses FMA, so results are not bitwise identical).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from elvibrot_gb300 import EVRError, ParamOp, Polynomial, SG4Basis, sub_scaledOpPsi, sub_TabOpPsi
+from elvibrot_gb300.configs import make_model, random_psi
+from oracle.oracle import OracleSG4
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def need_cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def rel_err(a, b):
+    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+
+def gpu_apply(op, psi, **kw):
+    P = torch.from_numpy(np.ascontiguousarray(psi.T)).cuda()
+    H = sub_TabOpPsi(P, op, **kw)
+    torch.cuda.synchronize()
+    return H.cpu().numpy().T
+
+
+def oracle_for(model):
+    O = OracleSG4(model.D, model.L, model.L, 1, 1, 2, 1, scaleQ=model.scaleQ)
+    Q = O.grid_points()
+    V = model.V(Q)
+    kw = dict(V=V)
+    if model.type_op == 1:
+        kw.update(type_op=1, F2=model.F2.ravel())
+    else:
+        tab_l = O.tables()[0]
+        nq = np.prod(tab_l + 2, axis=1)
+        kw.update(type_op=10, G=model.G_grid(Q, nq))
+    return O, kw
+
+
+@pytest.mark.parametrize("D,L,type_op,nrhs", [(3, 6, 1, 1), (3, 6, 1, 5), (4, 5, 10, 7), (6, 4, 10, 3),
+                                              (5, 5, 1, 4), (2, 9, 10, 2)])
+def test_hpsi_matches_oracle(D, L, type_op, nrhs):
+    need_cuda()
+    m = make_model(D, L, type_op, 1234 + D * 10 + L)
+    op = m.operator()
+    psi = random_psi(op.basis.N, nrhs, 99)
+    O, kw = oracle_for(m)
+    ref = O.hpsi(psi, **kw)
+    got = gpu_apply(op, psi)
+    assert rel_err(got, ref) <= TOL
+    assert op.last_launches == 2
+
+
+def test_type0_and_fields_from_grids():
+    need_cuda()
+    D, L = 4, 5
+    b = SG4Basis(D, L, scaleQ=np.full(D, 0.4))
+    O = OracleSG4(D, L, L, 1, 1, 2, 1, scaleQ=np.full(D, 0.4))
+    rng = np.random.default_rng(5)
+    V = rng.normal(size=b.sum_nq)
+    psi = random_psi(b.N, 3, 5)
+    op0 = ParamOp(b, 0, V=V)
+    assert rel_err(gpu_apply(op0, psi), O.hpsi(psi, type_op=0, V=V)) <= TOL
+    # type 10 with explicit G, Jac and sqRho grids (GGiq layout)
+    G = rng.normal(size=b.sum_nq * D * D) * 0.1
+    Jac = rng.uniform(0.5, 2.0, size=b.sum_nq)
+    sq = rng.uniform(0.5, 2.0, size=b.sum_nq)
+    op10 = ParamOp(b, 10, V=V, G=G, Jac=Jac, sqRho=sq)
+    ref = O.hpsi(psi, type_op=10, V=V, G=G, Jac=Jac, sqRho=sq)
+    assert rel_err(gpu_apply(op10, psi), ref) <= TOL
+    # type 1 with off-diagonal and first-derivative terms
+    F2 = np.triu(rng.normal(size=(D, D)))
+    F1 = rng.normal(size=D)
+    op1 = ParamOp(b, 1, V=V, F2=F2, F1=F1)
+    ref = O.hpsi(psi, type_op=1, V=V, F2=F2.ravel(), F1=F1)
+    assert rel_err(gpu_apply(op1, psi), ref) <= TOL
+
+
+def test_plain_equals_batched_and_scaled_and_complex():
+    need_cuda()
+    m = make_model(4, 6, 10, 77)
+    op = m.operator()
+    N = op.basis.N
+    psi = random_psi(N, 4, 3)
+    P = torch.from_numpy(np.ascontiguousarray(psi.T)).cuda()
+    hb = torch.empty_like(P)
+    hp = torch.empty_like(P)
+    op.hpsi_dev(P, hb)
+    op.hpsi_dev(P, hp, plain=True)
+    assert op.last_launches == 1 + op.basis.nb_SG
+    torch.cuda.synchronize()
+    assert rel_err(hp.cpu().numpy(), hb.cpu().numpy()) <= TOL
+    # (H - E0)/Esc fused
+    E0, Esc = 0.37, 2.5
+    hs = sub_scaledOpPsi(P, op, E0, Esc)
+    want = (hb - E0 * P) / Esc
+    assert rel_err(hs.cpu().numpy(), want.cpu().numpy()) <= TOL
+    # complex psi = real operator on Re and Im
+    pc = random_psi(N, 3, 4, complex_=True)
+    Pc = torch.from_numpy(np.ascontiguousarray(pc.T)).cuda()
+    hc = sub_TabOpPsi(Pc, op).cpu().numpy().T
+    hr = gpu_apply(op, np.ascontiguousarray(pc.real))
+    hi = gpu_apply(op, np.ascontiguousarray(pc.imag))
+    assert rel_err(hc, hr + 1j * hi) <= TOL
+    # host-pointer path
+    hh = op.hpsi_host(psi)
+    assert rel_err(hh, hb.cpu().numpy().T) <= TOL
+
+
+def test_large_terms_use_global_scratch():
+    need_cuda()
+    # a 7-D L=9 type-10 basis has terms whose D+4 work arrays exceed shared memory
+    m = make_model(7, 9, 10, 4242)
+    op = m.operator()
+    assert op.basis.max_nq * (7 + 4) > 110 * 1024 // 8
+    psi = random_psi(op.basis.N, 2, 8)
+    O, kw = oracle_for(m)
+    assert rel_err(gpu_apply(op, psi), O.hpsi(psi, **kw)) <= TOL
+
+
+def test_benchmark_6d_workload_full_size():
+    need_cuda()
+    # 6-D L=8, Q-dependent G, 20 right-hand sides (the benchmark workload)
+    m = make_model(6, 8, 10, 20261204)
+    op = m.operator()
+    assert (op.basis.N, op.basis.nb_SG, op.basis.sum_nq) == (3003, 2975, 1953127)
+    psi = random_psi(op.basis.N, 20, 20261204)
+    O, kw = oracle_for(m)
+    ref = O.hpsi(psi, **kw)
+    got = gpu_apply(op, psi)
+    assert rel_err(got, ref) <= TOL
+    # linearity: H(a x + b y) = a Hx + b Hy
+    comb = gpu_apply(op, 0.3 * psi[:, :1] - 1.7 * psi[:, 1:2])
+    assert rel_err(comb, 0.3 * got[:, :1] - 1.7 * got[:, 1:2]) <= TOL
+
+
+def test_henon_heiles_golden_levels_on_gpu():
+    need_cuda()
+    c = json.load(open(os.path.join(GOLD, "hh_levels.json")))["cases"]["6D_Davidson_S0"]
+    D, L, B = c["D"], c["L"], c["L_TO_nq_B"]
+    b = SG4Basis(D, L, L, 1, B, 1, B)
+    Q = b.grid_points()
+    lam = c["lambda"]
+    V = 0.5 * np.sum(Q ** 2, axis=1)
+    for i in range(D - 1):
+        V += lam * (Q[:, i] ** 2 * Q[:, i + 1] - Q[:, i + 1] ** 3 / 3.0)
+    op = ParamOp(b, 1, V=V, F2=-0.5 * np.eye(D))
+    H = gpu_apply(op, np.eye(b.N))
+    ev = np.sort(np.linalg.eigvalsh(0.5 * (H + H.T)))
+    ref = np.array(c["levels_au"])
+    assert np.max(np.abs(ev[: len(ref)] - ref)) < 2e-7
+
+
+def test_errors_are_status_codes():
+    need_cuda()
+    m = make_model(3, 4, 1, 1)
+    op = m.operator()
+    N = op.basis.N
+    with pytest.raises(EVRError):
+        sub_TabOpPsi(torch.zeros((0, N), dtype=torch.float64, device="cuda"), op)
+    with pytest.raises(EVRError):
+        op.hpsi_dev(torch.zeros((2, N + 1), dtype=torch.float64, device="cuda"),
+                    torch.zeros((2, N + 1), dtype=torch.float64, device="cuda"))
+    with pytest.raises(EVRError):
+        ParamOp(op.basis, 10, V=np.full(op.basis.sum_nq, np.nan))
+    # the context stays usable after rejected calls
+    psi = random_psi(N, 1, 1)
+    O, kw = oracle_for(m)
+    assert rel_err(gpu_apply(op, psi), O.hpsi(psi, **kw)) <= TOL
