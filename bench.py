@@ -138,6 +138,61 @@ def profile_traffic():
     return float(m.group(1)) if m else None
 
 
+def bench_davidson(op):
+    """Lowest 20 levels of the benchmark operator (restart 60, residual 1e-8)."""
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    d = op.diagonal()
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    ev, vec, rs, its = op.davidson(20, max_subspace=60, conv_resi=1e-8, symmetrize=True, diag=d, max_it=1000)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    return {"levels": 20, "max_subspace": 60, "conv_resi": 1e-8, "iterations": its, "davidson_s": t2 - t1,
+            "diagonal_s": t1 - t0, "max_residual": float(np.max(rs)), "E0_hartree": float(ev[0])}
+
+
+def bench_oc_gradient():
+    """Config 3: 4-D L=7, H(t) = H0 - E(t) mu, 2000 RK4 steps of 5 a.u., checkpoints
+    every 45 steps; seconds per gradient evaluation and its ratio to one forward
+    propagation."""
+    import torch
+    from elvibrot_gb300 import ParamOp
+    from elvibrot_gb300.configs import config, make_dipole
+    cfg = config(3)
+    m = cfg["model"]
+    H0 = m.operator()
+    mu = ParamOp(H0.basis, 0, V_poly=make_dipole(m, cfg["seed"]))
+    ev, vec, rs, its = H0.davidson(3, conv_resi=1e-10, max_it=500)
+    psi0 = vec[0].to(torch.complex128).contiguous()
+    target = vec[2].to(torch.complex128).contiguous()
+    E = np.random.Generator(np.random.PCG64(cfg["seed"])).normal(0.0, 1e-3, size=2000)
+    v = torch.randn((1, H0.basis.N), dtype=torch.float64, device="cuda")
+    hv = torch.empty_like(v)
+    for _ in range(60):                                  # power iteration for the top of the spectrum
+        v /= torch.linalg.vector_norm(v)
+        H0.hpsi_dev(v, hv)
+        Hmax = float((v * hv).sum().item())
+        v, hv = hv, v
+    E0 = 0.5 * (float(ev[0]) + Hmax)                     # RK4 on H0 - E0 (fcn_field's para_H%E0)
+    P = psi0.clone()
+    nsub = 10                                            # RK4 steps of 0.5 a.u. per 5-a.u. field sample
+    H0.rk4_field(mu, E[:10], P, 5.0, E0=E0, nsub=nsub)  # warm
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    P = psi0.clone()
+    H0.rk4_field(mu, E, P, 5.0, E0=E0, nsub=nsub)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    J, g = H0.oc_gradient(mu, E, psi0, target, 5.0, checkpoint=45, E0=E0, nsub=nsub)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    return {"workload": "4-D SG4 L=7 type 1, 2000 field samples of 5 a.u. (10 RK4 steps each), checkpoint every 45",
+            "s_per_iter": t2 - t1, "forward_s": t1 - t0, "ratio_to_forward": (t2 - t1) / (t1 - t0),
+            "J": J, "E0": E0, "Hmax_estimate": Hmax, "norm_after_forward": float(torch.linalg.vector_norm(P).item())}
+
+
 def run_ours(args, ws, rank, local):
     import torch
     import torch.distributed as dist
@@ -219,6 +274,12 @@ def run_ours(args, ws, rank, local):
         pt += a.elapsed_time(b) / 1e3
     plain_value = plain_steps * nrhs / pt
 
+    # callers of the path: Davidson on the same operator, OC gradient on the 4-D L=7 system
+    extras = {}
+    if not args.no_extras:
+        extras["davidson"] = bench_davidson(op)
+        extras["oc_gradient"] = bench_oc_gradient()
+
     flops = op.flops_per_rhs * nrhs
     achieved = flops / (ms_step / 1e3) / 1e12
     b = op.basis
@@ -259,6 +320,7 @@ def run_ours(args, ws, rank, local):
             "clocks": {"sm_mhz": clocks["sm_mhz"], "sm_max_mhz": clocks["sm_max_mhz"], "reasons": clocks["reasons"]},
             "gpu_launches": launches,
         }
+        result.update(extras)
     return result
 
 
@@ -296,6 +358,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-extras", action="store_true", help="skip the Davidson and OC-gradient timings")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if ws > 1:

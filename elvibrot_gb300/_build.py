@@ -17,7 +17,7 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libevrsg4.so")
 
-SOURCES = ["sg4_device.cu", "sg4_setup.cpp"]
+SOURCES = ["sg4_device.cu", "sg4_solvers.cu", "sg4_setup.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -64,7 +64,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
     tmp = LIB + ".tmp"
-    cmd = [cc, "-shared", "-o", tmp] + objs + ARCH + ["-lcudart"]
+    cmd = [cc, "-shared", "-o", tmp] + objs + ARCH + ["-lcudart", "-lcublas"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -109,6 +109,27 @@ def make_model(D: int, L: int, type_op: int, seed: int) -> SG4Model:
     return SG4Model(D, L, omega, s, V, 10, G0=np.eye(D), G1=G1)
 
 
+def make_dipole(model: SG4Model, seed: int) -> Polynomial:
+    """mu(Q) = sum_i a_i y_i + sum_{i<=j} b_ij y_i y_j, a ~ N(0,1), b ~ N(0,0.1),
+    in the dimensionless coordinates y = scaleQ Q (the optimal-control workload)."""
+    rng = np.random.Generator(np.random.PCG64(seed + 11))
+    D, s = model.D, model.scaleQ
+    coef, expo = [], []
+    for i in range(D):
+        e = np.zeros(D, dtype=np.int32)
+        e[i] = 1
+        coef.append(rng.normal(0.0, 1.0) * s[i])
+        expo.append(e)
+    for i in range(D):
+        for j in range(i, D):
+            e = np.zeros(D, dtype=np.int32)
+            e[i] += 1
+            e[j] += 1
+            coef.append(rng.normal(0.0, 0.1) * s[i] * s[j])
+            expo.append(e)
+    return Polynomial(np.array(coef), np.array(expo, dtype=np.int32))
+
+
 def random_psi(N: int, nrhs: int, seed: int, complex_: bool = False) -> np.ndarray:
     """(N, nrhs) column-normalised N(0,1) vectors."""
     rng = np.random.Generator(np.random.PCG64(seed + 7))

@@ -86,6 +86,8 @@ int desc_sizes(const evr_sg4_desc* d, DescSizes* z) {
 }
 
 // ------------------------------------------------------------------ device
+#define EVR_FUSED_MAXD 12  // type-10 items with D <= 12 use the fused grid passes
+
 struct TermInfo {
   long long off_nb;   // into map
   long long off_nq;   // into the operator fields
@@ -125,7 +127,8 @@ struct KParams {
   unsigned int* counter;     // batched path: global work counter
   const int* map;
   const double* mats;
-  const int* mat_off;        // [D*Lp1*4]
+  const int* mat_off;        // [D*Lp1*8]: forward set, then transposed set
+  int transpose;             // 1: apply H^T (the adjoint of the real operator)
   const int* nb_of_l;
   const int* nq_of_l;
   const double* psi;
@@ -144,10 +147,14 @@ struct KParams {
   int smem_doubles;
   double* gscratch;
   long long scratch_per_cta; // doubles
+  double* contrib;           // [sum_nb][nrhs_v] weighted term contributions
+  const double* cfac;        // [sum_nq] -1/2/(Jac sqRho) or NULL (= -1/2)
+  long long sum_nb;
 };
 
 struct ItemShared {
   int nb[EVR_MAXD], nq[EVR_MAXD];
+  int ord[EVR_MAXD];          // basis->grid mode order
   int mo[EVR_MAXD][4];
   long long off_nb, off_nq;
   int nb_t, nq_t, r, rhs0, term;
@@ -161,34 +168,62 @@ __device__ __forceinline__ long long vaddr(const KParams& p, int v, int n, long 
 }
 
 // out[a + S*(k + nout*b)] (+)= scale * sum_m M[k*NIN+m] in[a + S*(m + NIN*b)]
-template <int NIN>
-__device__ __forceinline__ void mode_pass_t(const double* __restrict__ M, int nout, long long S,
-                                            long long R, const double* in, double* out, bool acc,
-                                            double scale) {
-  const long long nf = S * R;
-  for (long long f = threadIdx.x; f < nf; f += blockDim.x) {
-    long long b = f / S, a = f - b * S;
+// One thread per fibre (a, b); the NIN inputs of the fibre stay in registers,
+// matrix loads are warp-uniform, and four outputs are formed at once as
+// independent FMA chains (GB300's FP64 pipe has a long latency, one chain per
+// warp cannot keep it busy).  MODE 0 stores, 1 adds, 2 adds scale times.
+template <int NIN, int MODE>
+__device__ __forceinline__ void mode_pass_t(const double* __restrict__ M, int nout, int S, int R,
+                                            const double* in, double* out, double scale) {
+  const int nf = S * R;
+  for (int f = threadIdx.x; f < nf; f += blockDim.x) {
+    const int b = f / S, a = f - b * S;
     const double* fi = in + a + S * NIN * b;
     double v[NIN];
 #pragma unroll
     for (int m = 0; m < NIN; ++m) v[m] = fi[S * m];
-    double* fo = out + a + S * (long long)nout * b;
-    for (int k = 0; k < nout; ++k) {
-      const double* Mk = M + k * NIN;
-      double s = 0.0;
+    double* fo = out + a + S * nout * b;
+    int k = 0;
+    for (; k + 4 <= nout; k += 4) {
+      const double* M0 = M + k * NIN;
+      double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
 #pragma unroll
-      for (int m = 0; m < NIN; ++m) s = fma(__ldg(Mk + m), v[m], s);
-      fo[S * k] = acc ? fma(scale, s, fo[S * k]) : (scale == 1.0 ? s : scale * s);
+      for (int m = 0; m < NIN; ++m) {
+        s0 = fma(__ldg(M0 + m), v[m], s0);
+        s1 = fma(__ldg(M0 + NIN + m), v[m], s1);
+        s2 = fma(__ldg(M0 + 2 * NIN + m), v[m], s2);
+        s3 = fma(__ldg(M0 + 3 * NIN + m), v[m], s3);
+      }
+      if (MODE == 0) {
+        fo[S * k] = s0; fo[S * (k + 1)] = s1; fo[S * (k + 2)] = s2; fo[S * (k + 3)] = s3;
+      } else if (MODE == 1) {
+        fo[S * k] += s0; fo[S * (k + 1)] += s1; fo[S * (k + 2)] += s2; fo[S * (k + 3)] += s3;
+      } else {
+        fo[S * k] = fma(scale, s0, fo[S * k]);
+        fo[S * (k + 1)] = fma(scale, s1, fo[S * (k + 1)]);
+        fo[S * (k + 2)] = fma(scale, s2, fo[S * (k + 2)]);
+        fo[S * (k + 3)] = fma(scale, s3, fo[S * (k + 3)]);
+      }
+    }
+    for (; k < nout; ++k) {
+      const double* Mk = M + k * NIN;
+      double s0 = 0.0;
+#pragma unroll
+      for (int m = 0; m < NIN; ++m) s0 = fma(__ldg(Mk + m), v[m], s0);
+      if (MODE == 0) fo[S * k] = s0;
+      else if (MODE == 1) fo[S * k] += s0;
+      else fo[S * k] = fma(scale, s0, fo[S * k]);
     }
   }
 }
 
-__device__ void mode_pass(const double* M, int nin, int nout, long long S, long long R,
-                          const double* in, double* out, bool acc, double scale) {
+template <int MODE>
+__device__ __noinline__ void mode_pass_m(const double* M, int nin, int nout, int S, int R, const double* in, double* out,
+                            double scale) {
   switch (nin) {
 #define EVR_CASE(n) \
   case n:           \
-    mode_pass_t<n>(M, nout, S, R, in, out, acc, scale); break;
+    mode_pass_t<n, MODE>(M, nout, S, R, in, out, scale); break;
     EVR_CASE(1) EVR_CASE(2) EVR_CASE(3) EVR_CASE(4) EVR_CASE(5) EVR_CASE(6) EVR_CASE(7) EVR_CASE(8)
     EVR_CASE(9) EVR_CASE(10) EVR_CASE(11) EVR_CASE(12) EVR_CASE(13) EVR_CASE(14) EVR_CASE(15) EVR_CASE(16)
 #undef EVR_CASE
@@ -196,10 +231,17 @@ __device__ void mode_pass(const double* M, int nin, int nout, long long S, long 
   }
 }
 
+__device__ void mode_pass(const double* M, int nin, int nout, int S, int R, const double* in, double* out,
+                          bool acc, double scale) {
+  if (!acc) mode_pass_m<0>(M, nin, nout, S, R, in, out, 1.0);
+  else if (scale == 1.0) mode_pass_m<1>(M, nin, nout, S, R, in, out, 1.0);
+  else mode_pass_m<2>(M, nin, nout, S, R, in, out, scale);
+}
+
 // Derivative pass along mode i on the grid (DerivOp_TO_RDP_OF_SmolaykRep).
 __device__ void grid_deriv(const KParams& p, const ItemShared& it, int i, int which, const double* in,
                            double* out, bool acc, double scale) {
-  long long S = 1, R = it.r;
+  int S = 1, R = it.r;
   for (int j = 0; j < p.D; ++j) {
     if (j < i) S *= it.nq[j];
     else if (j > i) R *= it.nq[j];
@@ -207,22 +249,157 @@ __device__ void grid_deriv(const KParams& p, const ItemShared& it, int i, int wh
   mode_pass(p.mats + it.mo[i][which], it.nq[i], it.nq[i], S, R, in, out, acc, scale);
 }
 
-// basis->grid (to_grid = true, BDP_TO_GDP) or grid->basis (GDP_TO_BDP), modes 1..D
+// basis->grid (to_grid, BDP_TO_GDP) or grid->basis (GDP_TO_BDP).  The
+// reference applies modes 1..D; the product of 1-D maps commutes, so the
+// modes are taken in the order that minimises multiply-adds: basis->grid in
+// ascending (nq-nb)/(nb*nq) (the modes that grow the array most go last),
+// grid->basis in the reverse order (they shrink it first).
 __device__ double* transform(const KParams& p, const ItemShared& it, bool to_grid, double* a, double* b) {
-  long long S = 1, R = it.r;
-  for (int j = 0; j < p.D; ++j) R *= to_grid ? it.nb[j] : it.nq[j];
-  for (int i = 0; i < p.D; ++i) {
-    int nin = to_grid ? it.nb[i] : it.nq[i];
-    int nout = to_grid ? it.nq[i] : it.nb[i];
-    R /= nin;
+  int cur[EVR_MAXD];
+  for (int j = 0; j < p.D; ++j) cur[j] = to_grid ? it.nb[j] : it.nq[j];
+  for (int k = 0; k < p.D; ++k) {
+    const int i = it.ord[to_grid ? k : p.D - 1 - k];
+    const int nin = cur[i];
+    const int nout = to_grid ? it.nq[i] : it.nb[i];
+    int S = 1, R = it.r;
+    for (int j = 0; j < p.D; ++j) {
+      if (j < i) S *= cur[j];
+      else if (j > i) R *= cur[j];
+    }
     mode_pass(p.mats + it.mo[i][to_grid ? M_BG : M_GB], nin, nout, S, R, a, b, false, 1.0);
-    S *= nout;
+    cur[i] = nout;
     __syncthreads();
     double* t = a;
     a = b;
     b = t;
   }
   return a;
+}
+
+// Type-10 grid operator in two fused passes over the grid points of an item
+// (D <= 12):
+//   pass A, per point: phi_j = (d_j x)(point) for every mode j (D independent
+//     FMA chains over the mode fibres through the point), then
+//     U_i = Jac sum_j G_ji phi_j, stored;
+//   pass B, per point: O = c * sum_i (d_i U_i)(point) + O  (O holds V.x).
+// The reference applies d_j to the whole grid mode by mode
+// (DerivOp_TO_RDP_OF_SmolaykRep); the same products, with two barriers
+// instead of 2D+2 and no phi arrays.  For H^T the matrices are transposed
+// and c (= -1/2/(Jac s)) and s trade places (done by the caller).
+template <int DD>
+__device__ void type10_fused(const KParams& p, const ItemShared& it, const double* x, double* O, double* U,
+                             int NQR) {
+  const int nqt = it.nq_t;
+  const long long oq = it.off_nq;
+  int nq[DD], st[DD];
+  const double* Md[DD];
+  {
+    int stride = 1;
+#pragma unroll
+    for (int i = 0; i < DD; ++i) {
+      nq[i] = it.nq[i];
+      st[i] = stride;
+      stride *= nq[i];
+      Md[i] = p.mats + it.mo[i][M_D1];
+    }
+  }
+  const long long GD = (long long)DD * DD;
+  const long long si = p.transpose ? nqt : (long long)nqt * DD;  // G offset step of the output index
+  const long long sj = p.transpose ? (long long)nqt * DD : nqt;  // ... and of the input index
+  for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
+    const int q = e % nqt;
+    const double* xr = x + (e - q);
+    int idx[DD];
+    {
+      int rem = q;
+#pragma unroll
+      for (int i = 0; i < DD; ++i) {
+        idx[i] = rem % nq[i];
+        rem /= nq[i];
+      }
+    }
+    double phi[DD];
+#pragma unroll
+    for (int j = 0; j < DD; ++j) {
+      const double* fib = xr + (q - idx[j] * st[j]);
+      const double* row = Md[j] + idx[j] * nq[j];
+      double a = 0.0;
+      for (int m = 0; m < nq[j]; ++m) a = fma(__ldg(row + m), fib[m * st[j]], a);
+      phi[j] = a;
+    }
+    const double jac = p.Jac ? __ldg(p.Jac + oq + q) : 1.0;
+    const double* g = p.G ? p.G + oq * GD + q : nullptr;
+#pragma unroll
+    for (int i = 0; i < DD; ++i) {
+      double u;
+      if (g) {
+        u = 0.0;
+#pragma unroll
+        for (int j = 0; j < DD; ++j) u = fma(__ldg(g + si * i + sj * j), phi[j], u);
+      } else {
+        u = phi[i];
+      }
+      U[(long long)i * NQR + e] = p.Jac ? u * jac : u;
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
+    const int q = e % nqt;
+    int idx[DD];
+    {
+      int rem = q;
+#pragma unroll
+      for (int i = 0; i < DD; ++i) {
+        idx[i] = rem % nq[i];
+        rem /= nq[i];
+      }
+    }
+    double acc[DD];
+#pragma unroll
+    for (int i = 0; i < DD; ++i) {
+      const double* fib = U + (long long)i * NQR + (e - idx[i] * st[i]);
+      const double* row = Md[i] + idx[i] * nq[i];
+      double a = 0.0;
+      for (int m = 0; m < nq[i]; ++m) a = fma(__ldg(row + m), fib[m * st[i]], a);
+      acc[i] = a;
+    }
+    double sum = 0.0;
+#pragma unroll
+    for (int i = 0; i < DD; ++i) sum += acc[i];
+    const double cf = !p.transpose ? (p.cfac ? __ldg(p.cfac + oq + q) : -0.5)
+                                   : (p.sqRho ? __ldg(p.sqRho + oq + q) : 1.0);
+    O[e] = fma(cf, sum, O[e]);
+  }
+  __syncthreads();
+}
+
+__device__ void type10_fused_dispatch(const KParams& p, const ItemShared& it, const double* x, double* O, double* U,
+                                      int NQR) {
+  switch (p.D) {
+#define EVR_T10(n) \
+  case n:          \
+    type10_fused<n>(p, it, x, O, U, NQR); break;
+    EVR_T10(1) EVR_T10(2) EVR_T10(3) EVR_T10(4) EVR_T10(5) EVR_T10(6) EVR_T10(7) EVR_T10(8) EVR_T10(9)
+    EVR_T10(10) EVR_T10(11) EVR_T10(12)
+#undef EVR_T10
+    default: break;
+  }
+}
+
+// The weighted term result WeightSG(l) * y_b goes to contrib[off_nb + k][v]
+// (no atomics); hpsi_reduce_kernel adds the contributions of each packed
+// function in Smolyak-term order, as tabR_AT_iG_TO_tabPackedBasis
+// accumulates them (sub_module_basis_BtoG_GtoB_SG4.f90:1255-1294).
+__device__ void store_contrib(const KParams& p, const ItemShared& it, const double* yb) {
+  const int nbt = it.nb_t;
+  const double wt = it.w;
+  const int* map = p.map + it.off_nb;
+  const int r = it.r;
+  for (int e = threadIdx.x; e < nbt * r; e += blockDim.x) {
+    const int k = e / r, j = e - k * r;
+    if (__ldg(map + k) > 0) p.contrib[(it.off_nb + k) * p.nrhs_v + it.rhs0 + j] = wt * yb[j * nbt + k];
+  }
+  __syncthreads();
 }
 
 __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int item_idx) {
@@ -246,19 +423,34 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ite
     const int k = i * p.Lp1 + l;
     it.nb[i] = p.nb_of_l[k];
     it.nq[i] = p.nq_of_l[k];
-    for (int q = 0; q < 4; ++q) it.mo[i][q] = p.mat_off[k * 4 + q];
+    for (int q = 0; q < 4; ++q) it.mo[i][q] = p.mat_off[k * 8 + 4 * p.transpose + q];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {  // insertion sort of the modes by (nq-nb)/(nb*nq), ties by index
+    for (int i = 0; i < p.D; ++i) {
+      int j = i;
+      const double key = (double)(it.nq[i] - it.nb[i]) / ((double)it.nb[i] * it.nq[i]);
+      while (j > 0) {
+        const int o = it.ord[j - 1];
+        const double ko = (double)(it.nq[o] - it.nb[o]) / ((double)it.nb[o] * it.nq[o]);
+        if (ko <= key) break;
+        it.ord[j] = o;
+        --j;
+      }
+      it.ord[j] = i;
+    }
   }
   __syncthreads();
   const int D = p.D, r = it.r, nbt = it.nb_t, nqt = it.nq_t;
-  const long long NQR = (long long)nqt * r;
+  const int NQR = nqt * r;
   double* buf = it.base;
   double* X = buf;
   double* T = buf + NQR;
   const int* map = p.map + it.off_nb;
 
   // gather (tabPackedBasis_TO_tabR_AT_iG)
-  for (long long e = threadIdx.x; e < (long long)nbt * r; e += blockDim.x) {
-    int j = (int)(e / nbt), k = (int)(e - (long long)j * nbt);
+  for (int e = threadIdx.x; e < nbt * r; e += blockDim.x) {
+    const int j = e / nbt, k = e - j * nbt;
     int n = __ldg(map + k);
     X[e] = n > 0 ? p.psi[vaddr(p, it.rhs0 + j, n - 1, p.ldpsi)] : 0.0;
   }
@@ -269,19 +461,18 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ite
 
   if (p.type == 0) {
     // CASE 0: y = V.x
-    for (long long e = threadIdx.x; e < NQR; e += blockDim.x) {
-      long long q = e % nqt;
+    for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
+      const int q = e % nqt;
       x[e] = (p.V ? __ldg(p.V + oq + q) : 0.0) * x[e];
     }
     y = x;
     __syncthreads();
   } else if (p.type == 1) {
     // CASE 1: y = V.x + sum F2_ij d_i d_j x + sum F1_i d_i x
-    double* other = (x == X) ? T : X;
     double* Y = buf + 2 * NQR;
     double* C = buf + 3 * NQR;
-    for (long long e = threadIdx.x; e < NQR; e += blockDim.x) {
-      long long q = e % nqt;
+    for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
+      const int q = e % nqt;
       Y[e] = p.V ? __ldg(p.V + oq + q) * x[e] : 0.0;
     }
     __syncthreads();
@@ -304,18 +495,42 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ite
       grid_deriv(p, it, i, M_D1, x, Y, true, f);
       __syncthreads();
     }
-    (void)other;
     y = Y;
+  } else if (D <= EVR_FUSED_MAXD) {
+    // CASE 10 through the fused grid passes; buffers: the transform pair
+    // {X, T}, then U_1..U_D.  O (= the free transform buffer) starts as V.x.
+    double* O = (x == X) ? T : X;
+    double* U = buf + 2 * NQR;
+    for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
+      const int q = e % nqt;
+      const double xv = x[e];
+      O[e] = p.V ? __ldg(p.V + oq + q) * xv : 0.0;
+      if (!p.transpose) {
+        if (p.sqRho) x[e] = xv * __ldg(p.sqRho + oq + q);
+      } else {
+        x[e] = xv * (p.cfac ? __ldg(p.cfac + oq + q) : -0.5);
+      }
+    }
+    __syncthreads();
+    type10_fused_dispatch(p, it, x, O, U, NQR);
+    double* yb = transform(p, it, false, O, x);
+    store_contrib(p, it, yb);
+    return;
   } else {
     // CASE 10: -1/2 sum_i d_i(Jac sum_j G_ji d_j(s x)) / (Jac s) + V x
     double* VX = buf + 2 * NQR;
     double* O = buf + 3 * NQR;
     double* Phi = buf + 4 * NQR;
-    for (long long e = threadIdx.x; e < NQR; e += blockDim.x) {
-      long long q = e % nqt;
+    // forward: s.x first and -1/2/(Jac s) last; H^T swaps the two scalings
+    for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
+      const int q = e % nqt;
       double xv = x[e];
       VX[e] = p.V ? __ldg(p.V + oq + q) * xv : 0.0;
-      if (p.sqRho) x[e] = xv * __ldg(p.sqRho + oq + q);
+      if (!p.transpose) {
+        if (p.sqRho) x[e] = xv * __ldg(p.sqRho + oq + q);
+      } else {
+        x[e] = xv * (p.cfac ? __ldg(p.cfac + oq + q) : -0.5);
+      }
     }
     __syncthreads();
     for (int j = 0; j < D; ++j) grid_deriv(p, it, j, M_D1, x, Phi + (long long)j * NQR, false, 1.0);
@@ -323,12 +538,16 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ite
     double* U = x;  // s.x is no longer needed
     const long long GD = (long long)D * D;
     for (int i = 0; i < D; ++i) {
-      for (long long e = threadIdx.x; e < NQR; e += blockDim.x) {
-        long long q = e % nqt;
+      for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
+        const int q = e % nqt;
         double u = 0.0;
         if (p.G) {
-          const double* g = p.G + oq * GD + (long long)nqt * ((long long)D * i) + q;
-          for (int j = 0; j < D; ++j) u = fma(__ldg(g + (long long)nqt * j), Phi[(long long)j * NQR + e], u);
+          // output i, input j: G_ji = GGiq(q, j, i) forward, G_ij for H^T
+          const double* g = p.G + oq * GD + q;
+          const long long si = p.transpose ? nqt : (long long)nqt * D;
+          const long long sj = p.transpose ? (long long)nqt * D : nqt;
+          for (int j = 0; j < D; ++j)
+            u = fma(__ldg(g + si * i + sj * j), Phi[(long long)j * NQR + e], u);
         } else {
           u = Phi[(long long)i * NQR + e];
         }
@@ -339,35 +558,24 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ite
       grid_deriv(p, it, i, M_D1, U, O, i > 0, 1.0);
       __syncthreads();
     }
-    for (long long e = threadIdx.x; e < NQR; e += blockDim.x) {
-      long long q = e % nqt;
-      double jac = p.Jac ? __ldg(p.Jac + oq + q) : 1.0;
-      double s = p.sqRho ? __ldg(p.sqRho + oq + q) : 1.0;
-      O[e] = -0.5 * O[e] / (jac * s) + VX[e];
+    // -1/2 O / (Jac s) + V x, with -1/2/(Jac s) formed once per operator
+    for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
+      const int q = e % nqt;
+      const double cf = !p.transpose ? (p.cfac ? __ldg(p.cfac + oq + q) : -0.5)
+                                     : (p.sqRho ? __ldg(p.sqRho + oq + q) : 1.0);
+      O[e] = fma(cf, O[e], VX[e]);
     }
     __syncthreads();
     y = O;
     // G->B ping-pongs between O and U
     double* yb = transform(p, it, false, O, U);
-    const double wt = it.w * p.scale;
-    for (long long e = threadIdx.x; e < (long long)nbt * r; e += blockDim.x) {
-      int j = (int)(e / nbt), k = (int)(e - (long long)j * nbt);
-      int n = __ldg(map + k);
-      if (n > 0) atomicAdd(p.hpsi + vaddr(p, it.rhs0 + j, n - 1, p.ldh), wt * yb[e]);
-    }
-    __syncthreads();
+    store_contrib(p, it, yb);
     return;
   }
   double* other = (y == X) ? T : X;
   if (p.type == 1) other = (x == X) ? X : T;  // x is free after the operator
   double* yb = transform(p, it, false, y, other);
-  const double wt = it.w * p.scale;
-  for (long long e = threadIdx.x; e < (long long)nbt * r; e += blockDim.x) {
-    int j = (int)(e / nbt), k = (int)(e - (long long)j * nbt);
-    int n = __ldg(map + k);
-    if (n > 0) atomicAdd(p.hpsi + vaddr(p, it.rhs0 + j, n - 1, p.ldh), wt * yb[e]);
-  }
-  __syncthreads();
+  store_contrib(p, it, yb);
 }
 
 __global__ void __launch_bounds__(256, 2) hpsi_batched_kernel(KParams p) {
@@ -390,19 +598,94 @@ __global__ void __launch_bounds__(256, 2) hpsi_plain_kernel(KParams p) {
   run_item(p, it, smem, p.item_base + blockIdx.x);
 }
 
-// hpsi(:,v) = -(E0/Esc) psi(:,v) over the packed vectors; also resets the
-// work counter of the batched kernel that follows on the same stream.
-__global__ void hpsi_init_kernel(double* hpsi, const double* psi, long long N, int nrhs_v, int cshift,
-                                 long long ldpsi, long long ldh, double a, unsigned int* counter) {
-  if (blockIdx.x == 0 && threadIdx.x == 0 && counter) *counter = 0u;
-  long long total = N * nrhs_v;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
-       e += (long long)gridDim.x * blockDim.x) {
-    int v = (int)(e / N);
-    long long n = e - (long long)v * N;
-    long long oh = (long long)(v >> cshift) * ldh + (n << cshift) + (v & cshift);
-    long long op = (long long)(v >> cshift) * ldpsi + (n << cshift) + (v & cshift);
-    hpsi[oh] = (a == 0.0) ? 0.0 : a * psi[op];
+// hpsi(n, v) = (sum_t contrib(k_t(n), v) - E0 psi(n, v)) / Esc, the sum over
+// the terms holding packed function n (inv_ptr/inv_idx is the inverse of
+// tab_iB_OF_SRep_TO_iB, in Smolyak-term order).  One warp per packed
+// function: lane l adds entries l, l+32, ... in order with Neumaier
+// compensation, then a fixed shuffle tree combines the lanes with TwoSum.
+// The schedule is fixed, so the result is deterministic, and the compensated
+// sums keep it independent of the sign pattern of the Smolyak weights.
+__device__ __forceinline__ void neumaier_add(double& s, double& c, double x) {
+  const double t = s + x;
+  c += (fabs(s) >= fabs(x)) ? ((s - t) + x) : ((x - t) + s);
+  s = t;
+}
+
+__device__ __forceinline__ void out_value(double* hpsi, const double* psi, long long n, int v, int cshift,
+                                          long long ldpsi, long long ldh, double sum, double E0, double Esc) {
+  const long long oh = (long long)(v >> cshift) * ldh + (n << cshift) + (v & cshift);
+  if (E0 == 0.0 && Esc == 1.0) {
+    hpsi[oh] = sum;
+  } else {
+    const long long op = (long long)(v >> cshift) * ldpsi + (n << cshift) + (v & cshift);
+    hpsi[oh] = (sum - E0 * psi[op]) / Esc;
+  }
+}
+
+// Packed functions with short contribution lists (<= EVR_LONG_LIST, nearly
+// all of them) get one thread per (function, right-hand side) that adds its
+// list sequentially in term order; the few held by many terms (the ground
+// state is in every term) get one warp each, lanes taking entries l, l+32, ...
+// and a fixed shuffle tree joining the lanes with TwoSum.
+#define EVR_LONG_LIST 128
+__global__ void __launch_bounds__(256) hpsi_reduce_kernel(
+    const double* __restrict__ contrib, const long long* __restrict__ inv_ptr,
+    const long long* __restrict__ inv_idx, const int* __restrict__ long_n, int n_long,
+    const int* __restrict__ short_n, long long n_short, int nrhs_v, int cshift, const double* psi,
+    long long ldpsi, double* hpsi, long long ldh, double E0, double Esc) {
+  constexpr int RV = 8;
+  const int lane = threadIdx.x & 31;
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  const long long short_warps = (n_short * nrhs_v + 31) / 32;
+  for (long long w = warp; w < n_long + short_warps; w += nwarps) {
+    if (w < n_long) {
+      const long long n = long_n[w];
+      const long long q0 = inv_ptr[n], q1 = inv_ptr[n + 1];
+      for (int v0 = 0; v0 < nrhs_v; v0 += RV) {
+        const int nv = min(RV, nrhs_v - v0);
+        double s[RV], c[RV];
+#pragma unroll
+        for (int u = 0; u < RV; ++u) s[u] = c[u] = 0.0;
+        for (long long q = q0 + lane; q < q1; q += 32) {
+          const double* cp = contrib + inv_idx[q] * nrhs_v + v0;
+#pragma unroll
+          for (int u = 0; u < RV; ++u)
+            if (u < nv) neumaier_add(s[u], c[u], cp[u]);
+        }
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1) {
+#pragma unroll
+          for (int u = 0; u < RV; ++u) {
+            if (u >= nv) continue;
+            const double so = __shfl_down_sync(0xffffffffu, s[u], off);
+            const double co = __shfl_down_sync(0xffffffffu, c[u], off);
+            const double t = s[u] + so;  // TwoSum(s, so)
+            const double bp = t - s[u];
+            const double err = (s[u] - (t - bp)) + (so - bp);
+            s[u] = t;
+            c[u] += co + err;
+          }
+        }
+        double mine = 0.0;
+#pragma unroll
+        for (int u = 0; u < RV; ++u) {
+          if (u >= nv) continue;
+          const double tot = __shfl_sync(0xffffffffu, s[u] + c[u], 0);
+          if (lane == u) mine = tot;
+        }
+        if (lane < nv) out_value(hpsi, psi, n, v0 + lane, cshift, ldpsi, ldh, mine, E0, Esc);
+      }
+    } else {
+      const long long pidx = (w - n_long) * 32 + lane;
+      if (pidx < n_short * nrhs_v) {
+        const long long n = short_n[pidx / nrhs_v];
+        const int v = (int)(pidx % nrhs_v);
+        double s = 0.0, c = 0.0;
+        for (long long q = inv_ptr[n]; q < inv_ptr[n + 1]; ++q) neumaier_add(s, c, contrib[inv_idx[q] * nrhs_v + v]);
+        out_value(hpsi, psi, n, v, cshift, ldpsi, ldh, s + c, E0, Esc);
+      }
+    }
   }
 }
 
@@ -499,6 +782,14 @@ struct evr_sg4_ctx {
   int n_items = 0;
   std::vector<int> term_item_start;  // plain path
   unsigned int* d_counter = nullptr;
+  long long* d_inv_ptr = nullptr;    // [N+1] packed function -> contributions
+  long long* d_inv_idx = nullptr;    // [count(map>0)] global DP indices, term order
+  int* d_long_n = nullptr;           // packed functions with > EVR_LONG_LIST contributions
+  int* d_short_n = nullptr;          // the others
+  int n_long = 0;
+  long long n_short = 0;
+  double* d_contrib = nullptr;       // [nrhs_v][sum_nb]
+  size_t contrib_cap = 0;
   double* d_scratch = nullptr;
   long long scratch_per_cta = 0;
   int grid = 0;
@@ -510,6 +801,7 @@ struct evr_sg4_ctx {
   double* d_G = nullptr;
   double* d_Jac = nullptr;
   double* d_sqRho = nullptr;
+  double* d_cfac = nullptr;
   double* d_F2 = nullptr;
   double* d_F1 = nullptr;
   double F2[EVR_MAXD * EVR_MAXD] = {0};
@@ -520,11 +812,15 @@ struct evr_sg4_ctx {
   long long last_launches = 0;
 };
 
-static int nbuf_for(int type, int D) { return type == 0 ? 2 : (type == 1 ? 4 : D + 4); }
+static int nbuf_for(int type, int D) {
+  return type == 0 ? 2 : (type == 1 ? 4 : (D <= EVR_FUSED_MAXD ? D + 2 : D + 4));
+}
 
 static void free_ctx(evr_sg4_ctx* c) {
   void* ptrs[] = {c->d_map, c->d_mats, c->d_mat_off, c->d_nb_of_l, c->d_nq_of_l, c->d_x, c->d_x_off,
-                  c->d_terms, c->d_items, c->d_counter, c->d_scratch, c->d_V, c->d_G, c->d_Jac,
+                  c->d_terms, c->d_items, c->d_counter, c->d_inv_ptr, c->d_inv_idx, c->d_contrib,
+                  c->d_long_n, c->d_short_n,
+                  c->d_scratch, c->d_V, c->d_G, c->d_Jac, c->d_cfac,
                   c->d_sqRho, c->d_F2, c->d_F1, c->d_io};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -571,25 +867,39 @@ extern "C" int evr_sg4_create(const evr_sg4_desc* d, evr_sg4_ctx** out) {
   c->nq_of_l.assign(d->nq_of_l, d->nq_of_l + D * Lp1);
   // matrices, re-laid out row-major [nout][nin]
   std::vector<double> mats;
-  c->mat_off.resize((size_t)D * Lp1 * 4);
+  c->mat_off.resize((size_t)D * Lp1 * 8);
   c->x_off.resize((size_t)D * Lp1);
   size_t o_rgb = 0, o_gb = 0, o_gg = 0, o_x = 0;
   for (int k = 0; k < D * Lp1; ++k) {
     int nb = c->nb_of_l[k], nq = c->nq_of_l[k];
     c->x_off[k] = (int)o_x;
     o_x += nq;
-    c->mat_off[k * 4 + M_BG] = (int)mats.size();
+    // forward set: RGB [nq][nb], RBGwrho [nb][nq], d1GG, d2GG [nq][nq] (row-major)
+    c->mat_off[k * 8 + M_BG] = (int)mats.size();
     for (int q = 0; q < nq; ++q)
       for (int b = 0; b < nb; ++b) mats.push_back(d->RGB[o_rgb + q + (size_t)nq * b]);
-    c->mat_off[k * 4 + M_GB] = (int)mats.size();
+    c->mat_off[k * 8 + M_GB] = (int)mats.size();
     for (int b = 0; b < nb; ++b)
       for (int q = 0; q < nq; ++q) mats.push_back(d->RBGwrho[o_gb + b + (size_t)nb * q]);
-    c->mat_off[k * 4 + M_D1] = (int)mats.size();
+    c->mat_off[k * 8 + M_D1] = (int)mats.size();
     for (int r = 0; r < nq; ++r)
       for (int s = 0; s < nq; ++s) mats.push_back(d->d1GG[o_gg + r + (size_t)nq * s]);
-    c->mat_off[k * 4 + M_D2] = (int)mats.size();
+    c->mat_off[k * 8 + M_D2] = (int)mats.size();
     for (int r = 0; r < nq; ++r)
       for (int s = 0; s < nq; ++s) mats.push_back(d->d2GG[o_gg + r + (size_t)nq * s]);
+    // transposed set (H^T = B->G with RBGwrho^T, G->B with RGB^T, d^T):
+    c->mat_off[k * 8 + 4 + M_BG] = (int)mats.size();
+    for (int q = 0; q < nq; ++q)
+      for (int b = 0; b < nb; ++b) mats.push_back(d->RBGwrho[o_gb + b + (size_t)nb * q]);
+    c->mat_off[k * 8 + 4 + M_GB] = (int)mats.size();
+    for (int b = 0; b < nb; ++b)
+      for (int q = 0; q < nq; ++q) mats.push_back(d->RGB[o_rgb + q + (size_t)nq * b]);
+    c->mat_off[k * 8 + 4 + M_D1] = (int)mats.size();
+    for (int r = 0; r < nq; ++r)
+      for (int s = 0; s < nq; ++s) mats.push_back(d->d1GG[o_gg + s + (size_t)nq * r]);
+    c->mat_off[k * 8 + 4 + M_D2] = (int)mats.size();
+    for (int r = 0; r < nq; ++r)
+      for (int s = 0; s < nq; ++s) mats.push_back(d->d2GG[o_gg + s + (size_t)nq * r]);
     o_rgb += (size_t)nq * nb;
     o_gb += (size_t)nq * nb;
     o_gg += (size_t)nq * nq;
@@ -614,6 +924,22 @@ extern "C" int evr_sg4_create(const evr_sg4_desc* d, evr_sg4_ctx** out) {
     onb += nb;
     onq += nq;
   }
+  // inverse of the gather map: for each packed function, its DP entries in term order
+  std::vector<long long> inv_ptr(d->N + 1, 0), inv_idx;
+  for (long long k = 0; k < z.sum_nb; ++k)
+    if (d->map[k] > 0) inv_ptr[d->map[k]]++;
+  for (long long n = 0; n < d->N; ++n) inv_ptr[n + 1] += inv_ptr[n];
+  inv_idx.resize(inv_ptr[d->N] > 0 ? inv_ptr[d->N] : 1);
+  {
+    std::vector<long long> fill(inv_ptr.begin(), inv_ptr.end() - 1);
+    for (long long k = 0; k < z.sum_nb; ++k)
+      if (d->map[k] > 0) inv_idx[fill[d->map[k] - 1]++] = k;
+  }
+  std::vector<int> long_n, short_n;
+  for (long long n = 0; n < d->N; ++n)
+    (inv_ptr[n + 1] - inv_ptr[n] > EVR_LONG_LIST ? long_n : short_n).push_back((int)n);
+  c->n_long = (int)long_n.size();
+  c->n_short = (long long)short_n.size();
   // launch geometry: two 256-thread CTAs per SM, ~110 KB of shared memory each
   c->smem_doubles = 110 * 1024 / 8;
   c->grid = 2 * c->num_sms;
@@ -625,7 +951,11 @@ extern "C" int evr_sg4_create(const evr_sg4_desc* d, evr_sg4_ctx** out) {
       (rc = upload(&c->d_x, d->x, o_x)) ||
       (rc = upload(&c->d_x_off, c->x_off.data(), c->x_off.size())) ||
       (rc = upload<TermInfo>(&c->d_terms, nullptr, c->terms.size())) ||
-      (rc = upload<unsigned int>(&c->d_counter, nullptr, 1))) {
+      (rc = upload<unsigned int>(&c->d_counter, nullptr, 1)) ||
+      (rc = upload(&c->d_inv_ptr, inv_ptr.data(), inv_ptr.size())) ||
+      (rc = upload(&c->d_inv_idx, inv_idx.data(), inv_idx.size())) ||
+      (rc = upload(&c->d_long_n, long_n.data(), long_n.size())) ||
+      (rc = upload(&c->d_short_n, short_n.data(), short_n.size()))) {
     free_ctx(c);
     return rc;
   }
@@ -653,7 +983,7 @@ extern "C" int evr_sg4_set_operator(evr_sg4_ctx* c, const evr_sg4_op_desc* op) {
     return set_error(EVR_ERR_ARG, "evr_sg4_set_operator: type_Op=%d not in {0,1,10}", op->type);
   const int D = c->D;
   const long long snq = c->z.sum_nq;
-  for (double** p : {&c->d_V, &c->d_G, &c->d_Jac, &c->d_sqRho, &c->d_F2, &c->d_F1})
+  for (double** p : {&c->d_V, &c->d_G, &c->d_Jac, &c->d_sqRho, &c->d_cfac, &c->d_F2, &c->d_F1})
     if (*p) {
       cudaFree(*p);
       *p = nullptr;
@@ -692,6 +1022,12 @@ extern "C" int evr_sg4_set_operator(evr_sg4_ctx* c, const evr_sg4_op_desc* op) {
         if (!(op->sqRho_grid[k] != 0.0) || !std::isfinite(op->sqRho_grid[k]))
           return set_error(EVR_ERR_NUMERIC, "sqRho_grid[%lld] is zero or not finite", k);
       if ((rc = upload(&c->d_sqRho, op->sqRho_grid, (size_t)snq))) return rc;
+    }
+    if (op->Jac_grid || op->sqRho_grid) {  // -1/2 / (Jac sqRhoOVERJac) per point
+      std::vector<double> cf((size_t)snq);
+      for (long long k = 0; k < snq; ++k)
+        cf[k] = -0.5 / ((op->Jac_grid ? op->Jac_grid[k] : 1.0) * (op->sqRho_grid ? op->sqRho_grid[k] : 1.0));
+      if ((rc = upload(&c->d_cfac, cf.data(), cf.size()))) return rc;
     }
   }
   memset(c->F2, 0, sizeof(c->F2));
@@ -738,12 +1074,15 @@ extern "C" int evr_sg4_set_operator(evr_sg4_ctx* c, const evr_sg4_op_desc* op) {
 
 // Builds the (term, rhs block) work list for nrhs_v virtual right-hand sides,
 // sorted by decreasing cost so the persistent kernel balances well.
-static int build_items(evr_sg4_ctx* c, int nrhs_v) {
-  if (c->items_nrhs == nrhs_v) return EVR_OK;
+// Work list of one H.psi over nrhs_v virtual right-hand sides: (term, rhs
+// block) items, term-ordered and cost-sorted (decreasing, so the persistent
+// kernel ends balanced), with each term's block size r written into c->terms.
+static void plan_items(evr_sg4_ctx* c, int nrhs_v, std::vector<Item>& items, std::vector<Item>& sorted,
+                       long long& max_need) {
   const int nbuf = nbuf_for(c->type, c->D);
   const int Rmax = 32;
-  long long max_need = 0;
-  std::vector<Item> items;
+  max_need = 0;
+  items.clear();
   std::vector<float> cost;
   for (long long t = 0; t < c->nb_SG; ++t) {
     TermInfo& T = c->terms[t];
@@ -759,12 +1098,18 @@ static int build_items(evr_sg4_ctx* c, int nrhs_v) {
       cost.push_back(T.cost * std::min(r, nrhs_v - r0));
     }
   }
-  // plain path keeps the term order; the batched path gets a sorted copy
   std::vector<int> order(items.size());
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
-  std::vector<Item> sorted(items.size());
+  sorted.resize(items.size());
   for (size_t k = 0; k < order.size(); ++k) sorted[k] = items[order[k]];
+}
+
+static int build_items(evr_sg4_ctx* c, int nrhs_v) {
+  if (c->items_nrhs == nrhs_v) return EVR_OK;
+  std::vector<Item> items, sorted;
+  long long max_need = 0;
+  plan_items(c, nrhs_v, items, sorted, max_need);
   c->term_item_start.assign(c->nb_SG + 1, 0);
   for (size_t k = 0; k < items.size(); ++k) c->term_item_start[items[k].term + 1]++;
   for (long long t = 0; t < c->nb_SG; ++t) c->term_item_start[t + 1] += c->term_item_start[t];
@@ -787,7 +1132,25 @@ static int build_items(evr_sg4_ctx* c, int nrhs_v) {
     CUDA_TRY(cudaMalloc(&c->d_scratch, (size_t)per_cta * c->grid * 8));
     c->scratch_per_cta = per_cta;
   }
+  size_t cneed = (size_t)c->z.sum_nb * nrhs_v;
+  if (cneed > c->contrib_cap) {
+    if (c->d_contrib) cudaFree(c->d_contrib);
+    c->d_contrib = nullptr;
+    CUDA_TRY(cudaMalloc(&c->d_contrib, cneed * 8));
+    c->contrib_cap = cneed;
+  }
   c->items_nrhs = nrhs_v;
+  return EVR_OK;
+}
+
+static int launch_reduce(evr_sg4_ctx* c, const double* contrib, int nrhs_v, int cshift, const double* psi,
+                         long long ldpsi, double* hpsi, long long ldh, double E0, double Esc, cudaStream_t s) {
+  const long long warps = c->n_long + (c->n_short * nrhs_v + 31) / 32;
+  const long long blocks = std::max<long long>(1, std::min<long long>((warps + 7) / 8, 16LL * c->num_sms));
+  hpsi_reduce_kernel<<<(unsigned)blocks, 256, 0, s>>>(contrib, c->d_inv_ptr, c->d_inv_idx, c->d_long_n, c->n_long,
+                                                     c->d_short_n, c->n_short, nrhs_v, cshift, psi, ldpsi, hpsi,
+                                                     ldh, E0, Esc);
+  CUDA_TRY(cudaGetLastError());
   return EVR_OK;
 }
 
@@ -823,11 +1186,15 @@ static KParams make_params(evr_sg4_ctx* c, int nrhs_v, int cshift, const double*
   p.smem_doubles = c->smem_doubles;
   p.gscratch = c->d_scratch;
   p.scratch_per_cta = c->scratch_per_cta;
+  p.contrib = c->d_contrib;
+  p.cfac = c->d_cfac;
+  p.sum_nb = c->z.sum_nb;
   return p;
 }
 
 static int hpsi_common(evr_sg4_ctx* c, int nrhs, int cshift, const double* psi, long long ldpsi,
-                       double* hpsi, long long ldh, double E0, double Esc, void* stream, bool plain) {
+                       double* hpsi, long long ldh, double E0, double Esc, void* stream, bool plain,
+                       bool transpose = false) {
   if (!c) return set_error(EVR_ERR_ARG, "hpsi: NULL context");
   if (!c->have_op) return set_error(EVR_ERR_STATE, "hpsi: set_operator was not called");
   if (nrhs < 1) return set_error(EVR_ERR_ARG, "hpsi: nrhs=%d (size(Psi)=0 stops the reference)", nrhs);
@@ -846,19 +1213,18 @@ static int hpsi_common(evr_sg4_ctx* c, int nrhs, int cshift, const double* psi, 
   if (rc) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   const long long ldv_psi = ldpsi << cshift, ldv_h = ldh << cshift;
-  hpsi_init_kernel<<<2 * c->num_sms, 256, 0, s>>>(hpsi, psi, c->N, nrhs_v, cshift, ldv_psi, ldv_h, -E0 / Esc,
-                                                 c->d_counter);
-  CUDA_TRY(cudaGetLastError());
-  KParams p = make_params(c, nrhs_v, cshift, psi, ldv_psi, hpsi, ldv_h, 1.0 / Esc);
+  KParams p = make_params(c, nrhs_v, cshift, psi, ldv_psi, hpsi, ldv_h, 1.0);
+  p.transpose = transpose ? 1 : 0;
   const size_t smem = (size_t)c->smem_doubles * 8;
+  long long launches = 0;
   if (!plain) {
+    CUDA_TRY(cudaMemsetAsync(c->d_counter, 0, sizeof(unsigned int), s));
     p.items = c->d_items;
     hpsi_batched_kernel<<<c->grid, 256, smem, s>>>(p);
     CUDA_TRY(cudaGetLastError());
-    c->last_launches = 2;
+    launches = 1;
   } else {
     p.items = c->d_items + c->n_items;  // term-ordered list
-    long long launches = 1;
     for (long long t = 0; t < c->nb_SG; ++t) {
       int n = c->term_item_start[t + 1] - c->term_item_start[t];
       p.item_base = c->term_item_start[t];
@@ -866,8 +1232,10 @@ static int hpsi_common(evr_sg4_ctx* c, int nrhs, int cshift, const double* psi, 
       ++launches;
     }
     CUDA_TRY(cudaGetLastError());
-    c->last_launches = launches;
   }
+  if ((rc = launch_reduce(c, c->d_contrib, nrhs_v, cshift, psi, ldv_psi, hpsi, ldv_h, E0, Esc, s))) return rc;
+  CUDA_TRY(cudaGetLastError());
+  c->last_launches = launches + 1;
   return EVR_OK;
 }
 
@@ -884,6 +1252,17 @@ extern "C" int evr_sg4_hpsi_plain(evr_sg4_ctx* c, int nrhs, const double* psi, l
 extern "C" int evr_sg4_hpsi_cplx(evr_sg4_ctx* c, int nrhs, const double* psi, long long ldpsi, double* hpsi,
                                  long long ldh, double E0, double Esc, void* stream) {
   return hpsi_common(c, nrhs, 1, psi, ldpsi, hpsi, ldh, E0, Esc, stream, false);
+}
+
+extern "C" int evr_sg4_apply(evr_sg4_ctx* c, int flags, int nrhs, const double* psi, long long ldpsi,
+                             double* hpsi, long long ldh, double E0, double Esc, void* stream) {
+  if (flags & ~(EVR_APPLY_TRANSPOSE | EVR_APPLY_COMPLEX | EVR_APPLY_PLAIN))
+    return set_error(EVR_ERR_ARG, "apply: unknown flags 0x%x", flags);
+  const bool plain = (flags & EVR_APPLY_PLAIN) != 0;
+  if (plain && ((flags & EVR_APPLY_COMPLEX) || E0 != 0.0 || Esc != 1.0))
+    return set_error(EVR_ERR_ARG, "apply: the per-term path takes real psi with E0=0, Esc=1");
+  return hpsi_common(c, nrhs, (flags & EVR_APPLY_COMPLEX) ? 1 : 0, psi, ldpsi, hpsi, ldh, E0, Esc, stream, plain,
+                     (flags & EVR_APPLY_TRANSPOSE) != 0);
 }
 
 extern "C" int evr_sg4_hpsi_host(evr_sg4_ctx* c, int nrhs, const double* psi, long long ldpsi, double* hpsi,
@@ -952,6 +1331,19 @@ extern "C" int evr_sg4_flops_per_rhs(const evr_sg4_ctx* c, double* flops) {
     F += f;
   }
   *flops = F;
+  return EVR_OK;
+}
+
+extern "C" int evr_sg4_ctx_sizes(const evr_sg4_ctx* c, long long* out) {
+  if (!c || !out) return set_error(EVR_ERR_ARG, "ctx_sizes: NULL argument");
+  out[0] = c->N;
+  out[1] = c->nb_SG;
+  out[2] = c->z.sum_nb;
+  out[3] = c->z.sum_nq;
+  out[4] = c->z.max_nb;
+  out[5] = c->z.max_nq;
+  out[6] = c->D;
+  out[7] = c->L;
   return EVR_OK;
 }
 

@@ -67,6 +67,21 @@ class Desc(ctypes.Structure):
                 ("map", ctypes.POINTER(ctypes.c_int)), ("N", ctypes.c_longlong)]
 
 
+class DavidsonOpts(ctypes.Structure):
+    _fields_ = [("nev", ctypes.c_int), ("block", ctypes.c_int), ("max_subspace", ctypes.c_int),
+                ("max_it", ctypes.c_int), ("conv_resi", ctypes.c_double), ("symmetrize", ctypes.c_int)]
+
+
+class ChebyOpts(ctypes.Structure):
+    _fields_ = [("Hmin", ctypes.c_double), ("Hmax", ctypes.c_double), ("dt", ctypes.c_double),
+                ("npoly", ctypes.c_int), ("nsteps", ctypes.c_int), ("poly_tol", ctypes.c_double)]
+
+
+class RK4Opts(ctypes.Structure):
+    _fields_ = [("dt", ctypes.c_double), ("nsteps", ctypes.c_int), ("checkpoint", ctypes.c_int),
+                ("E0", ctypes.c_double), ("nsub", ctypes.c_int)]
+
+
 class OpDesc(ctypes.Structure):
     _fields_ = [("type", ctypes.c_int), ("V_grid", ctypes.POINTER(ctypes.c_double)),
                 ("V_nterms", ctypes.c_int), ("V_coef", ctypes.POINTER(ctypes.c_double)),
@@ -91,9 +106,18 @@ def _declare(L):
         "evr_sg4_hpsi_plain": [vp, ctypes.c_int, vp, ll, vp, ll, vp],
         "evr_sg4_hpsi_cplx": [vp, ctypes.c_int, vp, ll, vp, ll, ctypes.c_double, ctypes.c_double, vp],
         "evr_sg4_hpsi_host": [vp, ctypes.c_int, vp, ll, vp, ll, ctypes.c_double, ctypes.c_double],
+        "evr_sg4_apply": [vp, ctypes.c_int, ctypes.c_int, vp, ll, vp, ll, ctypes.c_double, ctypes.c_double, vp],
         "evr_sg4_flops_per_rhs": [vp, dp],
         "evr_sg4_last_launches": [vp, ctypes.POINTER(ll)],
         "evr_probe_fp64_peak": [dp],
+        "evr_sg4_ctx_sizes": [vp, ctypes.POINTER(ll)],
+        "evr_sg4_rk4_field": [vp, vp, ctypes.POINTER(RK4Opts), dp, vp, vp],
+        "evr_sg4_oc_gradient": [vp, vp, ctypes.POINTER(RK4Opts), dp, vp, vp, dp, dp, vp],
+        "evr_sg4_cheby_propagate": [vp, ctypes.POINTER(ChebyOpts), ctypes.c_int, vp, vp, dp,
+                                    ctypes.POINTER(ctypes.c_int), vp],
+        "evr_sg4_diagonal": [vp, vp, vp],
+        "evr_sg4_davidson": [vp, ctypes.POINTER(DavidsonOpts), vp, ctypes.c_int, vp, dp, vp, dp,
+                             ctypes.POINTER(ctypes.c_int), vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -176,6 +200,30 @@ class SG4Basis:
                     d2GG=arr(d.d2GG, og, nq * nq).reshape(nq, nq).T)
 
 
+class SG4Tables:
+    """SG4 tables supplied by the caller (what a Fortran host copies out of
+    para_Op%BasisnD; see evr_sg4_desc in include/evr_sg4.h).
+
+    Per-(mode, level) arrays are concatenated mode-major, level-minor;
+    matrices are column-major: RGB nq x nb, RBGwrho nb x nq, d1GG/d2GG nq x nq.
+    """
+
+    def __init__(self, D, L, LB, nb_of_l, nq_of_l, x, RGB, RBGwrho, d1GG, d2GG, tab_l, weight, map_, N):
+        self.D, self.L, self.LB = int(D), int(L), int(LB)
+        i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32).ravel()
+        f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64).ravel()
+        self._keep = dict(nb_of_l=i32(nb_of_l), nq_of_l=i32(nq_of_l), x=f64(x), RGB=f64(RGB),
+                          RBGwrho=f64(RBGwrho), d1GG=f64(d1GG), d2GG=f64(d2GG), tab_l=i32(tab_l),
+                          weight=f64(weight), map=i32(map_))
+        k = self._keep
+        self.desc = Desc(self.D, self.L, self.LB, 1, _ip(k["nb_of_l"]), _ip(k["nq_of_l"]), _dp(k["x"]),
+                         _dp(k["RGB"]), _dp(k["RBGwrho"]), _dp(k["d1GG"]), _dp(k["d2GG"]),
+                         len(k["weight"]), _ip(k["tab_l"]), _dp(k["weight"]), _ip(k["map"]), int(N))
+        z = (ctypes.c_longlong * 8)()
+        check(lib().evr_sg4_desc_sizes(ctypes.byref(self.desc), z))
+        self.N, self.nb_SG, self.sum_nb, self.sum_nq, self.max_nb, self.max_nq = [int(v) for v in z[:6]]
+
+
 @dataclass
 class Polynomial:
     """sum_t coef[t] prod_i Q_i**expo[t, i] (raw coordinates Q)."""
@@ -248,7 +296,8 @@ class ParamOp:
         return n.value
 
     # -- device-pointer calls (torch CUDA tensors, column-major N x nrhs) --
-    def hpsi_dev(self, psi, out, E0: float = 0.0, Esc: float = 1.0, stream: int = 0, plain: bool = False):
+    def hpsi_dev(self, psi, out, E0: float = 0.0, Esc: float = 1.0, stream: int = 0, plain: bool = False,
+                 transpose: bool = False):
         import torch
         N = self.basis.N
         if psi.dtype not in (torch.float64, torch.complex128) or not psi.is_cuda:
@@ -259,6 +308,10 @@ class ParamOp:
         if P.shape[-1] != N or O.shape != P.shape or not P.is_contiguous() or not O.is_contiguous():
             raise EVRError(1, f"psi/out must be contiguous (nrhs, {N}) tensors of equal shape")
         nrhs = P.shape[0]
+        if transpose:
+            flags = 1 | (2 if cplx else 0) | (4 if plain else 0)
+            check(lib().evr_sg4_apply(self._h, flags, nrhs, P.data_ptr(), N, O.data_ptr(), N, E0, Esc, stream))
+            return out
         if plain:
             if cplx or E0 != 0.0 or Esc != 1.0:
                 raise EVRError(1, "the plain per-term path takes real psi with E0=0, Esc=1")
@@ -268,6 +321,68 @@ class ParamOp:
         else:
             check(lib().evr_sg4_hpsi(self._h, nrhs, P.data_ptr(), N, O.data_ptr(), N, E0, Esc, stream))
         return out
+
+    def diagonal(self):
+        """Exact diag(H) as a CUDA tensor (the Davidson preconditioner)."""
+        import torch
+        d = torch.empty(self.basis.N, dtype=torch.float64, device="cuda")
+        check(lib().evr_sg4_diagonal(self._h, d.data_ptr(), 0))
+        return d
+
+    def davidson(self, nev: int, block: int = 0, max_subspace: int = 0, max_it: int = 500,
+                 conv_resi: float = 1e-8, symmetrize: bool = False, guess=None, diag=None):
+        """Lowest nev levels (sub_propagation_Davidson).  Returns (evals, evecs
+        (CUDA tensor nev x N), residual norms, iterations); raises EVRError
+        when max_it is reached."""
+        import torch
+        N = self.basis.N
+        o = DavidsonOpts(nev, block, max_subspace, max_it, conv_resi, 1 if symmetrize else 0)
+        ev = np.zeros(nev)
+        rs = np.zeros(nev)
+        vec = torch.empty((nev, N), dtype=torch.float64, device="cuda")
+        its = ctypes.c_int()
+        gptr, ng = (guess.data_ptr(), guess.shape[0]) if guess is not None else (None, 0)
+        check(lib().evr_sg4_davidson(self._h, ctypes.byref(o), gptr, ng,
+                                     diag.data_ptr() if diag is not None else None, _dp(ev), vec.data_ptr(),
+                                     _dp(rs), ctypes.byref(its), 0))
+        return ev, vec, rs, its.value
+
+    def cheby_propagate(self, psi, Hmin: float, Hmax: float, dt: float, npoly: int, nsteps: int,
+                        poly_tol: float = 0.0, psi0=None):
+        """Propagates the CUDA complex128 tensor psi (nrhs, N) in place
+        (march_cheby); returns (autocorrelation [(nsteps+1), nrhs], npoly used)."""
+        import torch
+        if psi.dtype != torch.complex128 or not psi.is_cuda or not psi.is_contiguous():
+            raise EVRError(1, "psi must be a contiguous CUDA complex128 tensor (nrhs, N)")
+        P = psi if psi.dim() == 2 else psi.unsqueeze(0)
+        nrhs = P.shape[0]
+        ac = np.zeros((nsteps + 1) * nrhs * 2)
+        used = ctypes.c_int()
+        o = ChebyOpts(Hmin, Hmax, dt, npoly, nsteps, poly_tol)
+        check(lib().evr_sg4_cheby_propagate(self._h, ctypes.byref(o), nrhs, P.data_ptr(),
+                                            psi0.data_ptr() if psi0 is not None else None, _dp(ac),
+                                            ctypes.byref(used), 0))
+        a = ac.reshape(nsteps + 1, nrhs, 2)
+        return a[..., 0] + 1j * a[..., 1], used.value
+
+    def rk4_field(self, mu: "ParamOp", E: np.ndarray, psi, dt: float, E0: float = 0.0, nsub: int = 1):
+        """march_RK4_field: propagates the CUDA complex128 vector psi (N,) in place
+        under H0 - E(t) mu, E held at E[k] over step k."""
+        E = np.ascontiguousarray(E, dtype=np.float64)
+        o = RK4Opts(dt, len(E), 1, E0, nsub)
+        check(lib().evr_sg4_rk4_field(self._h, mu._h, ctypes.byref(o), _dp(E), psi.data_ptr(), 0))
+        return psi
+
+    def oc_gradient(self, mu: "ParamOp", E: np.ndarray, psi0, target, dt: float, checkpoint: int = 45,
+                    E0: float = 0.0, nsub: int = 1):
+        """(J, dJ/dE) for J = |<target|psi(T)>|^2 by the adjoint of the RK4 steps."""
+        E = np.ascontiguousarray(E, dtype=np.float64)
+        o = RK4Opts(dt, len(E), checkpoint, E0, nsub)
+        J = ctypes.c_double()
+        g = np.zeros(len(E))
+        check(lib().evr_sg4_oc_gradient(self._h, mu._h, ctypes.byref(o), _dp(E), psi0.data_ptr(), target.data_ptr(),
+                                        ctypes.byref(J), _dp(g), 0))
+        return J.value, g
 
     def hpsi_host(self, psi: np.ndarray, E0: float = 0.0, Esc: float = 1.0) -> np.ndarray:
         """psi (N,) or (N, nrhs) host float64; returns the same shape (copies in/out)."""

@@ -158,11 +158,106 @@ int evr_sg4_hpsi_plain(evr_sg4_ctx* c, int nrhs, const double* psi, long long ld
 int evr_sg4_hpsi_cplx(evr_sg4_ctx* c, int nrhs, const double* psi, long long ldpsi, double* hpsi,
                       long long ldh, double E0, double Esc, void* stream);
 
+/* General form of the three calls above plus the transposed operator:
+ *   flags & EVR_APPLY_TRANSPOSE : apply H^T instead of H.  The SG4 H is not
+ *       symmetric in general (grid-grid derivatives on nq > nb grids make the
+ *       type-10 KEO non-Hermitian); H^T gives its symmetric part
+ *       (H + H^T)/2, which is what Davidson diagonalises after
+ *       sub_hermitic_H (SRC/sub_inactive/sub_ana_HS.f90:56), and the adjoint
+ *       a costate propagation needs.  Same kernels, transposed 1-D matrices.
+ *   flags & EVR_APPLY_COMPLEX   : interleaved complex128 psi (as _cplx).
+ *   flags & EVR_APPLY_PLAIN     : one launch per term (as _plain).        */
+#define EVR_APPLY_TRANSPOSE 1
+#define EVR_APPLY_COMPLEX 2
+#define EVR_APPLY_PLAIN 4
+int evr_sg4_apply(evr_sg4_ctx* c, int flags, int nrhs, const double* psi, long long ldpsi, double* hpsi,
+                  long long ldh, double E0, double Esc, void* stream);
+
 /* Host-pointer variant: copies psi to the device, runs evr_sg4_hpsi,
  * copies the result back and synchronises (what a Fortran caller holding
  * RvecB in host memory calls). */
 int evr_sg4_hpsi_host(evr_sg4_ctx* c, int nrhs, const double* psi, long long ldpsi, double* hpsi,
                       long long ldh, double E0, double Esc);
+
+/* Sizes of a context: out[0..7] as evr_sg4_desc_sizes. */
+int evr_sg4_ctx_sizes(const evr_sg4_ctx* c, long long* out);
+
+/* ------------------------------------------------------------------------
+ * Callers of the path, on the device.
+ * ---------------------------------------------------------------------- */
+
+/* Block Davidson for the lowest levels (sub_propagation_Davidson,
+ * SRC/sub_propagation/sub_module_Davidson.f90:59-767: new block H.psi
+ * sub_MakeHPsi_Davidson :896, projected H, sub_hermitic_H symmetrisation,
+ * residuals MakeResidual_Davidson :1230, Davidson correction
+ * sub_NewVec_Davidson :1306 with the H diagonal, restart at max_subspace).
+ * With symmetrize = 1 the operator is (H + H^T)/2, applied exactly through
+ * EVR_APPLY_TRANSPOSE, so the residual threshold is met for the symmetric
+ * part the reference diagonalises.  guess: device N x nguess (or NULL: the
+ * first nev packed functions); diag: device N (or NULL: plain residuals);
+ * evals/resid: host nev; evecs: device N x nev or NULL.  Returns
+ * EVR_ERR_NUMERIC if max_it is reached (evals/resid still filled). */
+typedef struct {
+  int nev;             /* number of lowest levels */
+  int block;           /* directions added per iteration (0 = nev) */
+  int max_subspace;    /* restart size (0 = max(3 nev, nev + 2 block)) */
+  int max_it;          /* iterations */
+  double conv_resi;    /* residual 2-norm threshold */
+  int symmetrize;      /* 1: work on (H + H^T)/2 */
+} evr_davidson_opts;
+int evr_sg4_davidson(evr_sg4_ctx* c, const evr_davidson_opts* o, const double* guess, int nguess,
+                     const double* diag, double* evals, double* evecs, double* resid, int* iterations,
+                     void* stream);
+
+/* Exact diagonal of H on the device (diag: device N), from H applied to
+ * blocks of unit vectors; the Davidson preconditioner. */
+int evr_sg4_diagonal(evr_sg4_ctx* c, double* diag, void* stream);
+
+/* Chebyshev propagation of complex wave packets (march_cheby,
+ * SRC/sub_propagation/sub_module_propa_march.f90:4145-4437; coefficients
+ * cof :5739): nsteps steps of dt, expansion order npoly on [Hmin, Hmax]
+ * (E0, Esc of sub_scaledOpPsi fused into each H.psi), early exit when
+ * |c_k| |w_k|^2 < poly_tol (poly_tol <= 0: always npoly terms), a step that
+ * diverges (> 1e15) redone with Hmax raised by (Hmax-Hmin)/10 up to 10 times.
+ * psi: device interleaved complex128 N x nrhs (ld N), propagated in place.
+ * autocorr: host complex [(nsteps+1) x nrhs] = <psi0 | psi(t_k)> (psi0 NULL:
+ * the initial psi), or NULL. */
+typedef struct {
+  double Hmin, Hmax;   /* spectral bounds of H */
+  double dt;           /* time step (a.u.) */
+  int npoly;           /* expansion order */
+  int nsteps;          /* number of steps */
+  double poly_tol;     /* convergence of the expansion, <= 0: fixed order */
+} evr_cheby_opts;
+int evr_sg4_cheby_propagate(evr_sg4_ctx* c, const evr_cheby_opts* o, int nrhs, double* psi, const double* psi0,
+                            double* autocorr, int* npoly_used, void* stream);
+
+/* Field-driven RK4 propagation of one complex packet (march_RK4_field,
+ * SRC/sub_propagation/sub_module_propa_march.f90:397-548; fcn_field
+ * :1439-1520): dpsi/dt = -i (H0 - E(t) mu) psi with E held at E[k] over
+ * field interval k ('grid' field), each interval integrated with nsub RK4
+ * steps.  H0 and mu are contexts on the same basis (mu a type-0 operator).
+ * psi: device complex128 N, propagated in place. */
+typedef struct {
+  double dt;           /* time step (a.u.) */
+  int nsteps;          /* number of steps = number of field samples */
+  int checkpoint;      /* oc_gradient: keep psi every `checkpoint` steps */
+  double E0;           /* energy shift: stages use H0 - E0, then psi *= exp(-i E0 dt)
+                          (fcn_field's para_H%E0; mid-spectrum keeps RK4 stable) */
+  int nsub;            /* RK4 steps per field interval (dt/nsub each, E held) */
+} evr_rk4_opts;
+int evr_sg4_rk4_field(evr_sg4_ctx* H0, evr_sg4_ctx* mu, const evr_rk4_opts* o, const double* E, double* psi,
+                      void* stream);
+
+/* Optimal-control objective J = |<target|psi(T)>|^2 after the RK4 propagation
+ * above from psi0, and its exact gradient dJ/dE[k] for every field sample,
+ * by the adjoint (costate) of the discrete RK4 steps; psi is checkpointed
+ * every o->checkpoint steps and recomputed.  This is the derivative the
+ * reference's field update uses in continuous form (build_field,
+ * SRC/sub_propagation/sub_control.f90:907-1010).  psi0/target: device
+ * complex128 N; E, grad: host [nsteps]; J: host scalar. */
+int evr_sg4_oc_gradient(evr_sg4_ctx* H0, evr_sg4_ctx* mu, const evr_rk4_opts* o, const double* E,
+                        const double* psi0, const double* target, double* J, double* grad, void* stream);
 
 /* Algorithmic FP64 operation count of one H.psi per right-hand side for the
  * current operator (flop, counted from the term sizes). */

@@ -40,8 +40,9 @@ def lib():
         L.orc_tables.argtypes = [ctypes.c_void_p, ip, dp, ip, ip]
         L.orc_basis1d.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int] + [dp] * 8
         L.orc_grid_points.argtypes = [ctypes.c_void_p, dp]
-        L.orc_hpsi.restype = ctypes.c_int
-        L.orc_hpsi.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, dp, dp, ctypes.c_int]
+        for fn in (L.orc_hpsi, L.orc_hpsi_ld):
+            fn.restype = ctypes.c_int
+            fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, dp, dp, ctypes.c_int]
         L.orc_gauss_hermite.argtypes = [ctypes.c_int, dp, dp, dp]
         _lib = L
     return _lib
@@ -123,8 +124,12 @@ class OracleSG4:
         lib().orc_grid_points(self.h, _dp(Q))
         return Q.reshape(self.sum_nq, self.D)
 
-    def hpsi(self, psi, type_op=10, V=None, G=None, Jac=None, sqRho=None, F2=None, F1=None, nthreads=0):
-        """psi: (N,) or (N, nrhs) float64, column-major per RHS."""
+    def hpsi(self, psi, type_op=10, V=None, G=None, Jac=None, sqRho=None, F2=None, F1=None, nthreads=0,
+             extended=False):
+        """psi: (N,) or (N, nrhs) float64, column-major per RHS.
+
+        extended=True runs the same algorithm with long-double intermediates
+        (the accuracy yardstick); the result is rounded to double."""
         psi = np.asarray(psi, dtype=np.float64)
         one = psi.ndim == 1
         P = psi.reshape(self.N, -1)
@@ -133,8 +138,30 @@ class OracleSG4:
         H = np.zeros_like(Pc)
         keep = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (V, G, Jac, sqRho, F2, F1)]
         op = _OrcOp(type_op, *[_dp(a) for a in keep])
-        rc = lib().orc_hpsi(self.h, ctypes.byref(op), nrhs, _dp(Pc), _dp(H), int(nthreads))
+        fn = lib().orc_hpsi_ld if extended else lib().orc_hpsi
+        rc = fn(self.h, ctypes.byref(op), nrhs, _dp(Pc), _dp(H), int(nthreads))
         if rc != 0:
             raise RuntimeError(f"orc_hpsi failed rc={rc}")
         H = H.T
         return H[:, 0] if one else H
+
+
+def oracle_tables(O: "OracleSG4"):
+    """The oracle's SG4 tables in the evr_sg4_desc layout (a dict of arrays)."""
+    D, L = O.D, O.L
+    nb_of_l, nq_of_l, xs, rgb, bgw, d1, d2 = [], [], [], [], [], [], []
+    for i in range(D):
+        for l in range(L + 1):
+            b = O.basis1d(i, l)
+            nb, nq = O.nb_nq(l)
+            nb_of_l.append(nb)
+            nq_of_l.append(nq)
+            xs.append(b["x"])
+            rgb.append(b["d0"].ravel(order="F"))
+            bgw.append(b["bgw"].ravel(order="F"))
+            d1.append(b["d1gg"].ravel(order="F"))
+            d2.append(b["d2gg"].ravel(order="F"))
+    tab_l, w, m, _ = O.tables()
+    return dict(D=D, L=L, LB=O.LB, nb_of_l=np.array(nb_of_l), nq_of_l=np.array(nq_of_l),
+                x=np.concatenate(xs), RGB=np.concatenate(rgb), RBGwrho=np.concatenate(bgw),
+                d1GG=np.concatenate(d1), d2GG=np.concatenate(d2), tab_l=tab_l, weight=w, map_=m, N=O.N)

@@ -498,191 +498,19 @@ void orc_grid_points(const orc_sg4* s, double* Q) {
 }
 
 /* ------------------------------------------------------------------------ */
-/* Per-term kernels (reference loop order).                                  */
+/* Per-term kernels, instantiated in double and in long double.              */
 /* ------------------------------------------------------------------------ */
-
-/* out[S][nout][R] = M(nout x nin, column-major, leading dim ldm) applied to
- * in[S][nin][R] along the middle index; RB_TO_RG_basis / RG_TO_RB_basis
- * (sub_module_basis_set_alloc.f90:2148-2287) is matmul(Mat, fibre). */
-static void mode_apply(const double* M, int ldm, int nout, int nin, long long S, long long R,
-                       const double* in, double* out) {
-  for (long long r = 0; r < R; ++r)
-    for (long long a = 0; a < S; ++a) {
-      const double* fi = in + a + S * nin * r;
-      double* fo = out + a + S * nout * r;
-      for (int k = 0; k < nout; ++k) {
-        double acc = 0.0;
-        for (int m = 0; m < nin; ++m) acc += M[k + (long long)ldm * m] * fi[S * m];
-        fo[S * k] = acc;
-      }
-    }
-}
-
-/* BDP_TO_GDP_OF_SmolyakRep (sub_module_basis_BtoG_GtoB_SG4.f90:2383-2484) */
-static void b_to_g(const orc_sg4* s, const int* l, double* buf0, double* buf1, double** res) {
-  int D = s->D;
-  long long S = 1, R = 1;
-  for (int i = 0; i < D; ++i) R *= s->b[i * (s->L + 1) + l[i]].nb;
-  double *in = buf0, *out = buf1;
-  for (int i = 0; i < D; ++i) {
-    const orc_basis1* b = &s->b[i * (s->L + 1) + l[i]];
-    R /= b->nb;
-    mode_apply(b->d0, b->nq, b->nq, b->nb, S, R, in, out);
-    S *= b->nq;
-    double* t = in; in = out; out = t;
-  }
-  *res = in;
-}
-
-/* GDP_TO_BDP_OF_SmolyakRep (sub_module_basis_BtoG_GtoB_SG4.f90:2485-2561) */
-static void g_to_b(const orc_sg4* s, const int* l, double* buf0, double* buf1, double** res) {
-  int D = s->D;
-  long long S = 1, R = 1;
-  for (int i = 0; i < D; ++i) R *= s->b[i * (s->L + 1) + l[i]].nq;
-  double *in = buf0, *out = buf1;
-  for (int i = 0; i < D; ++i) {
-    const orc_basis1* b = &s->b[i * (s->L + 1) + l[i]];
-    R /= b->nq;
-    mode_apply(b->bgw, b->nb, b->nb, b->nq, S, R, in, out);
-    S *= b->nb;
-    double* t = in; in = out; out = t;
-  }
-  *res = in;
-}
-
-/* DerivOp_TO_RDP_OF_SmolaykRep (sub_module_basis_BtoG_GtoB_SG4.f90:2670-2775):
- * der = (i, j) 1-based mode indices, 0 = none; per mode, d2GG when both hit
- * the mode, d1GG when one does.  In place, using tmp. */
-static void deriv_op(const orc_sg4* s, const int* l, int di, int dj, double* R_, double* tmp) {
-  int D = s->D;
-  if (di == 0 && dj == 0) return;
-  long long nq = 1;
-  for (int i = 0; i < D; ++i) nq *= s->b[i * (s->L + 1) + l[i]].nq;
-  long long S = 1, R = nq;
-  for (int i = 0; i < D; ++i) {
-    const orc_basis1* b = &s->b[i * (s->L + 1) + l[i]];
-    R /= b->nq;
-    int hit = (di == i + 1) + (dj == i + 1);
-    if (hit) {
-      const double* M = (hit == 2) ? b->d2gg : b->d1gg;
-      mode_apply(M, b->nq, b->nq, b->nq, S, R, R_, tmp);
-      memcpy(R_, tmp, sizeof(double) * nq);
-    }
-    S *= b->nq;
-  }
-}
-
-int orc_hpsi(const orc_sg4* s, const orc_op* op, int nrhs, const double* psi, double* hpsi,
-             int nthreads) {
-  const int D = s->D;
-  const long long N = s->N;
-  if (!op || (op->type != 0 && op->type != 1 && op->type != 10)) return 1;
-  memset(hpsi, 0, sizeof(double) * N * nrhs);
-#ifdef _OPENMP
-  if (nthreads <= 0) nthreads = omp_get_max_threads();
-#else
-  nthreads = 1;
-#endif
-  const int nbuf = D + 4;
-#pragma omp parallel num_threads(nthreads)
-  {
-    double* work = (double*)malloc(sizeof(double) * (size_t)s->max_nq * nbuf);
-    double* A = work;
-    double* B = work + s->max_nq;
-    double* C = work + 2 * (size_t)s->max_nq;
-    double* Uu = work + 3 * (size_t)s->max_nq;
-    double* Phi = work + 4 * (size_t)s->max_nq;   /* D arrays */
-#pragma omp for schedule(static)
-    for (long long t = 0; t < s->nb_SG; ++t) {
-      const int* l = s->tab_l + t * D;
-      const long long nb_t = s->off_nb[t + 1] - s->off_nb[t];
-      const long long nq_t = s->off_nq[t + 1] - s->off_nq[t];
-      const long long oq = s->off_nq[t];
-      const int* map = s->map + s->off_nb[t];
-      for (int r = 0; r < nrhs; ++r) {
-        /* tabPackedBasis_TO_tabR_AT_iG (sub_module_basis_BtoG_GtoB_SG4.f90:1181-1251) */
-        for (long long k = 0; k < nb_t; ++k) {
-          int n = map[k];
-          A[k] = (n > 0 && n <= N) ? psi[(long long)r * N + n - 1] : 0.0;
-        }
-        double* x;
-        b_to_g(s, l, A, B, &x);
-        double* y = (x == A) ? B : A;                /* free buffer */
-        if (op->type == 0) {
-          /* CASE (0), sub_OpPsi_SG4.f90:1446-1486 */
-          for (long long p = 0; p < nq_t; ++p) y[p] = 0.0 + (op->V ? op->V[oq + p] : 0.0) * x[p];
-        } else if (op->type == 1) {
-          /* CASE (1), sub_OpPsi_SG4.f90:1488-1544; terms in Init_TypeOp order
-           * (0,0), (i,j>=i), (i,0) (Tnum-Tana .../sub_module_SimpleOp.f90:127-415) */
-          for (long long p = 0; p < nq_t; ++p) y[p] = 0.0;
-          if (op->V)
-            for (long long p = 0; p < nq_t; ++p) y[p] = y[p] + op->V[oq + p] * x[p];
-          for (int i = 1; i <= D; ++i)
-            for (int j = i; j <= D; ++j) {
-              double f = op->F2 ? op->F2[(i - 1) * D + (j - 1)] : 0.0;
-              if (f == 0.0) continue;               /* grid_zero: skipped */
-              memcpy(C, x, sizeof(double) * nq_t);
-              deriv_op(s, l, i, j, C, Uu);
-              for (long long p = 0; p < nq_t; ++p) y[p] = y[p] + f * C[p];
-            }
-          for (int i = 1; i <= D; ++i) {
-            double f = op->F1 ? op->F1[i - 1] : 0.0;
-            if (f == 0.0) continue;
-            memcpy(C, x, sizeof(double) * nq_t);
-            deriv_op(s, l, i, 0, C, Uu);
-            for (long long p = 0; p < nq_t; ++p) y[p] = y[p] + f * C[p];
-          }
-        } else {
-          /* CASE (10), sub_OpPsi_SG4.f90:1546-1630 */
-          double* VPsi = C;
-          for (long long p = 0; p < nq_t; ++p) VPsi[p] = 0.0 + (op->V ? op->V[oq + p] : 0.0) * x[p];
-          if (op->sqRho)
-            for (long long p = 0; p < nq_t; ++p) x[p] = x[p] * op->sqRho[oq + p];
-          for (int j = 0; j < D; ++j) {
-            double* phj = Phi + (size_t)j * s->max_nq;
-            memcpy(phj, x, sizeof(double) * nq_t);
-            deriv_op(s, l, j + 1, 0, phj, Uu);
-          }
-          for (long long p = 0; p < nq_t; ++p) y[p] = 0.0;
-          for (int i = 0; i < D; ++i) {
-            for (long long p = 0; p < nq_t; ++p) Uu[p] = 0.0;
-            for (int j = 0; j < D; ++j) {
-              const double* phj = Phi + (size_t)j * s->max_nq;
-              if (op->G) {
-                const double* g = op->G + oq * D * D + nq_t * (j + (long long)D * i);
-                for (long long p = 0; p < nq_t; ++p) Uu[p] = Uu[p] + g[p] * phj[p];
-              } else if (i == j) {
-                for (long long p = 0; p < nq_t; ++p) Uu[p] = Uu[p] + 1.0 * phj[p];
-              }
-            }
-            if (op->Jac)
-              for (long long p = 0; p < nq_t; ++p) Uu[p] = Uu[p] * op->Jac[oq + p];
-            deriv_op(s, l, i + 1, 0, Uu, x);          /* x is free now: tmp */
-            for (long long p = 0; p < nq_t; ++p) y[p] = y[p] + Uu[p];
-          }
-          for (long long p = 0; p < nq_t; ++p) {
-            double jac = op->Jac ? op->Jac[oq + p] : 1.0;
-            double sq = op->sqRho ? op->sqRho[oq + p] : 1.0;
-            y[p] = -0.5 * y[p] / (jac * sq) + VPsi[p];
-          }
-        }
-        /* y -> basis, reusing the buffer that is not y */
-        double* other = (y == A) ? B : A;
-        double* yb;
-        g_to_b(s, l, y, other, &yb);
-        /* tabR_AT_iG_TO_tabPackedBasis (sub_module_basis_BtoG_GtoB_SG4.f90:1255-1294) */
-        const double wt = s->weight[t];
-        for (long long k = 0; k < nb_t; ++k) {
-          int n = map[k];
-          if (n > 0 && n <= N) {
-            double v = wt * yb[k];
-#pragma omp atomic
-            hpsi[(long long)r * N + n - 1] += v;
-          }
-        }
-      }
-    }
-    free(work);
-  }
-  return 0;
-}
+#define REAL double
+#define ORC_FN(name) name##_d
+#define ORC_HPSI_NAME orc_hpsi
+#include "sg4_oracle_hpsi.inc"
+#undef REAL
+#undef ORC_FN
+#undef ORC_HPSI_NAME
+#define REAL long double
+#define ORC_FN(name) name##_ld
+#define ORC_HPSI_NAME orc_hpsi_ld
+#include "sg4_oracle_hpsi.inc"
+#undef REAL
+#undef ORC_FN
+#undef ORC_HPSI_NAME

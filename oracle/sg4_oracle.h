@@ -72,6 +72,11 @@ typedef struct {
 int orc_hpsi(const orc_sg4* s, const orc_op* op, int nrhs, const double* psi,
              double* hpsi, int nthreads);
 
+/* Same as orc_hpsi with every intermediate in long double (x87 80-bit on
+ * x86-64, IEEE binary128 on aarch64): the accuracy yardstick for the tests. */
+int orc_hpsi_ld(const orc_sg4* s, const orc_op* op, int nrhs, const double* psi,
+                double* hpsi, int nthreads);
+
 /* Gauss-Hermite quadrature of nq points: x[nq], w[nq] (weight for exp(-x^2) f),
  * wrho[nq] = w exp(x^2).  Restates hercom/herm*.txt (sub_quadra_herm.f90:48-244). */
 void orc_gauss_hermite(int nq, double* x, double* w, double* wrho);

@@ -12,9 +12,9 @@ import pytest
 
 torch = pytest.importorskip("torch")
 
-from elvibrot_gb300 import EVRError, ParamOp, Polynomial, SG4Basis, sub_scaledOpPsi, sub_TabOpPsi
+from elvibrot_gb300 import EVRError, ParamOp, Polynomial, SG4Basis, SG4Tables, sub_scaledOpPsi, sub_TabOpPsi
 from elvibrot_gb300.configs import make_model, random_psi
-from oracle.oracle import OracleSG4
+from oracle.oracle import OracleSG4, oracle_tables
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-12
@@ -51,17 +51,39 @@ def oracle_for(model):
     return O, kw
 
 
+def same_inputs_op(O, kw):
+    """GPU operator built from the oracle's own tables and operator grids
+    (the drop-in descriptor path: bit-identical inputs on both sides)."""
+    T = SG4Tables(**oracle_tables(O))
+    if kw["type_op"] == 1:
+        return ParamOp(T, 1, V=kw.get("V"), F2=kw.get("F2"), F1=kw.get("F1"))
+    if kw["type_op"] == 0:
+        return ParamOp(T, 0, V=kw.get("V"))
+    return ParamOp(T, 10, V=kw.get("V"), G=kw.get("G"), Jac=kw.get("Jac"), sqRho=kw.get("sqRho"))
+
+
+def check_against_oracle(op, O, kw, psi, label):
+    """GPU vs the oracle in double and in extended precision (the yardstick)."""
+    got = gpu_apply(op, psi)
+    ref = O.hpsi(psi, **kw)
+    # extended precision is software binary128 on aarch64: two columns suffice
+    ext = O.hpsi(psi[:, :2], extended=True, **kw)
+    e_ext, e_ref, e_orc = rel_err(got[:, :2], ext), rel_err(got, ref), rel_err(ref[:, :2], ext)
+    print(f"{label}: gpu-vs-extended {e_ext:.2e}  gpu-vs-double {e_ref:.2e}  double-vs-extended {e_orc:.2e}")
+    assert e_ext <= TOL and e_ref <= TOL
+    return got
+
+
 @pytest.mark.parametrize("D,L,type_op,nrhs", [(3, 6, 1, 1), (3, 6, 1, 5), (4, 5, 10, 7), (6, 4, 10, 3),
                                               (5, 5, 1, 4), (2, 9, 10, 2)])
 def test_hpsi_matches_oracle(D, L, type_op, nrhs):
     need_cuda()
     m = make_model(D, L, type_op, 1234 + D * 10 + L)
-    op = m.operator()
-    psi = random_psi(op.basis.N, nrhs, 99)
     O, kw = oracle_for(m)
-    ref = O.hpsi(psi, **kw)
-    got = gpu_apply(op, psi)
-    assert rel_err(got, ref) <= TOL
+    psi = random_psi(O.N, nrhs, 99)
+    check_against_oracle(same_inputs_op(O, kw), O, kw, psi, f"{D}-D L={L} type {type_op} (oracle tables)")
+    op = m.operator()   # product tables + device-evaluated fields
+    check_against_oracle(op, O, kw, psi, f"{D}-D L={L} type {type_op} (product tables)")
     assert op.last_launches == 2
 
 
@@ -125,24 +147,25 @@ def test_large_terms_use_global_scratch():
     need_cuda()
     # a 7-D L=9 type-10 basis has terms whose D+4 work arrays exceed shared memory
     m = make_model(7, 9, 10, 4242)
-    op = m.operator()
-    assert op.basis.max_nq * (7 + 4) > 110 * 1024 // 8
-    psi = random_psi(op.basis.N, 2, 8)
     O, kw = oracle_for(m)
-    assert rel_err(gpu_apply(op, psi), O.hpsi(psi, **kw)) <= TOL
+    psi = random_psi(O.N, 2, 8)
+    op = same_inputs_op(O, kw)
+    assert op.basis.max_nq * (7 + 4) > 110 * 1024 // 8
+    check_against_oracle(op, O, kw, psi, "7-D L=9 type 10 (oracle tables, global scratch)")
+    del op
+    check_against_oracle(m.operator(), O, kw, psi, "7-D L=9 type 10 (product tables, global scratch)")
 
 
 def test_benchmark_6d_workload_full_size():
     need_cuda()
     # 6-D L=8, Q-dependent G, 20 right-hand sides (the benchmark workload)
     m = make_model(6, 8, 10, 20261204)
+    O, kw = oracle_for(m)
+    psi = random_psi(O.N, 20, 20261204)
+    check_against_oracle(same_inputs_op(O, kw), O, kw, psi, "6-D L=8 type 10 x20 (oracle tables)")
     op = m.operator()
     assert (op.basis.N, op.basis.nb_SG, op.basis.sum_nq) == (3003, 2975, 1953127)
-    psi = random_psi(op.basis.N, 20, 20261204)
-    O, kw = oracle_for(m)
-    ref = O.hpsi(psi, **kw)
-    got = gpu_apply(op, psi)
-    assert rel_err(got, ref) <= TOL
+    got = check_against_oracle(op, O, kw, psi, "6-D L=8 type 10 x20 (product tables)")
     # linearity: H(a x + b y) = a Hx + b Hy
     comb = gpu_apply(op, 0.3 * psi[:, :1] - 1.7 * psi[:, 1:2])
     assert rel_err(comb, 0.3 * got[:, :1] - 1.7 * got[:, 1:2]) <= TOL
@@ -181,3 +204,38 @@ def test_errors_are_status_codes():
     psi = random_psi(N, 1, 1)
     O, kw = oracle_for(m)
     assert rel_err(gpu_apply(op, psi), O.hpsi(psi, **kw)) <= TOL
+
+
+@pytest.mark.parametrize("type_op", [0, 1, 10])
+def test_transposed_operator_matches_dense_transpose(type_op):
+    """evr_sg4_apply(EVR_APPLY_TRANSPOSE) = (dense oracle H)^T, with non-symmetric
+    G and general Jac/rho so every swapped index and scaling is exercised."""
+    need_cuda()
+    D, L = 4, 4
+    b = SG4Basis(D, L, scaleQ=np.full(D, 0.5))
+    O = OracleSG4(D, L, L, 1, 1, 2, 1, scaleQ=np.full(D, 0.5))
+    rng = np.random.default_rng(11 + type_op)
+    kw = dict(type_op=type_op, V=rng.normal(size=b.sum_nq))
+    if type_op == 1:
+        kw.update(F2=np.triu(rng.normal(size=(D, D))).ravel(), F1=rng.normal(size=D))
+        op = ParamOp(b, 1, V=kw["V"], F2=kw["F2"], F1=kw["F1"])
+    elif type_op == 10:
+        kw.update(G=rng.normal(size=b.sum_nq * D * D), Jac=rng.uniform(0.5, 2, b.sum_nq),
+                  sqRho=rng.uniform(0.5, 2, b.sum_nq))
+        op = ParamOp(b, 10, V=kw["V"], G=kw["G"], Jac=kw["Jac"], sqRho=kw["sqRho"])
+    else:
+        op = ParamOp(b, 0, V=kw["V"])
+    H = O.hpsi(np.eye(O.N), **kw)
+    psi = random_psi(O.N, 3, 2)
+    P = torch.from_numpy(np.ascontiguousarray(psi.T)).cuda()
+    out = torch.empty_like(P)
+    op.hpsi_dev(P, out, transpose=True)
+    torch.cuda.synchronize()
+    assert rel_err(out.cpu().numpy().T, H.T @ psi) <= TOL
+    # complex psi through the transposed operator
+    pc = random_psi(O.N, 2, 3, complex_=True)
+    Pc = torch.from_numpy(np.ascontiguousarray(pc.T)).cuda()
+    oc = torch.empty_like(Pc)
+    op.hpsi_dev(Pc, oc, transpose=True)
+    torch.cuda.synchronize()
+    assert rel_err(oc.cpu().numpy().T, H.T @ pc) <= TOL
