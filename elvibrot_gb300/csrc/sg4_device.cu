@@ -1383,3 +1383,107 @@ extern "C" int evr_probe_fp64_peak(double* tflops) {
   *tflops = 2.0 * 8 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
   return EVR_OK;
 }
+
+// ------------------------------------------------------------------------
+// H.psi without device allocation.
+//
+// Some callers cannot call cudaMalloc: code running inside a caller-owned
+// memory budget (a host program whose allocator owns every device byte), a
+// real-time loop that must not hit the driver's allocator, or a host thread
+// that is not allowed to change the device heap between two CUDA-graph
+// launches.  evr_sg4_hpsi_noalloc gives them the batched kernel with all of
+// its scratch -- the work counter, the work list, the per-term contributions
+// and the per-CTA slabs for terms larger than shared memory -- carved from
+// one fixed, file-scope device array instead of device allocations.
+//
+// The array (EVR_SG4_NOALLOC_SCRATCH_BYTES) exists on every device that
+// loads this library and stays resident until the process exits.  Every
+// call shares it and it keeps the previous call's contents: the counter is
+// cleared at the start of each call and every other byte a call reads is
+// written by that call first.  Two calls whose kernels overlap on the GPU
+// (different streams, or different host threads) race on the array: keep
+// calls on one stream, or serialise them.
+// ------------------------------------------------------------------------
+static __device__ __align__(256) unsigned char g_noalloc_scratch[EVR_SG4_NOALLOC_SCRATCH_BYTES];
+
+namespace evr {
+static std::mutex g_noalloc_mu;
+static unsigned char* g_noalloc_ptr[64];  // device address of the array, per device
+}  // namespace evr
+
+extern "C" int evr_sg4_hpsi_noalloc(evr_sg4_ctx* c, int nrhs, const double* psi, long long ldpsi,
+                                    double* hpsi, long long ldh, double E0, double Esc, void* stream) {
+  if (!c) return set_error(EVR_ERR_ARG, "hpsi_noalloc: NULL context");
+  if (!c->have_op) return set_error(EVR_ERR_STATE, "hpsi_noalloc: set_operator was not called");
+  if (nrhs < 1) return set_error(EVR_ERR_ARG, "hpsi_noalloc: nrhs=%d", nrhs);
+  if (!psi || !hpsi) return set_error(EVR_ERR_ARG, "hpsi_noalloc: NULL vector");
+  if (ldpsi < c->N || ldh < c->N) return set_error(EVR_ERR_ARG, "hpsi_noalloc: leading dimension < N=%lld", c->N);
+  if (!(Esc != 0.0) || !std::isfinite(Esc) || !std::isfinite(E0))
+    return set_error(EVR_ERR_ARG, "hpsi_noalloc: Esc must be finite and non-zero");
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64 || dev != c->device)
+    return set_error(EVR_ERR_STATE, "hpsi_noalloc: current device %d is not the context's device %d", dev, c->device);
+  unsigned char* base = nullptr;
+  {
+    // set-up, once per device with that device current: the device address of
+    // the array (its host-side name is only a stand-in, never passed to a kernel)
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+      void* ptr = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+      if (e != cudaSuccess || !ptr)
+        return set_error(EVR_ERR_CUDA, "hpsi_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+      g_noalloc_ptr[dev] = (unsigned char*)ptr;
+    }
+    base = g_noalloc_ptr[dev];
+  }
+  cudaPointerAttributes a1, a2;
+  if (cudaPointerGetAttributes(&a1, psi) != cudaSuccess || cudaPointerGetAttributes(&a2, hpsi) != cudaSuccess ||
+      a1.type != cudaMemoryTypeDevice || a2.type != cudaMemoryTypeDevice) {
+    cudaGetLastError();
+    return set_error(EVR_ERR_ARG, "hpsi_noalloc: psi and hpsi must be device pointers");
+  }
+  const int nrhs_v = nrhs;
+  std::vector<Item> items, sorted;
+  long long max_need = 0;
+  plan_items(c, nrhs_v, items, sorted, max_need);
+  c->items_nrhs = -1;  // the allocating path rebuilds its own list next time
+  // carve: [counter | items | contributions | large-term slabs], 256-byte aligned
+  auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const size_t off_items = 256;
+  const size_t off_contrib = off_items + up(sorted.size() * sizeof(Item));
+  const size_t off_slabs = off_contrib + up((size_t)c->z.sum_nb * nrhs_v * 8);
+  const long long per_cta = max_need > c->smem_doubles ? max_need : 0;
+  // with large-term slabs, launch only as many CTAs as the array has slabs for
+  int grid = c->grid;
+  if (per_cta > 0 && off_slabs < (size_t)EVR_SG4_NOALLOC_SCRATCH_BYTES)
+    grid = (int)std::min<long long>(c->grid, ((size_t)EVR_SG4_NOALLOC_SCRATCH_BYTES - off_slabs) / ((size_t)per_cta * 8));
+  const size_t total = off_slabs + (size_t)per_cta * std::max(grid, 1) * 8;
+  if (grid < 1 || total > (size_t)EVR_SG4_NOALLOC_SCRATCH_BYTES)
+    return set_error(EVR_ERR_ARG,
+                     "hpsi_noalloc: this operator and nrhs=%d need %zu bytes of scratch, more than the fixed "
+                     "%u-byte array; use evr_sg4_hpsi or fewer right-hand sides",
+                     nrhs, total, (unsigned)EVR_SG4_NOALLOC_SCRATCH_BYTES);
+  cudaStream_t s = (cudaStream_t)stream;
+  CUDA_TRY(cudaMemcpyAsync(c->d_terms, c->terms.data(), c->terms.size() * sizeof(TermInfo),
+                           cudaMemcpyHostToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(base + off_items, sorted.data(), sorted.size() * sizeof(Item), cudaMemcpyHostToDevice, s));
+  CUDA_TRY(cudaMemsetAsync(base, 0, sizeof(unsigned int), s));
+  KParams p = make_params(c, nrhs_v, 0, psi, ldpsi, hpsi, ldh, 1.0);
+  p.items = (const Item*)(base + off_items);
+  p.n_items = (int)sorted.size();
+  p.counter = (unsigned int*)base;
+  p.contrib = (double*)(base + off_contrib);
+  p.gscratch = per_cta ? (double*)(base + off_slabs) : nullptr;
+  p.scratch_per_cta = per_cta;
+  hpsi_batched_kernel<<<grid, 256, (size_t)c->smem_doubles * 8, s>>>(p);
+  CUDA_TRY(cudaGetLastError());
+  int rc = launch_reduce(c, p.contrib, nrhs_v, 0, psi, ldpsi, hpsi, ldh, E0, Esc, s);
+  if (rc) return rc;
+  CUDA_TRY(cudaGetLastError());
+  // (both host lists were copied from pageable memory, which cudaMemcpyAsync
+  // stages before it returns, so they may go out of scope now)
+  c->last_launches = 2;
+  return EVR_OK;
+}

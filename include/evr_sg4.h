@@ -179,6 +179,23 @@ int evr_sg4_apply(evr_sg4_ctx* c, int flags, int nrhs, const double* psi, long l
 int evr_sg4_hpsi_host(evr_sg4_ctx* c, int nrhs, const double* psi, long long ldpsi, double* hpsi,
                       long long ldh, double E0, double Esc);
 
+/* H.psi that allocates no device memory (no counterpart in the reference).
+ * For callers that cannot call cudaMalloc -- a host program whose own
+ * allocator owns the device memory, a real-time loop that must stay out of
+ * the driver's allocator -- this runs the same batched kernel as
+ * evr_sg4_hpsi with its scratch (work counter, work list, per-term
+ * contributions, slabs for terms larger than shared memory) carved from one
+ * fixed file-scope device array of EVR_SG4_NOALLOC_SCRATCH_BYTES, which every
+ * GPU that loads the library holds until the process exits.  Sizes that need
+ * more scratch are rejected with EVR_ERR_ARG.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress); make that first
+ * call before any stream capture.  All calls share the array: calls that
+ * overlap on the GPU (two streams or two threads) race.  Real psi only;
+ * device pointers; same result as evr_sg4_hpsi. */
+#define EVR_SG4_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+int evr_sg4_hpsi_noalloc(evr_sg4_ctx* c, int nrhs, const double* psi, long long ldpsi, double* hpsi,
+                         long long ldh, double E0, double Esc, void* stream);
+
 /* Sizes of a context: out[0..7] as evr_sg4_desc_sizes. */
 int evr_sg4_ctx_sizes(const evr_sg4_ctx* c, long long* out);
 
