@@ -45,11 +45,11 @@ class SG4Model:
     def basis(self) -> SG4Basis:
         return SG4Basis(self.D, self.L, self.L, 1, 1, 2, 1, Q0=np.zeros(self.D), scaleQ=self.scaleQ)
 
-    def operator(self, basis: Optional[SG4Basis] = None) -> ParamOp:
+    def operator(self, basis: Optional[SG4Basis] = None, field_budget: int = 0) -> ParamOp:
         b = basis if basis is not None else self.basis()
         if self.type_op == 1:
-            return ParamOp(b, 1, V_poly=self.V, F2=self.F2)
-        return ParamOp(b, 10, V_poly=self.V, G0=self.G0, G1=self.G1)
+            return ParamOp(b, 1, V_poly=self.V, F2=self.F2, field_budget=field_budget)
+        return ParamOp(b, 10, V_poly=self.V, G0=self.G0, G1=self.G1, field_budget=field_budget)
 
     def G_grid(self, Q: np.ndarray, nq_per_term: np.ndarray) -> np.ndarray:
         """GGiq(iq, j, i) per term, concatenated (what the oracle consumes)."""

@@ -11,10 +11,12 @@
 // work item of one H.psi: CTAs pull items from a cost-sorted list through a
 // global atomic counter, keep the whole term in shared memory (a per-CTA
 // slab of global scratch when a term does not fit), apply the 1-D matrices
-// mode by mode with one thread per fibre, and scatter with FP64 atomics.
+// mode by mode with one thread per fibre, and write each term's weighted
+// result to a contribution buffer that two small kernels then sum per packed
+// function in Smolyak-term order (compensated, deterministic, no atomics).
 // GB300's FP64 pipe (~1.2 TFLOP/s measured) is the binding resource, so the
-// kernel is organised to keep it busy: two CTAs per SM so one computes while
-// the other gathers/synchronises, right-hand sides batched per item so the
+// kernel is organised to keep it busy: four CTAs per SM so some compute while
+// the others gather or synchronise, right-hand sides batched per item so the
 // 1-D matrices and the operator fields are loaded once per point, and no
 // FP64 work spent on anything but the algorithm's own multiply-adds.
 #include <cuda_runtime.h>
@@ -31,6 +33,7 @@
 
 #include "evr_sg4.h"
 #include "sg4_internal.h"
+#include "sg4_reduce.cuh"
 
 namespace evr {
 
@@ -57,7 +60,7 @@ int desc_sizes(const evr_sg4_desc* d, DescSizes* z) {
   if (!d) return set_error(EVR_ERR_ARG, "descriptor is NULL");
   if (d->D < 1 || d->D > EVR_MAXD) return set_error(EVR_ERR_ARG, "D=%d outside [1,%d]", d->D, EVR_MAXD);
   if (d->L < 0) return set_error(EVR_ERR_ARG, "L < 0");
-  if (d->nb0 != 1) return set_error(EVR_ERR_ARG, "nb0=%d: only nb0=1 is supported", d->nb0);
+  if (d->nb0 < 1 || d->nb0 > EVR_MAXNB0) return set_error(EVR_ERR_ARG, "nb0=%d outside [1,%d]", d->nb0, EVR_MAXNB0);
   if (d->nb_SG < 1 || d->N < 1) return set_error(EVR_ERR_ARG, "empty basis (nb_SG=%lld, N=%lld)", d->nb_SG, d->N);
   if (!d->nb_of_l || !d->nq_of_l || !d->tab_l || !d->weight || !d->map)
     return set_error(EVR_ERR_ARG, "descriptor has NULL tables");
@@ -86,7 +89,19 @@ int desc_sizes(const evr_sg4_desc* d, DescSizes* z) {
 }
 
 // ------------------------------------------------------------------ device
+#ifndef EVR_FUSED_MAXD
 #define EVR_FUSED_MAXD 12  // type-10 items with D <= 12 use the fused grid passes
+#endif
+// persistent H.psi launch: threads per CTA and resident CTAs per SM.  Four
+// 128-thread CTAs (55 KB of shared memory each, 128 registers a thread) beat
+// two 256-thread ones by 0.7 % on the 6-D benchmark and let the ~600 items of
+// a small operator run in one wave.
+#ifndef EVR_CTA_THREADS
+#define EVR_CTA_THREADS 128
+#endif
+#ifndef EVR_CTAS_PER_SM
+#define EVR_CTAS_PER_SM 4
+#endif
 
 struct TermInfo {
   long long off_nb;   // into map
@@ -101,6 +116,11 @@ struct TermInfo {
 struct Item {
   int term;
   int rhs0;
+};
+
+// a work item of a launch over several contexts (context index first)
+struct MItem {
+  int ctx, term, rhs0, pad;
 };
 
 // 1-D matrices of (mode, level), row-major [nout][nin] for the kernel.
@@ -150,6 +170,10 @@ struct KParams {
   double* contrib;           // [sum_nb][nrhs_v] weighted term contributions
   const double* cfac;        // [sum_nq] -1/2/(Jac sqRho) or NULL (= -1/2)
   long long sum_nb;
+  long long fbase;           // grid point of the first field entry (term slices)
+  int nb0;                   // channels (electronic states): a vector is nb0 blocks of Nfun
+  long long Nfun;            // packed basis functions per channel
+  long long vstride;         // V[(a*nb0 + b)*vstride + point] for nb0 > 1
 };
 
 struct ItemShared {
@@ -163,8 +187,27 @@ struct ItemShared {
 };
 
 __device__ __forceinline__ long long vaddr(const KParams& p, int v, int n, long long ld) {
-  // element n (0-based, packed index) of virtual right-hand side v
-  return (long long)(v >> p.cshift) * ld + ((long long)n << p.cshift) + (v & p.cshift);
+  // element n (0-based, packed index) of virtual right-hand side v: column
+  // v >> cshift is channel a of right-hand side j (RvecB((a-1)*Max_nDI + n))
+  const int col = v >> p.cshift;
+  const int j = col / p.nb0, a = col - j * p.nb0;
+  return (long long)j * ld + (((long long)a * p.Nfun + n) << p.cshift) + (v & p.cshift);
+}
+
+// y(j,a) = sum_b V_ab x(j,b) at grid point q for nb0 > 1: the electronic
+// matrix of the operator (OpGrid(iterm)%Grid(:,a,b) of the reference) couples
+// the channels of one right-hand side; the item holds whole channel groups.
+__device__ __forceinline__ double vmat_apply(const KParams& p, const double* xs, int e, int nqt, long long oq,
+                                             int rhs0) {
+  const int q = e % nqt, jj = e / nqt;
+  const int a = ((rhs0 + jj) >> p.cshift) % p.nb0;
+  double y = 0.0;
+  for (int b = 0; b < p.nb0; ++b) {
+    const int jb = jj + ((b - a) << p.cshift);
+    const int ab = p.transpose ? b * p.nb0 + a : a * p.nb0 + b;
+    y = fma(__ldg(p.V + (long long)ab * p.vstride + oq + q), xs[jb * nqt + q], y);
+  }
+  return y;
 }
 
 // out[a + S*(k + nout*b)] (+)= scale * sum_m M[k*NIN+m] in[a + S*(m + NIN*b)]
@@ -376,9 +419,10 @@ __device__ void type10_fused(const KParams& p, const ItemShared& it, const doubl
 __device__ void type10_fused_dispatch(const KParams& p, const ItemShared& it, const double* x, double* O, double* U,
                                       int NQR) {
   switch (p.D) {
-#define EVR_T10(n) \
-  case n:          \
-    type10_fused<n>(p, it, x, O, U, NQR); break;
+#define EVR_T10(n)                                                        \
+  case n:                                                                 \
+    if constexpr (n <= EVR_FUSED_MAXD) type10_fused<n>(p, it, x, O, U, NQR); \
+    break;
     EVR_T10(1) EVR_T10(2) EVR_T10(3) EVR_T10(4) EVR_T10(5) EVR_T10(6) EVR_T10(7) EVR_T10(8) EVR_T10(9)
     EVR_T10(10) EVR_T10(11) EVR_T10(12)
 #undef EVR_T10
@@ -387,7 +431,7 @@ __device__ void type10_fused_dispatch(const KParams& p, const ItemShared& it, co
 }
 
 // The weighted term result WeightSG(l) * y_b goes to contrib[off_nb + k][v]
-// (no atomics); hpsi_reduce_kernel adds the contributions of each packed
+// (no atomics); the two reduce kernels add the contributions of each packed
 // function in Smolyak-term order, as tabR_AT_iG_TO_tabPackedBasis
 // accumulates them (sub_module_basis_BtoG_GtoB_SG4.f90:1255-1294).
 __device__ void store_contrib(const KParams& p, const ItemShared& it, const double* yb) {
@@ -402,15 +446,14 @@ __device__ void store_contrib(const KParams& p, const ItemShared& it, const doub
   __syncthreads();
 }
 
-__device__ void run_item(const KParams& p, ItemShared& it, double* smem, int item_idx) {
+__device__ void run_item(const KParams& p, ItemShared& it, double* smem, int term, int rhs0) {
   if (threadIdx.x == 0) {
-    const Item itm = p.items[item_idx];
-    const TermInfo& T = p.terms[itm.term];
-    it.term = itm.term;
-    it.rhs0 = itm.rhs0;
-    it.r = min(T.r, p.nrhs_v - itm.rhs0);
+    const TermInfo& T = p.terms[term];
+    it.term = term;
+    it.rhs0 = rhs0;
+    it.r = min(T.r, p.nrhs_v - rhs0);
     it.off_nb = T.off_nb;
-    it.off_nq = T.off_nq;
+    it.off_nq = T.off_nq - p.fbase;
     it.nb_t = T.nb;
     it.nq_t = T.nq;
     it.w = T.w;
@@ -419,7 +462,7 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ite
   }
   if (threadIdx.x < p.D) {
     const int i = threadIdx.x;
-    const int l = p.terms[p.items[item_idx].term].l[i];
+    const int l = p.terms[term].l[i];
     const int k = i * p.Lp1 + l;
     it.nb[i] = p.nb_of_l[k];
     it.nq[i] = p.nq_of_l[k];
@@ -429,11 +472,11 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ite
   if (threadIdx.x == 0) {  // insertion sort of the modes by (nq-nb)/(nb*nq), ties by index
     for (int i = 0; i < p.D; ++i) {
       int j = i;
-      const double key = (double)(it.nq[i] - it.nb[i]) / ((double)it.nb[i] * it.nq[i]);
+      const int ni = it.nq[i] - it.nb[i], di = it.nb[i] * it.nq[i];
       while (j > 0) {
         const int o = it.ord[j - 1];
-        const double ko = (double)(it.nq[o] - it.nb[o]) / ((double)it.nb[o] * it.nq[o]);
-        if (ko <= key) break;
+        // key(o) <= key(i)  <=>  (nq_o-nb_o) nb_i nq_i <= (nq_i-nb_i) nb_o nq_o  (integers)
+        if ((it.nq[o] - it.nb[o]) * di <= ni * (it.nb[o] * it.nq[o])) break;
         it.ord[j] = o;
         --j;
       }
@@ -461,11 +504,16 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ite
 
   if (p.type == 0) {
     // CASE 0: y = V.x
-    for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
-      const int q = e % nqt;
-      x[e] = (p.V ? __ldg(p.V + oq + q) : 0.0) * x[e];
+    if (p.nb0 == 1) {
+      for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
+        const int q = e % nqt;
+        x[e] = (p.V ? __ldg(p.V + oq + q) : 0.0) * x[e];
+      }
+      y = x;
+    } else {  // channel coupling: into the other transform buffer
+      y = (x == X) ? T : X;
+      for (int e = threadIdx.x; e < NQR; e += blockDim.x) y[e] = p.V ? vmat_apply(p, x, e, nqt, oq, it.rhs0) : 0.0;
     }
-    y = x;
     __syncthreads();
   } else if (p.type == 1) {
     // CASE 1: y = V.x + sum F2_ij d_i d_j x + sum F1_i d_i x
@@ -473,7 +521,7 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ite
     double* C = buf + 3 * NQR;
     for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
       const int q = e % nqt;
-      Y[e] = p.V ? __ldg(p.V + oq + q) * x[e] : 0.0;
+      Y[e] = !p.V ? 0.0 : (p.nb0 == 1 ? __ldg(p.V + oq + q) * x[e] : vmat_apply(p, x, e, nqt, oq, it.rhs0));
     }
     __syncthreads();
     for (int i = 0; i < D; ++i)
@@ -578,7 +626,7 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ite
   store_contrib(p, it, yb);
 }
 
-__global__ void __launch_bounds__(256, 2) hpsi_batched_kernel(KParams p) {
+__global__ void __launch_bounds__(EVR_CTA_THREADS, EVR_CTAS_PER_SM) hpsi_batched_kernel(KParams p) {
   extern __shared__ double smem[];
   __shared__ ItemShared it;
   __shared__ int next;
@@ -588,23 +636,39 @@ __global__ void __launch_bounds__(256, 2) hpsi_batched_kernel(KParams p) {
     int idx = next;
     __syncthreads();
     if (idx >= p.n_items) break;
-    run_item(p, it, smem, idx);
+    const Item itm = p.items[idx];
+    run_item(p, it, smem, itm.term, itm.rhs0);
   }
 }
 
-__global__ void __launch_bounds__(256, 2) hpsi_plain_kernel(KParams p) {
+// Items of several contexts in one launch: each item names its context,
+// whose parameter block is copied to shared memory before the item runs.
+// With a counter the CTAs pull items until the list is empty; without one
+// (the per-term path) CTA b runs item item_base + b.
+__global__ void __launch_bounds__(EVR_CTA_THREADS, EVR_CTAS_PER_SM) hpsi_multi_kernel(const KParams* __restrict__ ps,
+                                                              const MItem* __restrict__ items, int n_items,
+                                                              int item_base, unsigned int* counter) {
   extern __shared__ double smem[];
   __shared__ ItemShared it;
-  run_item(p, it, smem, p.item_base + blockIdx.x);
+  __shared__ KParams sp;
+  __shared__ int next;
+  for (int round = 0;; ++round) {
+    if (threadIdx.x == 0) next = counter ? (int)atomicAdd(counter, 1u) : (round == 0 ? item_base + (int)blockIdx.x : n_items);
+    __syncthreads();
+    const int idx = next;
+    __syncthreads();
+    if (idx >= n_items) break;
+    const MItem m = items[idx];
+    {
+      const int* src = (const int*)(ps + m.ctx);
+      int* dst = (int*)&sp;
+      for (int w = threadIdx.x; w < (int)(sizeof(KParams) / sizeof(int)); w += blockDim.x) dst[w] = src[w];
+    }
+    __syncthreads();
+    run_item(sp, it, smem, m.term, m.rhs0);
+  }
 }
 
-// hpsi(n, v) = (sum_t contrib(k_t(n), v) - E0 psi(n, v)) / Esc, the sum over
-// the terms holding packed function n (inv_ptr/inv_idx is the inverse of
-// tab_iB_OF_SRep_TO_iB, in Smolyak-term order).  One warp per packed
-// function: lane l adds entries l, l+32, ... in order with Neumaier
-// compensation, then a fixed shuffle tree combines the lanes with TwoSum.
-// The schedule is fixed, so the result is deterministic, and the compensated
-// sums keep it independent of the sign pattern of the Smolyak weights.
 __device__ __forceinline__ void neumaier_add(double& s, double& c, double x) {
   const double t = s + x;
   c += (fabs(s) >= fabs(x)) ? ((s - t) + x) : ((x - t) + s);
@@ -612,80 +676,57 @@ __device__ __forceinline__ void neumaier_add(double& s, double& c, double x) {
 }
 
 __device__ __forceinline__ void out_value(double* hpsi, const double* psi, long long n, int v, int cshift,
-                                          long long ldpsi, long long ldh, double sum, double E0, double Esc) {
-  const long long oh = (long long)(v >> cshift) * ldh + (n << cshift) + (v & cshift);
+                                          long long ldpsi, long long ldh, double sum, double E0, double Esc,
+                                          int nb0, long long Nfun) {
+  const int col = v >> cshift;
+  const int j = col / nb0, a = col - j * nb0;
+  const long long in = ((long long)a * Nfun + n) << cshift | (v & cshift);
+  const long long oh = (long long)j * ldh + in;
   if (E0 == 0.0 && Esc == 1.0) {
     hpsi[oh] = sum;
   } else {
-    const long long op = (long long)(v >> cshift) * ldpsi + (n << cshift) + (v & cshift);
-    hpsi[oh] = (sum - E0 * psi[op]) / Esc;
+    hpsi[oh] = (sum - E0 * psi[(long long)j * ldpsi + in]) / Esc;
   }
 }
 
-// Packed functions with short contribution lists (<= EVR_LONG_LIST, nearly
-// all of them) get one thread per (function, right-hand side) that adds its
-// list sequentially in term order; the few held by many terms (the ground
-// state is in every term) get one warp each, lanes taking entries l, l+32, ...
-// and a fixed shuffle tree joining the lanes with TwoSum.
-#define EVR_LONG_LIST 128
-__global__ void __launch_bounds__(256) hpsi_reduce_kernel(
-    const double* __restrict__ contrib, const long long* __restrict__ inv_ptr,
-    const long long* __restrict__ inv_idx, const int* __restrict__ long_n, int n_long,
-    const int* __restrict__ short_n, long long n_short, int nrhs_v, int cshift, const double* psi,
-    long long ldpsi, double* hpsi, long long ldh, double E0, double Esc) {
-  constexpr int RV = 8;
-  const int lane = threadIdx.x & 31;
-  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-  const long long short_warps = (n_short * nrhs_v + 31) / 32;
-  for (long long w = warp; w < n_long + short_warps; w += nwarps) {
-    if (w < n_long) {
-      const long long n = long_n[w];
-      const long long q0 = inv_ptr[n], q1 = inv_ptr[n + 1];
-      for (int v0 = 0; v0 < nrhs_v; v0 += RV) {
-        const int nv = min(RV, nrhs_v - v0);
-        double s[RV], c[RV];
-#pragma unroll
-        for (int u = 0; u < RV; ++u) s[u] = c[u] = 0.0;
-        for (long long q = q0 + lane; q < q1; q += 32) {
-          const double* cp = contrib + inv_idx[q] * nrhs_v + v0;
-#pragma unroll
-          for (int u = 0; u < RV; ++u)
-            if (u < nv) neumaier_add(s[u], c[u], cp[u]);
-        }
-#pragma unroll
-        for (int off = 16; off >= 1; off >>= 1) {
-#pragma unroll
-          for (int u = 0; u < RV; ++u) {
-            if (u >= nv) continue;
-            const double so = __shfl_down_sync(0xffffffffu, s[u], off);
-            const double co = __shfl_down_sync(0xffffffffu, c[u], off);
-            const double t = s[u] + so;  // TwoSum(s, so)
-            const double bp = t - s[u];
-            const double err = (s[u] - (t - bp)) + (so - bp);
-            s[u] = t;
-            c[u] += co + err;
-          }
-        }
-        double mine = 0.0;
-#pragma unroll
-        for (int u = 0; u < RV; ++u) {
-          if (u >= nv) continue;
-          const double tot = __shfl_sync(0xffffffffu, s[u] + c[u], 0);
-          if (lane == u) mine = tot;
-        }
-        if (lane < nv) out_value(hpsi, psi, n, v0 + lane, cshift, ldpsi, ldh, mine, E0, Esc);
-      }
-    } else {
-      const long long pidx = (w - n_long) * 32 + lane;
-      if (pidx < n_short * nrhs_v) {
-        const long long n = short_n[pidx / nrhs_v];
-        const int v = (int)(pidx % nrhs_v);
-        double s = 0.0, c = 0.0;
-        for (long long q = inv_ptr[n]; q < inv_ptr[n + 1]; ++q) neumaier_add(s, c, contrib[inv_idx[q] * nrhs_v + v]);
-        out_value(hpsi, psi, n, v, cshift, ldpsi, ldh, s + c, E0, Esc);
-      }
-    }
+// hpsi(n, v) = (sum_t contrib(k_t(n), v) - E0 psi(n, v)) / Esc, the sum over
+// the terms holding packed function n (inv_ptr/inv_idx is the inverse of
+// tab_iB_OF_SRep_TO_iB, in Smolyak-term order), in two phases so no thread
+// runs a long serial chain (the ground state is held by every term).  Each
+// packed function's list is cut into at most EVR_RED_CHUNKS chunks of at
+// least 16 entries:
+//   phase 1: one thread per (chunk, right-hand side) adds its chunk in term
+//            order with Neumaier compensation -> (s, c) partials;
+//   phase 2: one thread per (function, right-hand side) joins its chunk
+//            partials in order with TwoSum and writes (sum - E0 psi)/Esc.
+// The chunking is fixed at set-up, so results are deterministic, and the
+// compensated sums keep them independent of the sign pattern of the Smolyak
+// weights.
+#define EVR_RED_CHUNKS 32
+__global__ void __launch_bounds__(256) hpsi_reduce_chunks_kernel(
+    const double* __restrict__ contrib, const long long* __restrict__ chunk_q, long long n_chunks,
+    const long long* __restrict__ inv_idx, int nrhs_v, double2* __restrict__ part) {
+  const long long total = n_chunks * nrhs_v;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long ch = t / nrhs_v;
+    const int v = (int)(t - ch * nrhs_v);
+    double s = 0.0, c = 0.0;
+    for (long long q = chunk_q[ch]; q < chunk_q[ch + 1]; ++q) neumaier_add(s, c, contrib[inv_idx[q] * nrhs_v + v]);
+    part[t] = make_double2(s, c);
+  }
+}
+
+__global__ void __launch_bounds__(256) hpsi_reduce_join_kernel(
+    const double2* __restrict__ part, const long long* __restrict__ fun_chunk, long long N, int nrhs_v, int cshift,
+    const double* psi, long long ldpsi, double* hpsi, long long ldh, double E0, double Esc, int nb0) {
+  const long long total = N * nrhs_v;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long n = t / nrhs_v;
+    const int v = (int)(t - n * nrhs_v);
+    out_value(hpsi, psi, n, v, cshift, ldpsi, ldh, join_chunks(part, fun_chunk[n], fun_chunk[n + 1], nrhs_v, v), E0,
+              Esc, nb0, N);
   }
 }
 
@@ -702,11 +743,17 @@ __device__ void point_coords(const int* nq_of_l, const double* xcat, const int* 
   }
 }
 
+// V polynomial terms as up to EVR_VFAC (mode << 8 | exponent) factors in
+// ascending mode order (-1 ends a term): the same products, in the same
+// order, as the dense exponent table, without its D loop per term.
+#define EVR_VFAC 8
+
+// Fields of the grid points [gp0, gp1) (whole terms), written from index 0.
 __global__ void fields_kernel(const TermInfo* terms, long long nb_SG, const long long* pt_term_start,
                               const int* nq_of_l, const double* xcat, const int* x_off, int D, int Lp1,
-                              int V_nterms, const double* V_coef, const int* V_expo, double* V,
-                              const double* G0, const double* G1, double* G, long long sum_nq) {
-  for (long long gp = blockIdx.x * (long long)blockDim.x + threadIdx.x; gp < sum_nq;
+                              int V_nterms, const double* V_coef, const int* V_fac, double* V,
+                              const double* G0, const double* G1, double* G, long long gp0, long long gp1) {
+  for (long long gp = gp0 + blockIdx.x * (long long)blockDim.x + threadIdx.x; gp < gp1;
        gp += (long long)gridDim.x * blockDim.x) {
     // binary search of the term owning global point gp
     long long lo = 0, hi = nb_SG - 1;
@@ -722,13 +769,15 @@ __global__ void fields_kernel(const TermInfo* terms, long long nb_SG, const long
       double v = 0.0;
       for (int t = 0; t < V_nterms; ++t) {
         double m = V_coef[t];
-        for (int i = 0; i < D; ++i) {
-          int e = V_expo[t * D + i];
-          for (int k = 0; k < e; ++k) m *= Q[i];
+        for (int f = 0; f < EVR_VFAC; ++f) {
+          const int code = V_fac[t * EVR_VFAC + f];
+          if (code < 0) break;
+          const double x = Q[code >> 8];
+          for (int k = 0; k < (code & 255); ++k) m *= x;
         }
         v += m;
       }
-      V[gp] = v;
+      V[gp - gp0] = v;
     }
     if (G) {
       const long long nqt = T.nq;
@@ -738,7 +787,7 @@ __global__ void fields_kernel(const TermInfo* terms, long long nb_SG, const long
           if (G1)
             for (int k = 0; k < D; ++k) g = fma(G1[((long long)i * D + j) * D + k], Q[k], g);
           // GGiq(iq, j, i) of the term
-          G[T.off_nq * D * D + nqt * ((long long)D * i + j) + q] = g;
+          G[(T.off_nq - gp0) * D * D + nqt * ((long long)D * i + j) + q] = g;
         }
     }
   }
@@ -762,7 +811,9 @@ using namespace evr;
 // ----------------------------------------------------------------- context
 struct evr_sg4_ctx {
   int D = 0, L = 0, LB = 0;
-  long long N = 0, nb_SG = 0;
+  long long N = 0, nb_SG = 0;   // N: packed basis functions per channel
+  int nb0 = 1;                  // channels (electronic states)
+  long long nvec = 0;           // length of a vector: nb0 * N
   DescSizes z;
   int device = 0, num_sms = 0;
   std::vector<int> nb_of_l, nq_of_l, mat_off, x_off;
@@ -777,23 +828,27 @@ struct evr_sg4_ctx {
   int* d_x_off = nullptr;
   TermInfo* d_terms = nullptr;
   Item* d_items = nullptr;
+  MItem* d_plain_items = nullptr;    // term-ordered (context 0) items for the per-term path
+  KParams* d_params = nullptr;       // parameter block of the per-term path
   size_t items_cap = 0;
-  int items_nrhs = -1;           // items built for this virtual nrhs
+  int items_nrhs = -1;               // items built for this virtual nrhs
   int n_items = 0;
   std::vector<int> term_item_start;  // plain path
   unsigned int* d_counter = nullptr;
   long long* d_inv_ptr = nullptr;    // [N+1] packed function -> contributions
   long long* d_inv_idx = nullptr;    // [count(map>0)] global DP indices, term order
-  int* d_long_n = nullptr;           // packed functions with > EVR_LONG_LIST contributions
-  int* d_short_n = nullptr;          // the others
-  int n_long = 0;
-  long long n_short = 0;
-  double* d_contrib = nullptr;       // [nrhs_v][sum_nb]
+  long long* d_chunk_q = nullptr;    // [n_chunks+1] list positions where chunks start
+  long long* d_fun_chunk = nullptr;  // [N+1] first chunk of every packed function
+  long long n_chunks = 0;
+  double* d_part = nullptr;          // [n_chunks][nrhs_v] chunk partials (s, c)
+  size_t part_cap = 0;
+  double* d_contrib = nullptr;       // [sum_nb][nrhs_v]
   size_t contrib_cap = 0;
   double* d_scratch = nullptr;
   long long scratch_per_cta = 0;
   int grid = 0;
   int smem_doubles = 0;
+  int rmax = 32;                     // most right-hand sides per work item (evr_sg4_tune)
   // operator
   bool have_op = false;
   int type = -1;
@@ -806,6 +861,18 @@ struct evr_sg4_ctx {
   double* d_F1 = nullptr;
   double F2[EVR_MAXD * EVR_MAXD] = {0};
   double F1[EVR_MAXD] = {0};
+  // streamed operator fields: analytic V / G kept as coefficients and
+  // evaluated per slice of Smolyak terms just before the slice's items run
+  long long field_budget = 0;         // bytes; 0: fields stay resident
+  bool streamed = false;
+  int V_nterms = 0;
+  double* d_Vcoef = nullptr;
+  int* d_Vfac = nullptr;
+  double* d_G0 = nullptr;
+  double* d_G1 = nullptr;
+  long long* d_pt_start = nullptr;    // [nb_SG] first grid point of every term
+  std::vector<long long> slice_term;  // [nslices+1] term ranges
+  std::vector<int> slice_item;        // [nslices+1] ranges of the sorted work list
   // host-pointer path buffers
   double* d_io = nullptr;
   size_t io_cap = 0;
@@ -818,10 +885,11 @@ static int nbuf_for(int type, int D) {
 
 static void free_ctx(evr_sg4_ctx* c) {
   void* ptrs[] = {c->d_map, c->d_mats, c->d_mat_off, c->d_nb_of_l, c->d_nq_of_l, c->d_x, c->d_x_off,
-                  c->d_terms, c->d_items, c->d_counter, c->d_inv_ptr, c->d_inv_idx, c->d_contrib,
-                  c->d_long_n, c->d_short_n,
+                  c->d_terms, c->d_items, c->d_plain_items, c->d_params, c->d_counter, c->d_inv_ptr,
+                  c->d_inv_idx, c->d_contrib, c->d_chunk_q, c->d_fun_chunk, c->d_part,
                   c->d_scratch, c->d_V, c->d_G, c->d_Jac, c->d_cfac,
-                  c->d_sqRho, c->d_F2, c->d_F1, c->d_io};
+                  c->d_sqRho, c->d_F2, c->d_F1, c->d_io, c->d_Vcoef, c->d_Vfac, c->d_G0, c->d_G1,
+                  c->d_pt_start};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete c;
@@ -854,6 +922,8 @@ extern "C" int evr_sg4_create(const evr_sg4_desc* d, evr_sg4_ctx** out) {
   c->L = d->L;
   c->LB = d->LB;
   c->N = d->N;
+  c->nb0 = d->nb0;
+  c->nvec = (long long)d->nb0 * d->N;
   c->nb_SG = d->nb_SG;
   c->z = z;
   const int D = d->D, Lp1 = d->L + 1;
@@ -935,14 +1005,20 @@ extern "C" int evr_sg4_create(const evr_sg4_desc* d, evr_sg4_ctx** out) {
     for (long long k = 0; k < z.sum_nb; ++k)
       if (d->map[k] > 0) inv_idx[fill[d->map[k] - 1]++] = k;
   }
-  std::vector<int> long_n, short_n;
-  for (long long n = 0; n < d->N; ++n)
-    (inv_ptr[n + 1] - inv_ptr[n] > EVR_LONG_LIST ? long_n : short_n).push_back((int)n);
-  c->n_long = (int)long_n.size();
-  c->n_short = (long long)short_n.size();
-  // launch geometry: two 256-thread CTAs per SM, ~110 KB of shared memory each
-  c->smem_doubles = 110 * 1024 / 8;
-  c->grid = 2 * c->num_sms;
+  // chunks of each function's contribution list: at most EVR_RED_CHUNKS per function
+  std::vector<long long> chunk_q, fun_chunk(d->N + 1, 0);
+  for (long long n = 0; n < d->N; ++n) {
+    fun_chunk[n] = (long long)chunk_q.size();
+    const long long len = inv_ptr[n + 1] - inv_ptr[n];
+    const long long csz = std::max<long long>(16, (len + EVR_RED_CHUNKS - 1) / EVR_RED_CHUNKS);
+    for (long long q = inv_ptr[n]; q < inv_ptr[n + 1]; q += csz) chunk_q.push_back(q);
+  }
+  fun_chunk[d->N] = (long long)chunk_q.size();
+  c->n_chunks = (long long)chunk_q.size();
+  chunk_q.push_back(inv_ptr[d->N]);
+  // launch geometry: EVR_CTAS_PER_SM persistent CTAs per SM sharing ~220 KB of shared memory
+  c->smem_doubles = 220 * 1024 / EVR_CTAS_PER_SM / 8;
+  c->grid = EVR_CTAS_PER_SM * c->num_sms;
   if ((rc = upload(&c->d_map, d->map, (size_t)z.sum_nb)) ||
       (rc = upload(&c->d_mats, mats.data(), mats.size())) ||
       (rc = upload(&c->d_mat_off, c->mat_off.data(), c->mat_off.size())) ||
@@ -954,14 +1030,14 @@ extern "C" int evr_sg4_create(const evr_sg4_desc* d, evr_sg4_ctx** out) {
       (rc = upload<unsigned int>(&c->d_counter, nullptr, 1)) ||
       (rc = upload(&c->d_inv_ptr, inv_ptr.data(), inv_ptr.size())) ||
       (rc = upload(&c->d_inv_idx, inv_idx.data(), inv_idx.size())) ||
-      (rc = upload(&c->d_long_n, long_n.data(), long_n.size())) ||
-      (rc = upload(&c->d_short_n, short_n.data(), short_n.size()))) {
+      (rc = upload(&c->d_chunk_q, chunk_q.data(), chunk_q.size())) ||
+      (rc = upload(&c->d_fun_chunk, fun_chunk.data(), fun_chunk.size()))) {
     free_ctx(c);
     return rc;
   }
   e = cudaFuncSetAttribute(hpsi_batched_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, c->smem_doubles * 8);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(hpsi_plain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, c->smem_doubles * 8);
+    e = cudaFuncSetAttribute(hpsi_multi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, c->smem_doubles * 8);
   if (e != cudaSuccess) {
     free_ctx(c);
     return set_error(EVR_ERR_CUDA, "evr_sg4_create: shared-memory attribute: %s", cudaGetErrorString(e));
@@ -977,39 +1053,113 @@ extern "C" int evr_sg4_destroy(evr_sg4_ctx* c) {
   return EVR_OK;
 }
 
+// V (polynomial) and/or G (affine) on the grid points [g0, g1) (whole terms) into
+// the context's field arrays, from index 0.
+static int eval_fields(evr_sg4_ctx* c, long long g0, long long g1, bool V, bool G, cudaStream_t s) {
+  if (g1 <= g0) return EVR_OK;
+  const long long blocks = std::max<long long>(1, std::min<long long>((g1 - g0 + 255) / 256, 8LL * c->num_sms));
+  fields_kernel<<<(unsigned)blocks, 256, 0, s>>>(c->d_terms, c->nb_SG, c->d_pt_start, c->d_nq_of_l, c->d_x,
+                                                 c->d_x_off, c->D, c->L + 1, V ? c->V_nterms : 0, c->d_Vcoef,
+                                                 c->d_Vfac, V ? c->d_V : nullptr, c->d_G0, c->d_G1,
+                                                 G ? c->d_G : nullptr, g0, g1);
+  CUDA_TRY(cudaGetLastError());
+  return EVR_OK;
+}
+
+extern "C" int evr_sg4_set_field_budget(evr_sg4_ctx* c, long long bytes) {
+  if (!c) return set_error(EVR_ERR_ARG, "set_field_budget: NULL context");
+  if (bytes < 0) return set_error(EVR_ERR_ARG, "set_field_budget: negative budget");
+  c->field_budget = bytes;
+  return EVR_OK;
+}
+
+extern "C" int evr_sg4_field_slices(const evr_sg4_ctx* c, long long* nslices) {
+  if (!c || !nslices) return set_error(EVR_ERR_ARG, "field_slices: NULL argument");
+  *nslices = c->streamed ? (long long)c->slice_term.size() - 1 : 0;
+  return EVR_OK;
+}
+
 extern "C" int evr_sg4_set_operator(evr_sg4_ctx* c, const evr_sg4_op_desc* op) {
   if (!c || !op) return set_error(EVR_ERR_ARG, "evr_sg4_set_operator: NULL argument");
   if (op->type != 0 && op->type != 1 && op->type != 10)
     return set_error(EVR_ERR_ARG, "evr_sg4_set_operator: type_Op=%d not in {0,1,10}", op->type);
   const int D = c->D;
   const long long snq = c->z.sum_nq;
-  for (double** p : {&c->d_V, &c->d_G, &c->d_Jac, &c->d_sqRho, &c->d_cfac, &c->d_F2, &c->d_F1})
+  for (double** p : {&c->d_V, &c->d_G, &c->d_Jac, &c->d_sqRho, &c->d_cfac, &c->d_F2, &c->d_F1, &c->d_Vcoef, &c->d_G0,
+                     &c->d_G1})
     if (*p) {
       cudaFree(*p);
       *p = nullptr;
     }
+  if (c->d_Vfac) cudaFree(c->d_Vfac);
+  if (c->d_pt_start) cudaFree(c->d_pt_start);
+  c->d_Vfac = nullptr;
+  c->d_pt_start = nullptr;
+  c->streamed = false;
+  c->slice_term.clear();
+  c->V_nterms = 0;
   c->have_op = false;
   c->type = op->type;
+  c->items_nrhs = -1;  // work split depends on the operator's buffer count and the slices
   int rc;
-  if (op->V_grid) {
-    for (long long k = 0; k < snq; ++k)
-      if (!std::isfinite(op->V_grid[k])) return set_error(EVR_ERR_NUMERIC, "V_grid[%lld] is not finite", k);
-    if ((rc = upload(&c->d_V, op->V_grid, (size_t)snq))) return rc;
+  if (c->nb0 > 1) {  // electronic matrices: V(:, a, b) given on the grid, operators 0 and 1
+    if (op->type == 10) return set_error(EVR_ERR_ARG, "nb0=%d: type_Op 10 needs nb0 = 1", c->nb0);
+    if (op->V_nterms > 0 && !op->V_grid)
+      return set_error(EVR_ERR_ARG, "nb0=%d: pass V as V_grid[nb0*nb0*sum_nq]", c->nb0);
   }
-  bool need_fields_kernel = false;
-  if (!op->V_grid && op->V_nterms > 0) {
+  const long long nvg = snq * c->nb0 * c->nb0;  // V_grid entries
+  const bool polyV = !op->V_grid && op->V_nterms > 0;
+  const bool affG = op->type == 10 && !op->G_grid && (op->G0 || op->G1);
+  std::vector<int> vfac;
+  if (polyV) {
     if (!op->V_coef || !op->V_expo) return set_error(EVR_ERR_ARG, "V polynomial without coef/expo");
-    for (int t = 0; t < op->V_nterms * D; ++t)
-      if (op->V_expo[t] < 0 || op->V_expo[t] > 16) return set_error(EVR_ERR_ARG, "V exponent outside [0,16]");
-    CUDA_TRY(cudaMalloc(&c->d_V, (size_t)snq * 8));
-    need_fields_kernel = true;
+    vfac.assign((size_t)op->V_nterms * EVR_VFAC, -1);
+    for (int t = 0; t < op->V_nterms; ++t) {
+      int f = 0;
+      for (int i = 0; i < D; ++i) {
+        const int ex = op->V_expo[t * D + i];
+        if (ex < 0 || ex > 16) return set_error(EVR_ERR_ARG, "V exponent outside [0,16]");
+        if (ex == 0) continue;
+        if (f == EVR_VFAC) return set_error(EVR_ERR_ARG, "V term %d depends on more than %d modes", t, EVR_VFAC);
+        vfac[(size_t)t * EVR_VFAC + f++] = (i << 8) | ex;
+      }
+    }
   }
+  // fields given in analytic form are streamed per term slice when they exceed the budget
+  const bool grids = op->V_grid || (op->type == 10 && (op->G_grid || op->Jac_grid || op->sqRho_grid));
+  const double bpp = 8.0 * (polyV ? 1 : 0) + 8.0 * D * D * (affG ? 1 : 0);  // bytes per grid point
+  const bool stream = c->field_budget > 0 && !grids && (polyV || affG) && bpp * (double)snq > (double)c->field_budget;
+  long long slice_pts = snq;
+  if (stream) {
+    const long long cap = (long long)((double)c->field_budget / bpp);
+    c->slice_term.push_back(0);
+    long long pts = 0;
+    slice_pts = 0;
+    for (long long t = 0; t < c->nb_SG; ++t) {
+      const long long q = c->terms[t].nq;
+      if (q > cap)
+        return set_error(EVR_ERR_ARG, "field budget %lld B is below the fields of term %lld (%lld points)",
+                         c->field_budget, t, q);
+      if (pts + q > cap) {
+        c->slice_term.push_back(t);
+        pts = 0;
+      }
+      pts += q;
+      slice_pts = std::max(slice_pts, pts);
+    }
+    c->slice_term.push_back(c->nb_SG);
+  }
+  if (op->V_grid) {
+    for (long long k = 0; k < nvg; ++k)
+      if (!std::isfinite(op->V_grid[k])) return set_error(EVR_ERR_NUMERIC, "V_grid[%lld] is not finite", k);
+    if ((rc = upload(&c->d_V, op->V_grid, (size_t)nvg))) return rc;
+  }
+  if (polyV) CUDA_TRY(cudaMalloc(&c->d_V, (size_t)slice_pts * 8));
   if (op->type == 10) {
     if (op->G_grid) {
       if ((rc = upload(&c->d_G, op->G_grid, (size_t)snq * D * D))) return rc;
-    } else if (op->G0 || op->G1) {
-      CUDA_TRY(cudaMalloc(&c->d_G, (size_t)snq * D * D * 8));
-      need_fields_kernel = true;
+    } else if (affG) {
+      CUDA_TRY(cudaMalloc(&c->d_G, (size_t)slice_pts * D * D * 8));
     }
     if (op->Jac_grid) {
       for (long long k = 0; k < snq; ++k)
@@ -1040,54 +1190,47 @@ extern "C" int evr_sg4_set_operator(evr_sg4_ctx* c, const evr_sg4_op_desc* op) {
       for (int i = 0; i < D; ++i) c->F1[i] = op->F1[i];
   }
   if ((rc = upload(&c->d_F2, c->F2, (size_t)D * D)) || (rc = upload(&c->d_F1, c->F1, (size_t)D))) return rc;
-  if (need_fields_kernel) {
+  if (polyV || affG) {  // the analytic forms stay on the device (evaluated again per slice when streamed)
     std::vector<long long> start(c->nb_SG);
     for (long long t = 0; t < c->nb_SG; ++t) start[t] = c->terms[t].off_nq;
-    long long* d_start = nullptr;
-    double *d_coef = nullptr, *d_G0 = nullptr, *d_G1 = nullptr;
-    int* d_expo = nullptr;
-    TermInfo* d_terms = c->d_terms;
-    CUDA_TRY(cudaMemcpy(d_terms, c->terms.data(), c->terms.size() * sizeof(TermInfo), cudaMemcpyHostToDevice));
-    if ((rc = upload(&d_start, start.data(), start.size()))) return rc;
-    bool polyV = !op->V_grid && op->V_nterms > 0;
-    if (polyV && ((rc = upload(&d_coef, op->V_coef, (size_t)op->V_nterms)) ||
-                  (rc = upload(&d_expo, op->V_expo, (size_t)op->V_nterms * D))))
+    CUDA_TRY(cudaMemcpy(c->d_terms, c->terms.data(), c->terms.size() * sizeof(TermInfo), cudaMemcpyHostToDevice));
+    if ((rc = upload(&c->d_pt_start, start.data(), start.size()))) return rc;
+    if (polyV && ((rc = upload(&c->d_Vcoef, op->V_coef, (size_t)op->V_nterms)) ||
+                  (rc = upload(&c->d_Vfac, vfac.data(), vfac.size()))))
       return rc;
-    bool affG = op->type == 10 && !op->G_grid && (op->G0 || op->G1);
-    if (affG && op->G0 && (rc = upload(&d_G0, op->G0, (size_t)D * D))) return rc;
-    if (affG && op->G1 && (rc = upload(&d_G1, op->G1, (size_t)D * D * D))) return rc;
-    fields_kernel<<<4 * c->num_sms, 256>>>(c->d_terms, c->nb_SG, d_start, c->d_nq_of_l, c->d_x, c->d_x_off, D,
-                                           c->L + 1, polyV ? op->V_nterms : 0, d_coef, d_expo,
-                                           polyV ? c->d_V : nullptr, d_G0, d_G1, affG ? c->d_G : nullptr, snq);
-    CUDA_TRY(cudaGetLastError());
-    CUDA_TRY(cudaDeviceSynchronize());
-    cudaFree(d_start);
-    if (d_coef) cudaFree(d_coef);
-    if (d_expo) cudaFree(d_expo);
-    if (d_G0) cudaFree(d_G0);
-    if (d_G1) cudaFree(d_G1);
+    c->V_nterms = polyV ? op->V_nterms : 0;
+    if (affG && op->G0 && (rc = upload(&c->d_G0, op->G0, (size_t)D * D))) return rc;
+    if (affG && op->G1 && (rc = upload(&c->d_G1, op->G1, (size_t)D * D * D))) return rc;
+    if (!stream) {
+      if ((rc = eval_fields(c, 0, snq, polyV, affG, 0))) return rc;
+      CUDA_TRY(cudaDeviceSynchronize());
+    }
   }
+  c->streamed = stream;
   c->have_op = true;
-  c->items_nrhs = -1;  // work split depends on the operator's buffer count
   return EVR_OK;
 }
 
-// Builds the (term, rhs block) work list for nrhs_v virtual right-hand sides,
-// sorted by decreasing cost so the persistent kernel balances well.
+
 // Work list of one H.psi over nrhs_v virtual right-hand sides: (term, rhs
-// block) items, term-ordered and cost-sorted (decreasing, so the persistent
-// kernel ends balanced), with each term's block size r written into c->terms.
-static void plan_items(evr_sg4_ctx* c, int nrhs_v, std::vector<Item>& items, std::vector<Item>& sorted,
-                       long long& max_need) {
+// block) items in term order with their costs, and the term table with each
+// term's block size r for this nrhs_v (the context itself is not modified).
+static void plan_work(const evr_sg4_ctx* c, int nrhs_v, std::vector<TermInfo>& terms, std::vector<Item>& items,
+                      std::vector<float>& cost, long long& max_need) {
   const int nbuf = nbuf_for(c->type, c->D);
-  const int Rmax = 32;
+  const int Rmax = c->rmax;
   max_need = 0;
   items.clear();
-  std::vector<float> cost;
+  cost.clear();
+  if (&terms != &c->terms) terms = c->terms;
   for (long long t = 0; t < c->nb_SG; ++t) {
-    TermInfo& T = c->terms[t];
+    TermInfo& T = terms[t];
     long long per = (long long)nbuf * T.nq;
     int r = (int)std::min<long long>(std::min(nrhs_v, Rmax), std::max<long long>(1, c->smem_doubles / per));
+    if (c->nb0 > 1) {  // whole channel groups (both halves of complex columns): 2 nb0 columns
+      const int g = 2 * c->nb0;
+      r = std::max(g, r / g * g);
+    }
     T.r = r;
     max_need = std::max(max_need, per * r);
     double fl = 0;  // cost ~ grid size times the 1-D lengths
@@ -1098,6 +1241,14 @@ static void plan_items(evr_sg4_ctx* c, int nrhs_v, std::vector<Item>& items, std
       cost.push_back(T.cost * std::min(r, nrhs_v - r0));
     }
   }
+}
+
+// The same list sorted by decreasing cost (the persistent kernel then ends
+// balanced), with each term's block size written into c->terms.
+static void plan_items(evr_sg4_ctx* c, int nrhs_v, std::vector<Item>& items, std::vector<Item>& sorted,
+                       long long& max_need) {
+  std::vector<float> cost;
+  plan_work(c, nrhs_v, c->terms, items, cost, max_need);
   std::vector<int> order(items.size());
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
@@ -1110,10 +1261,28 @@ static int build_items(evr_sg4_ctx* c, int nrhs_v) {
   std::vector<Item> items, sorted;
   long long max_need = 0;
   plan_items(c, nrhs_v, items, sorted, max_need);
+  // streamed fields: the list runs slice by slice (decreasing cost within a slice)
+  c->slice_item.assign(1, 0);
+  if (c->streamed) {
+    auto slice_of = [&](int term) {
+      return (int)(std::upper_bound(c->slice_term.begin(), c->slice_term.end(), (long long)term) -
+                   c->slice_term.begin()) - 1;
+    };
+    std::stable_sort(sorted.begin(), sorted.end(),
+                     [&](const Item& a, const Item& b) { return slice_of(a.term) < slice_of(b.term); });
+    const int ns = (int)c->slice_term.size() - 1;
+    size_t q = 0;
+    for (int k = 0; k < ns; ++k) {
+      while (q < sorted.size() && slice_of(sorted[q].term) == k) ++q;
+      c->slice_item.push_back((int)q);
+    }
+  } else {
+    c->slice_item.push_back((int)sorted.size());
+  }
   c->term_item_start.assign(c->nb_SG + 1, 0);
   for (size_t k = 0; k < items.size(); ++k) c->term_item_start[items[k].term + 1]++;
   for (long long t = 0; t < c->nb_SG; ++t) c->term_item_start[t + 1] += c->term_item_start[t];
-  size_t need = items.size() * 2;
+  size_t need = std::max<size_t>(1, items.size());
   if (need > c->items_cap) {
     if (c->d_items) cudaFree(c->d_items);
     c->d_items = nullptr;
@@ -1121,7 +1290,14 @@ static int build_items(evr_sg4_ctx* c, int nrhs_v) {
     c->items_cap = need;
   }
   CUDA_TRY(cudaMemcpy(c->d_items, sorted.data(), sorted.size() * sizeof(Item), cudaMemcpyHostToDevice));
-  CUDA_TRY(cudaMemcpy(c->d_items + items.size(), items.data(), items.size() * sizeof(Item), cudaMemcpyHostToDevice));
+  {
+    std::vector<MItem> pl(items.size());
+    for (size_t k = 0; k < items.size(); ++k) pl[k] = MItem{0, items[k].term, items[k].rhs0, 0};
+    if (c->d_plain_items) cudaFree(c->d_plain_items);
+    c->d_plain_items = nullptr;
+    CUDA_TRY(cudaMalloc(&c->d_plain_items, std::max<size_t>(1, pl.size()) * sizeof(MItem)));
+    CUDA_TRY(cudaMemcpy(c->d_plain_items, pl.data(), pl.size() * sizeof(MItem), cudaMemcpyHostToDevice));
+  }
   CUDA_TRY(cudaMemcpy(c->d_terms, c->terms.data(), c->terms.size() * sizeof(TermInfo), cudaMemcpyHostToDevice));
   c->n_items = (int)items.size();
   // global scratch for terms that do not fit in shared memory
@@ -1131,6 +1307,13 @@ static int build_items(evr_sg4_ctx* c, int nrhs_v) {
     c->d_scratch = nullptr;
     CUDA_TRY(cudaMalloc(&c->d_scratch, (size_t)per_cta * c->grid * 8));
     c->scratch_per_cta = per_cta;
+  }
+  size_t pneed = (size_t)c->n_chunks * nrhs_v * 2;
+  if (pneed > c->part_cap) {
+    if (c->d_part) cudaFree(c->d_part);
+    c->d_part = nullptr;
+    CUDA_TRY(cudaMalloc(&c->d_part, pneed * 8));
+    c->part_cap = pneed;
   }
   size_t cneed = (size_t)c->z.sum_nb * nrhs_v;
   if (cneed > c->contrib_cap) {
@@ -1143,13 +1326,16 @@ static int build_items(evr_sg4_ctx* c, int nrhs_v) {
   return EVR_OK;
 }
 
-static int launch_reduce(evr_sg4_ctx* c, const double* contrib, int nrhs_v, int cshift, const double* psi,
-                         long long ldpsi, double* hpsi, long long ldh, double E0, double Esc, cudaStream_t s) {
-  const long long warps = c->n_long + (c->n_short * nrhs_v + 31) / 32;
-  const long long blocks = std::max<long long>(1, std::min<long long>((warps + 7) / 8, 16LL * c->num_sms));
-  hpsi_reduce_kernel<<<(unsigned)blocks, 256, 0, s>>>(contrib, c->d_inv_ptr, c->d_inv_idx, c->d_long_n, c->n_long,
-                                                     c->d_short_n, c->n_short, nrhs_v, cshift, psi, ldpsi, hpsi,
-                                                     ldh, E0, Esc);
+static int launch_reduce(evr_sg4_ctx* c, const double* contrib, double2* part, int nrhs_v, int cshift,
+                         const double* psi, long long ldpsi, double* hpsi, long long ldh, double E0, double Esc,
+                         cudaStream_t s) {
+  const long long t1 = c->n_chunks * nrhs_v, t2 = c->N * nrhs_v;
+  const long long b1 = std::max<long long>(1, std::min<long long>((t1 + 255) / 256, 16LL * c->num_sms));
+  const long long b2 = std::max<long long>(1, std::min<long long>((t2 + 255) / 256, 16LL * c->num_sms));
+  hpsi_reduce_chunks_kernel<<<(unsigned)b1, 256, 0, s>>>(contrib, c->d_chunk_q, c->n_chunks, c->d_inv_idx, nrhs_v,
+                                                        part);
+  hpsi_reduce_join_kernel<<<(unsigned)b2, 256, 0, s>>>(part, c->d_fun_chunk, c->N, nrhs_v, cshift, psi, ldpsi, hpsi,
+                                                      ldh, E0, Esc, c->nb0);
   CUDA_TRY(cudaGetLastError());
   return EVR_OK;
 }
@@ -1189,6 +1375,9 @@ static KParams make_params(evr_sg4_ctx* c, int nrhs_v, int cshift, const double*
   p.contrib = c->d_contrib;
   p.cfac = c->d_cfac;
   p.sum_nb = c->z.sum_nb;
+  p.nb0 = c->nb0;
+  p.Nfun = c->N;
+  p.vstride = c->z.sum_nq;
   return p;
 }
 
@@ -1197,9 +1386,12 @@ static int hpsi_common(evr_sg4_ctx* c, int nrhs, int cshift, const double* psi, 
                        bool transpose = false) {
   if (!c) return set_error(EVR_ERR_ARG, "hpsi: NULL context");
   if (!c->have_op) return set_error(EVR_ERR_STATE, "hpsi: set_operator was not called");
+  if (plain && c->streamed)
+    return set_error(EVR_ERR_STATE, "hpsi: the per-term path needs resident operator fields (the budget streams them)");
   if (nrhs < 1) return set_error(EVR_ERR_ARG, "hpsi: nrhs=%d (size(Psi)=0 stops the reference)", nrhs);
   if (!psi || !hpsi) return set_error(EVR_ERR_ARG, "hpsi: NULL vector");
-  if (ldpsi < c->N || ldh < c->N) return set_error(EVR_ERR_ARG, "hpsi: leading dimension < N=%lld", c->N);
+  if (ldpsi < c->nvec || ldh < c->nvec)
+    return set_error(EVR_ERR_ARG, "hpsi: leading dimension < nb0*N=%lld", c->nvec);
   if (!(Esc != 0.0) || !std::isfinite(Esc) || !std::isfinite(E0))
     return set_error(EVR_ERR_ARG, "hpsi: Esc must be finite and non-zero");
   cudaPointerAttributes a1, a2;
@@ -1208,7 +1400,7 @@ static int hpsi_common(evr_sg4_ctx* c, int nrhs, int cshift, const double* psi, 
     cudaGetLastError();
     return set_error(EVR_ERR_ARG, "hpsi: psi and hpsi must be device pointers (use evr_sg4_hpsi_host)");
   }
-  const int nrhs_v = nrhs << cshift;
+  const int nrhs_v = (nrhs * c->nb0) << cshift;  // one virtual column per (rhs, channel, re/im)
   int rc = build_items(c, nrhs_v);
   if (rc) return rc;
   cudaStream_t s = (cudaStream_t)stream;
@@ -1217,25 +1409,42 @@ static int hpsi_common(evr_sg4_ctx* c, int nrhs, int cshift, const double* psi, 
   p.transpose = transpose ? 1 : 0;
   const size_t smem = (size_t)c->smem_doubles * 8;
   long long launches = 0;
-  if (!plain) {
+  if (!plain && c->streamed) {  // per slice: its fields, then its items
+    for (size_t k = 0; k + 1 < c->slice_term.size(); ++k) {
+      const long long t0 = c->slice_term[k], t1 = c->slice_term[k + 1];
+      const long long g0 = c->terms[t0].off_nq, g1 = t1 < c->nb_SG ? c->terms[t1].off_nq : c->z.sum_nq;
+      if ((rc = eval_fields(c, g0, g1, c->V_nterms > 0, c->d_G1 || c->d_G0, s))) return rc;
+      CUDA_TRY(cudaMemsetAsync(c->d_counter, 0, sizeof(unsigned int), s));
+      KParams q = p;
+      q.items = c->d_items + c->slice_item[k];
+      q.n_items = c->slice_item[k + 1] - c->slice_item[k];
+      q.fbase = g0;
+      hpsi_batched_kernel<<<c->grid, EVR_CTA_THREADS, smem, s>>>(q);
+      CUDA_TRY(cudaGetLastError());
+      launches += 2;
+    }
+  } else if (!plain) {
     CUDA_TRY(cudaMemsetAsync(c->d_counter, 0, sizeof(unsigned int), s));
     p.items = c->d_items;
-    hpsi_batched_kernel<<<c->grid, 256, smem, s>>>(p);
+    hpsi_batched_kernel<<<c->grid, EVR_CTA_THREADS, smem, s>>>(p);
     CUDA_TRY(cudaGetLastError());
     launches = 1;
   } else {
-    p.items = c->d_items + c->n_items;  // term-ordered list
-    for (long long t = 0; t < c->nb_SG; ++t) {
-      int n = c->term_item_start[t + 1] - c->term_item_start[t];
-      p.item_base = c->term_item_start[t];
-      hpsi_plain_kernel<<<n, 256, smem, s>>>(p);
+    if (!c->d_params) CUDA_TRY(cudaMalloc(&c->d_params, sizeof(KParams)));
+    CUDA_TRY(cudaMemcpyAsync(c->d_params, &p, sizeof(KParams), cudaMemcpyHostToDevice, s));
+    for (long long t = 0; t < c->nb_SG; ++t) {  // one launch per Smolyak term
+      const int b0 = c->term_item_start[t], b1 = c->term_item_start[t + 1];
+      hpsi_multi_kernel<<<b1 - b0, EVR_CTA_THREADS, smem, s>>>(c->d_params, c->d_plain_items, b1, b0, nullptr);
       ++launches;
     }
     CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaStreamSynchronize(s));  // the parameter block was copied from the stack
   }
-  if ((rc = launch_reduce(c, c->d_contrib, nrhs_v, cshift, psi, ldv_psi, hpsi, ldv_h, E0, Esc, s))) return rc;
+  if ((rc = launch_reduce(c, c->d_contrib, (double2*)c->d_part, nrhs_v, cshift, psi, ldv_psi, hpsi, ldv_h, E0, Esc,
+                          s)))
+    return rc;
   CUDA_TRY(cudaGetLastError());
-  c->last_launches = launches + 1;
+  c->last_launches = launches + 2;
   return EVR_OK;
 }
 
@@ -1268,9 +1477,9 @@ extern "C" int evr_sg4_apply(evr_sg4_ctx* c, int flags, int nrhs, const double* 
 extern "C" int evr_sg4_hpsi_host(evr_sg4_ctx* c, int nrhs, const double* psi, long long ldpsi, double* hpsi,
                                  long long ldh, double E0, double Esc) {
   if (!c) return set_error(EVR_ERR_ARG, "hpsi_host: NULL context");
-  if (nrhs < 1 || !psi || !hpsi || ldpsi < c->N || ldh < c->N)
+  if (nrhs < 1 || !psi || !hpsi || ldpsi < c->nvec || ldh < c->nvec)
     return set_error(EVR_ERR_ARG, "hpsi_host: bad sizes or NULL vectors");
-  size_t n = (size_t)c->N * nrhs;
+  size_t n = (size_t)c->nvec * nrhs;
   if (2 * n > c->io_cap) {
     if (c->d_io) cudaFree(c->d_io);
     c->d_io = nullptr;
@@ -1279,11 +1488,11 @@ extern "C" int evr_sg4_hpsi_host(evr_sg4_ctx* c, int nrhs, const double* psi, lo
   }
   double* dpsi = c->d_io;
   double* dh = c->d_io + n;
-  CUDA_TRY(cudaMemcpy2DAsync(dpsi, (size_t)c->N * 8, psi, (size_t)ldpsi * 8, (size_t)c->N * 8, nrhs,
+  CUDA_TRY(cudaMemcpy2DAsync(dpsi, (size_t)c->nvec * 8, psi, (size_t)ldpsi * 8, (size_t)c->nvec * 8, nrhs,
                              cudaMemcpyHostToDevice, 0));
-  int rc = evr_sg4_hpsi(c, nrhs, dpsi, c->N, dh, c->N, E0, Esc, nullptr);
+  int rc = evr_sg4_hpsi(c, nrhs, dpsi, c->nvec, dh, c->nvec, E0, Esc, nullptr);
   if (rc) return rc;
-  CUDA_TRY(cudaMemcpy2DAsync(hpsi, (size_t)ldh * 8, dh, (size_t)c->N * 8, (size_t)c->N * 8, nrhs,
+  CUDA_TRY(cudaMemcpy2DAsync(hpsi, (size_t)ldh * 8, dh, (size_t)c->nvec * 8, (size_t)c->nvec * 8, nrhs,
                              cudaMemcpyDeviceToHost, 0));
   CUDA_TRY(cudaStreamSynchronize(0));
   return EVR_OK;
@@ -1300,14 +1509,31 @@ extern "C" int evr_sg4_flops_per_rhs(const evr_sg4_ctx* c, double* flops) {
       nb[i] = c->nb_of_l[i * Lp1 + T.l[i]];
       nq[i] = c->nq_of_l[i * Lp1 + T.l[i]];
     }
-    double f = 0.0;
-    for (int i = 0; i < D; ++i) {  // B->G and G->B
-      double a = 1.0, b = 1.0;
-      for (int j = 0; j < D; ++j) {
-        if (j < i) { a *= nq[j]; b *= nb[j]; }
-        if (j > i) { a *= nb[j]; b *= nq[j]; }
+    // B->G and G->B in the mode order the kernel uses (ascending
+    // (nq-nb)/(nb*nq), ties by index; G->B reversed): 2 nin nout flops per fibre
+    int ord[EVR_MAXD];
+    for (int i = 0; i < D; ++i) {
+      int j = i;
+      while (j > 0) {
+        const int o = ord[j - 1];
+        if ((nq[o] - nb[o]) * (nb[i] * nq[i]) <= (nq[i] - nb[i]) * (nb[o] * nq[o])) break;
+        ord[j] = o;
+        --j;
       }
-      f += 2.0 * nq[i] * nb[i] * (a + b);
+      ord[j] = i;
+    }
+    double f = 0.0;
+    for (int dir = 0; dir < 2; ++dir) {
+      int cur[EVR_MAXD];
+      for (int i = 0; i < D; ++i) cur[i] = dir == 0 ? nb[i] : nq[i];
+      for (int k = 0; k < D; ++k) {
+        const int i = ord[dir == 0 ? k : D - 1 - k];
+        double rest = 1.0;
+        for (int j = 0; j < D; ++j)
+          if (j != i) rest *= cur[j];
+        f += 2.0 * nb[i] * nq[i] * rest;
+        cur[i] = dir == 0 ? nq[i] : nb[i];
+      }
     }
     double sum_nqi = 0;
     for (int i = 0; i < D; ++i) sum_nqi += nq[i];
@@ -1336,7 +1562,7 @@ extern "C" int evr_sg4_flops_per_rhs(const evr_sg4_ctx* c, double* flops) {
 
 extern "C" int evr_sg4_ctx_sizes(const evr_sg4_ctx* c, long long* out) {
   if (!c || !out) return set_error(EVR_ERR_ARG, "ctx_sizes: NULL argument");
-  out[0] = c->N;
+  out[0] = c->nvec;
   out[1] = c->nb_SG;
   out[2] = c->z.sum_nb;
   out[3] = c->z.sum_nq;
@@ -1415,9 +1641,11 @@ extern "C" int evr_sg4_hpsi_noalloc(evr_sg4_ctx* c, int nrhs, const double* psi,
                                     double* hpsi, long long ldh, double E0, double Esc, void* stream) {
   if (!c) return set_error(EVR_ERR_ARG, "hpsi_noalloc: NULL context");
   if (!c->have_op) return set_error(EVR_ERR_STATE, "hpsi_noalloc: set_operator was not called");
+  if (c->streamed) return set_error(EVR_ERR_STATE, "hpsi_noalloc: the operator fields are streamed (use evr_sg4_hpsi)");
   if (nrhs < 1) return set_error(EVR_ERR_ARG, "hpsi_noalloc: nrhs=%d", nrhs);
   if (!psi || !hpsi) return set_error(EVR_ERR_ARG, "hpsi_noalloc: NULL vector");
-  if (ldpsi < c->N || ldh < c->N) return set_error(EVR_ERR_ARG, "hpsi_noalloc: leading dimension < N=%lld", c->N);
+  if (ldpsi < c->nvec || ldh < c->nvec)
+    return set_error(EVR_ERR_ARG, "hpsi_noalloc: leading dimension < nb0*N=%lld", c->nvec);
   if (!(Esc != 0.0) || !std::isfinite(Esc) || !std::isfinite(E0))
     return set_error(EVR_ERR_ARG, "hpsi_noalloc: Esc must be finite and non-zero");
   int dev = 0;
@@ -1444,16 +1672,17 @@ extern "C" int evr_sg4_hpsi_noalloc(evr_sg4_ctx* c, int nrhs, const double* psi,
     cudaGetLastError();
     return set_error(EVR_ERR_ARG, "hpsi_noalloc: psi and hpsi must be device pointers");
   }
-  const int nrhs_v = nrhs;
+  const int nrhs_v = nrhs * c->nb0;
   std::vector<Item> items, sorted;
   long long max_need = 0;
   plan_items(c, nrhs_v, items, sorted, max_need);
   c->items_nrhs = -1;  // the allocating path rebuilds its own list next time
-  // carve: [counter | items | contributions | large-term slabs], 256-byte aligned
+  // carve: [counter | items | contributions | chunk partials | large-term slabs], 256-byte aligned
   auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
   const size_t off_items = 256;
   const size_t off_contrib = off_items + up(sorted.size() * sizeof(Item));
-  const size_t off_slabs = off_contrib + up((size_t)c->z.sum_nb * nrhs_v * 8);
+  const size_t off_part = off_contrib + up((size_t)c->z.sum_nb * nrhs_v * 8);
+  const size_t off_slabs = off_part + up((size_t)c->n_chunks * nrhs_v * 16);
   const long long per_cta = max_need > c->smem_doubles ? max_need : 0;
   // with large-term slabs, launch only as many CTAs as the array has slabs for
   int grid = c->grid;
@@ -1477,13 +1706,410 @@ extern "C" int evr_sg4_hpsi_noalloc(evr_sg4_ctx* c, int nrhs, const double* psi,
   p.contrib = (double*)(base + off_contrib);
   p.gscratch = per_cta ? (double*)(base + off_slabs) : nullptr;
   p.scratch_per_cta = per_cta;
-  hpsi_batched_kernel<<<grid, 256, (size_t)c->smem_doubles * 8, s>>>(p);
+  hpsi_batched_kernel<<<grid, EVR_CTA_THREADS, (size_t)c->smem_doubles * 8, s>>>(p);
   CUDA_TRY(cudaGetLastError());
-  int rc = launch_reduce(c, p.contrib, nrhs_v, 0, psi, ldpsi, hpsi, ldh, E0, Esc, s);
+  int rc = launch_reduce(c, p.contrib, (double2*)(base + off_part), nrhs_v, 0, psi, ldpsi, hpsi, ldh, E0, Esc, s);
   if (rc) return rc;
   CUDA_TRY(cudaGetLastError());
   // (both host lists were copied from pageable memory, which cudaMemcpyAsync
   // stages before it returns, so they may go out of scope now)
-  c->last_launches = 2;
+  c->last_launches = 3;
+  return EVR_OK;
+}
+
+// ------------------------------------------------------------------------
+// Several independent Hamiltonians in one persistent launch.  The plan owns
+// everything that depends on the right-hand-side count (term blocks, the
+// per-term contributions, chunk partials, one global-scratch slab per CTA
+// shared by all contexts) and the merged cost-sorted item list; the contexts
+// lend their read-only tables and operator grids.
+// ------------------------------------------------------------------------
+struct evr_sg4_multi {
+  int n = 0, cshift = 0, transpose = 0, grid = 0, smem_doubles = 0;
+  std::vector<evr_sg4_ctx*> ctxs;
+  std::vector<int> nrhs_v, type;
+  std::vector<TermInfo*> d_terms;
+  std::vector<double*> d_contrib;
+  std::vector<double*> d_part;
+  double* d_scratch = nullptr;
+  long long scratch_per_cta = 0;
+  std::vector<MItem> sorted;     // all contexts, decreasing cost
+  MItem* d_items = nullptr;      // the full list
+  MItem* d_sub = nullptr;        // a filtered list (some contexts skipped)
+  KParams* d_params = nullptr;
+  unsigned int* d_counter = nullptr;
+  long long last_launches = 0;
+};
+
+void evr::multi_shape(const evr_sg4_multi* m, std::vector<evr_sg4_ctx*>* ctxs, std::vector<int>* nrhs,
+                      int* cshift, int* transpose) {
+  *ctxs = m->ctxs;
+  nrhs->resize(m->n);
+  for (int k = 0; k < m->n; ++k) (*nrhs)[k] = (m->nrhs_v[k] >> m->cshift) / m->ctxs[k]->nb0;
+  *cshift = m->cshift;
+  *transpose = m->transpose;
+}
+
+static void free_multi(evr_sg4_multi* m) {
+  for (TermInfo* p : m->d_terms) if (p) cudaFree(p);
+  for (double* p : m->d_contrib) if (p) cudaFree(p);
+  for (double* p : m->d_part) if (p) cudaFree(p);
+  void* ptrs[] = {m->d_scratch, m->d_items, m->d_sub, m->d_params, m->d_counter};
+  for (void* q : ptrs) if (q) cudaFree(q);
+  delete m;
+}
+
+extern "C" int evr_sg4_multi_create(int n, evr_sg4_ctx* const* ctxs, const int* nrhs, int flags,
+                                    evr_sg4_multi** out) {
+  if (!out) return set_error(EVR_ERR_ARG, "multi_create: NULL output");
+  *out = nullptr;
+  if (n < 1 || !ctxs || !nrhs) return set_error(EVR_ERR_ARG, "multi_create: NULL argument or n < 1");
+  if (flags & ~(EVR_APPLY_TRANSPOSE | EVR_APPLY_COMPLEX)) return set_error(EVR_ERR_ARG, "multi_create: bad flags");
+  for (int k = 0; k < n; ++k) {
+    if (!ctxs[k] || !ctxs[k]->have_op) return set_error(EVR_ERR_STATE, "multi_create: context %d has no operator", k);
+    if (ctxs[k]->streamed)
+      return set_error(EVR_ERR_STATE, "multi_create: context %d streams its operator fields (use evr_sg4_hpsi)", k);
+    if (nrhs[k] < 1) return set_error(EVR_ERR_ARG, "multi_create: nrhs[%d]=%d < 1", k, nrhs[k]);
+    if (ctxs[k]->device != ctxs[0]->device) return set_error(EVR_ERR_ARG, "multi_create: contexts on different devices");
+  }
+  evr_sg4_multi* m = new evr_sg4_multi();
+  m->n = n;
+  m->cshift = (flags & EVR_APPLY_COMPLEX) ? 1 : 0;
+  m->transpose = (flags & EVR_APPLY_TRANSPOSE) ? 1 : 0;
+  m->grid = ctxs[0]->grid;
+  m->ctxs.assign(ctxs, ctxs + n);
+  m->nrhs_v.resize(n);
+  m->type.resize(n);
+  m->d_terms.assign(n, nullptr);
+  m->d_contrib.assign(n, nullptr);
+  m->d_part.assign(n, nullptr);
+  std::vector<MItem> all;
+  std::vector<float> allcost;
+  long long max_need = 0;
+  auto fail = [&](int rc) { free_multi(m); return rc; };
+  for (int k = 0; k < n; ++k) {
+    evr_sg4_ctx* c = ctxs[k];
+    const int nv = (nrhs[k] * c->nb0) << m->cshift;
+    m->nrhs_v[k] = nv;
+    m->type[k] = c->type;
+    m->grid = std::min(m->grid, c->grid);
+    m->smem_doubles = std::max(m->smem_doubles, c->smem_doubles);
+    std::vector<TermInfo> terms;
+    std::vector<Item> items;
+    std::vector<float> cost;
+    long long need = 0;
+    plan_work(c, nv, terms, items, cost, need);
+    if (need > c->smem_doubles) max_need = std::max(max_need, need);
+    for (size_t q = 0; q < items.size(); ++q) {
+      all.push_back(MItem{k, items[q].term, items[q].rhs0, 0});
+      allcost.push_back(cost[q]);
+    }
+    if (cudaMalloc(&m->d_terms[k], terms.size() * sizeof(TermInfo)) != cudaSuccess ||
+        cudaMemcpy(m->d_terms[k], terms.data(), terms.size() * sizeof(TermInfo), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMalloc(&m->d_contrib[k], (size_t)c->z.sum_nb * nv * 8) != cudaSuccess ||
+        cudaMalloc(&m->d_part[k], (size_t)c->n_chunks * nv * 16) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(set_error(EVR_ERR_CUDA, "multi_create: device allocation for context %d failed", k));
+    }
+  }
+  std::vector<int> order(all.size());
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return allcost[a] > allcost[b]; });
+  m->sorted.resize(all.size());
+  for (size_t q = 0; q < order.size(); ++q) m->sorted[q] = all[order[q]];
+  m->scratch_per_cta = max_need;
+  const size_t ni = m->sorted.size();
+  if ((max_need && cudaMalloc(&m->d_scratch, (size_t)max_need * m->grid * 8) != cudaSuccess) ||
+      cudaMalloc(&m->d_items, ni * sizeof(MItem)) != cudaSuccess ||
+      cudaMalloc(&m->d_sub, ni * sizeof(MItem)) != cudaSuccess ||
+      cudaMalloc(&m->d_params, (size_t)n * sizeof(KParams)) != cudaSuccess ||
+      cudaMalloc(&m->d_counter, sizeof(unsigned int)) != cudaSuccess ||
+      cudaMemcpy(m->d_items, m->sorted.data(), ni * sizeof(MItem), cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(set_error(EVR_ERR_CUDA, "multi_create: device allocation failed"));
+  }
+  *out = m;
+  return EVR_OK;
+}
+
+extern "C" int evr_sg4_multi_destroy(evr_sg4_multi* m) {
+  if (!m) return set_error(EVR_ERR_ARG, "multi_destroy: NULL plan");
+  cudaDeviceSynchronize();
+  free_multi(m);
+  return EVR_OK;
+}
+
+extern "C" int evr_sg4_multi_hpsi(evr_sg4_multi* m, const double* const* psi, const long long* ldpsi,
+                                  double* const* hpsi, const long long* ldh, const double* E0, const double* Esc,
+                                  void* stream) {
+  if (!m || !psi || !hpsi || !ldpsi || !ldh) return set_error(EVR_ERR_ARG, "multi_hpsi: NULL argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  std::vector<KParams> params(m->n);
+  int active = 0;
+  for (int k = 0; k < m->n; ++k) {
+    evr_sg4_ctx* c = m->ctxs[k];
+    if (!psi[k]) continue;  // context k is skipped in this call
+    if (!c->have_op || c->type != m->type[k] || c->streamed)
+      return set_error(EVR_ERR_STATE, "multi_hpsi: the operator of context %d changed since multi_create", k);
+    if (!hpsi[k] || ldpsi[k] < c->nvec || ldh[k] < c->nvec)
+      return set_error(EVR_ERR_ARG, "multi_hpsi: bad output or leading dimension for context %d", k);
+    const double e0 = E0 ? E0[k] : 0.0, esc = Esc ? Esc[k] : 1.0;
+    if (!(esc != 0.0) || !std::isfinite(esc) || !std::isfinite(e0))
+      return set_error(EVR_ERR_ARG, "multi_hpsi: Esc of context %d must be finite and non-zero", k);
+    KParams& p = params[k];
+    p = make_params(c, m->nrhs_v[k], m->cshift, psi[k], ldpsi[k] << m->cshift, hpsi[k], ldh[k] << m->cshift, 1.0);
+    p.transpose = m->transpose;
+    p.terms = m->d_terms[k];
+    p.contrib = m->d_contrib[k];
+    p.gscratch = m->d_scratch;
+    p.scratch_per_cta = m->scratch_per_cta;
+    p.counter = nullptr;
+    p.items = nullptr;
+    ++active;
+  }
+  if (active == 0) return set_error(EVR_ERR_ARG, "multi_hpsi: every context is skipped");
+  const MItem* items = m->d_items;
+  int n_items = (int)m->sorted.size();
+  if (active < m->n) {  // the sorted list without the skipped contexts
+    std::vector<MItem> sub;
+    sub.reserve(m->sorted.size());
+    for (const MItem& q : m->sorted)
+      if (psi[q.ctx]) sub.push_back(q);
+    CUDA_TRY(cudaMemcpyAsync(m->d_sub, sub.data(), sub.size() * sizeof(MItem), cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaStreamSynchronize(s));  // `sub` leaves scope
+    items = m->d_sub;
+    n_items = (int)sub.size();
+  }
+  CUDA_TRY(cudaMemcpyAsync(m->d_params, params.data(), (size_t)m->n * sizeof(KParams), cudaMemcpyHostToDevice, s));
+  CUDA_TRY(cudaMemsetAsync(m->d_counter, 0, sizeof(unsigned int), s));
+  CUDA_TRY(cudaFuncSetAttribute(hpsi_multi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                m->smem_doubles * 8));
+  hpsi_multi_kernel<<<m->grid, EVR_CTA_THREADS, (size_t)m->smem_doubles * 8, s>>>(m->d_params, items, n_items, 0,
+                                                                                   m->d_counter);
+  CUDA_TRY(cudaGetLastError());
+  for (int k = 0; k < m->n; ++k) {
+    if (!psi[k]) continue;
+    int rc = launch_reduce(m->ctxs[k], m->d_contrib[k], (double2*)m->d_part[k], m->nrhs_v[k], m->cshift, psi[k],
+                           ldpsi[k] << m->cshift, hpsi[k], ldh[k] << m->cshift, E0 ? E0[k] : 0.0,
+                           Esc ? Esc[k] : 1.0, s);
+    if (rc) return rc;
+  }
+  // `params` is pageable: the copy above is staged before cudaMemcpyAsync returns
+  m->last_launches = 1 + 2LL * active;
+  return EVR_OK;
+}
+
+extern "C" int evr_sg4_multi_last_launches(const evr_sg4_multi* m, long long* n) {
+  if (!m || !n) return set_error(EVR_ERR_ARG, "multi_last_launches: NULL argument");
+  *n = m->last_launches;
+  return EVR_OK;
+}
+
+extern "C" int evr_sg4_hpsi_multi(int n, evr_sg4_ctx* const* ctxs, const int* nrhs, const double* const* psi,
+                                  const long long* ldpsi, double* const* hpsi, const long long* ldh, const double* E0,
+                                  const double* Esc, int flags, void* stream) {
+  evr_sg4_multi* m = nullptr;
+  int rc = evr_sg4_multi_create(n, ctxs, nrhs, flags, &m);
+  if (rc) return rc;
+  rc = evr_sg4_multi_hpsi(m, psi, ldpsi, hpsi, ldh, E0, Esc, stream);
+  if (!rc && cudaStreamSynchronize((cudaStream_t)stream) != cudaSuccess)
+    rc = set_error(EVR_ERR_CUDA, "hpsi_multi: %s", cudaGetErrorString(cudaGetLastError()));
+  if (!rc)
+    for (int k = 0; k < n; ++k) ctxs[k]->last_launches = m->last_launches;
+  free_multi(m);
+  return rc;
+}
+
+// ------------------------------------------------------------------------
+// Two operators of one basis (H0 and mu of a field-driven propagation)
+// applied to one complex vector in one persistent launch, up to the chunk
+// partials of their ordered accumulations; the caller joins them (and fuses
+// its own element-wise update into that join).  The parameter blocks point
+// at a vector owned by the pair, so an apply uploads nothing and launches
+// two kernels: the merged item list, then the chunk sums of both operators
+// (which also rearms the work counter).
+// ------------------------------------------------------------------------
+struct evr::FieldPair {
+  evr_sg4_multi* m = nullptr;
+  double* x = nullptr;         // [N] complex input
+  double2* part = nullptr;     // [2][n_chunks][2]
+  int grid = 0;
+  long long N = 0;
+};
+
+__global__ void __launch_bounds__(256) pair_chunks_kernel(const double* __restrict__ contrib0,
+                                                          const double* __restrict__ contrib1,
+                                                          const long long* __restrict__ chunk_q, long long n_chunks,
+                                                          const long long* __restrict__ inv_idx,
+                                                          double2* __restrict__ part, unsigned int* counter) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) *counter = 0u;  // the item kernel before this one has finished
+  const long long per = n_chunks * 2, total = 2 * per;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int op = t >= per ? 1 : 0;
+    const long long r = t - op * per;
+    const long long ch = r >> 1;
+    const int v = (int)(r & 1);
+    const double* contrib = op ? contrib1 : contrib0;
+    double s = 0.0, c = 0.0;
+    for (long long q = chunk_q[ch]; q < chunk_q[ch + 1]; ++q) neumaier_add(s, c, contrib[inv_idx[q] * 2 + v]);
+    part[t] = make_double2(s, c);
+  }
+}
+
+int evr::field_pair_create(evr_sg4_ctx* a, evr_sg4_ctx* b, int transpose, FieldPair** out) {
+  *out = nullptr;
+  if (!a || !b) return set_error(EVR_ERR_ARG, "field pair: NULL context");
+  if (a->N != b->N || a->nb_SG != b->nb_SG || a->z.sum_nb != b->z.sum_nb || a->n_chunks != b->n_chunks)
+    return set_error(EVR_ERR_ARG, "field pair: the two operators are on different bases");
+  if (a->nb0 != 1 || b->nb0 != 1) return set_error(EVR_ERR_ARG, "field pair: one channel (nb0 = 1) only");
+  evr_sg4_ctx* cs[2] = {a, b};
+  const int nrhs[2] = {1, 1};
+  FieldPair* f = new FieldPair();
+  int rc = evr_sg4_multi_create(2, cs, nrhs, EVR_APPLY_COMPLEX | (transpose ? EVR_APPLY_TRANSPOSE : 0), &f->m);
+  if (rc) {
+    delete f;
+    return rc;
+  }
+  f->N = a->N;
+  if (cudaMalloc(&f->x, (size_t)a->N * 16) != cudaSuccess ||
+      cudaMalloc(&f->part, (size_t)a->n_chunks * 4 * sizeof(double2)) != cudaSuccess) {
+    cudaGetLastError();
+    field_pair_destroy(f);
+    return set_error(EVR_ERR_CUDA, "field pair: device allocation failed");
+  }
+  evr_sg4_multi* m = f->m;
+  KParams ps[2];
+  for (int k = 0; k < 2; ++k) {
+    ps[k] = make_params(cs[k], 2, 1, f->x, 2 * a->N, nullptr, 2 * a->N, 1.0);
+    ps[k].transpose = m->transpose;
+    ps[k].terms = m->d_terms[k];
+    ps[k].contrib = m->d_contrib[k];
+    ps[k].gscratch = m->d_scratch;
+    ps[k].scratch_per_cta = m->scratch_per_cta;
+    ps[k].counter = nullptr;
+    ps[k].items = nullptr;
+  }
+  if (cudaMemcpy(m->d_params, ps, sizeof(ps), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemset(m->d_counter, 0, sizeof(unsigned int)) != cudaSuccess) {
+    cudaGetLastError();
+    field_pair_destroy(f);
+    return set_error(EVR_ERR_CUDA, "field pair: parameter upload failed");
+  }
+  // enough CTAs for every item, so small operators leave SMs to other streams
+  f->grid = (int)std::min<size_t>((size_t)m->grid, std::max<size_t>(1, m->sorted.size()));
+  if (cudaFuncSetAttribute(hpsi_multi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, m->smem_doubles * 8) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    field_pair_destroy(f);
+    return set_error(EVR_ERR_CUDA, "field pair: shared-memory attribute");
+  }
+  *out = f;
+  return EVR_OK;
+}
+
+void evr::field_pair_destroy(FieldPair* f) {
+  if (!f) return;
+  if (f->m) free_multi(f->m);
+  if (f->x) cudaFree(f->x);
+  if (f->part) cudaFree(f->part);
+  delete f;
+}
+
+int evr::field_pair_apply(FieldPair* f, void* stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  evr_sg4_multi* m = f->m;
+  evr_sg4_ctx* c = m->ctxs[0];
+  hpsi_multi_kernel<<<f->grid, EVR_CTA_THREADS, (size_t)m->smem_doubles * 8, s>>>(
+      m->d_params, m->d_items, (int)m->sorted.size(), 0, m->d_counter);
+  const long long t1 = c->n_chunks * 4;
+  const long long b1 = std::max<long long>(1, std::min<long long>((t1 + 255) / 256, 16LL * c->num_sms));
+  pair_chunks_kernel<<<(unsigned)b1, 256, 0, s>>>(m->d_contrib[0], m->d_contrib[1], c->d_chunk_q, c->n_chunks,
+                                                 c->d_inv_idx, f->part, m->d_counter);
+  CUDA_TRY(cudaGetLastError());
+  return EVR_OK;
+}
+
+evr::FieldPairView evr::field_pair_view(const FieldPair* f) {
+  FieldPairView v;
+  const evr_sg4_ctx* c = f->m->ctxs[0];
+  v.N = f->N;
+  v.n_chunks = c->n_chunks;
+  v.fun_chunk = c->d_fun_chunk;
+  v.part = f->part;
+  v.x = f->x;
+  return v;
+}
+
+// ------------------------------------------------------------------------
+// Autotuner: the most right-hand sides one work item carries trades reuse of
+// the 1-D matrices and operator fields (large blocks) against the number and
+// balance of items (small blocks).  Times H.psi on nrhs vectors for each
+// candidate and keeps the fastest, as Tune_SG4threads_HPsi
+// (SRC/sub_main/vib.f90:2013-2123) times H.psi for each OpenMP thread count.
+// ------------------------------------------------------------------------
+extern "C" int evr_sg4_tune(evr_sg4_ctx* c, int nrhs, int flags, int* best_rmax, double* best_ms) {
+  if (!c || nrhs < 1) return set_error(EVR_ERR_ARG, "tune: NULL context or nrhs < 1");
+  if (!c->have_op) return set_error(EVR_ERR_STATE, "tune: set_operator was not called");
+  if (flags & ~EVR_APPLY_COMPLEX) return set_error(EVR_ERR_ARG, "tune: flags may only hold EVR_APPLY_COMPLEX");
+  const size_t n = (size_t)c->nvec * nrhs * ((flags & EVR_APPLY_COMPLEX) ? 2 : 1);
+  double *psi = nullptr, *out = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  auto cleanup = [&]() {
+    if (psi) cudaFree(psi);
+    if (out) cudaFree(out);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+  };
+  if (cudaMalloc(&psi, n * 8) != cudaSuccess || cudaMalloc(&out, n * 8) != cudaSuccess ||
+      cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    cudaGetLastError();
+    cleanup();
+    return set_error(EVR_ERR_CUDA, "tune: allocation failed");
+  }
+  {  // deterministic test vectors: a linear congruential sequence in [-1, 1)
+    std::vector<double> h(n);
+    unsigned long long st = 0x9E3779B97F4A7C15ull;
+    for (size_t k = 0; k < n; ++k) {
+      st = st * 6364136223846793005ull + 1442695040888963407ull;
+      h[k] = (double)(st >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+    }
+    if (cudaMemcpy(psi, h.data(), n * 8, cudaMemcpyHostToDevice) != cudaSuccess) {
+      cleanup();
+      return set_error(EVR_ERR_CUDA, "tune: upload failed");
+    }
+  }
+  const int keep = c->rmax;
+  int best = keep;
+  double best_t = 1e300;
+  for (int rmax : {1, 2, 4, 8, 16, 32}) {
+    c->rmax = rmax;
+    c->items_nrhs = -1;
+    int rc = evr_sg4_apply(c, flags, nrhs, psi, c->nvec, out, c->nvec, 0.0, 1.0, nullptr);  // plan + warm
+    float ms = 0.f, tot = 0.f;
+    for (int rep = 0; rep < 3 && !rc; ++rep) {
+      cudaEventRecord(e0, 0);
+      rc = evr_sg4_apply(c, flags, nrhs, psi, c->nvec, out, c->nvec, 0.0, 1.0, nullptr);
+      cudaEventRecord(e1, 0);
+      if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+        rc = set_error(EVR_ERR_CUDA, "tune: timing failed");
+      tot += ms;
+    }
+    if (rc) {
+      c->rmax = keep;
+      c->items_nrhs = -1;
+      cleanup();
+      return rc;
+    }
+    if (tot / 3.0 < best_t) {
+      best_t = tot / 3.0;
+      best = rmax;
+    }
+  }
+  c->rmax = best;
+  c->items_nrhs = -1;
+  cleanup();
+  if (best_rmax) *best_rmax = best;
+  if (best_ms) *best_ms = best_t;
   return EVR_OK;
 }

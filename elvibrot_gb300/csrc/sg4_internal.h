@@ -8,6 +8,7 @@
 
 #define EVR_MAXD 24   // modes per term handled by the kernels
 #define EVR_MAXN 16   // largest 1-D grid / basis size (nq, nb) per level
+#define EVR_MAXNB0 8  // channels (electronic states) per vector
 
 namespace evr {
 
@@ -26,6 +27,26 @@ struct DescSizes {
 
 int set_error(int code, const char* fmt, ...);
 int desc_sizes(const evr_sg4_desc* d, DescSizes* z);
+
+// Two operators on one basis applied to one complex vector in one launch,
+// up to the chunk partials of both ordered accumulations (part: [2][n_chunks]
+// [re, im] (s, c) pairs, operator 0 first); `x` is the device input vector
+// (N complex) of every apply.  `transpose` applies both transposed.
+struct FieldPair;
+struct FieldPairView {
+  long long N = 0, n_chunks = 0;
+  const long long* fun_chunk = nullptr;  // [N+1] first chunk of each packed function
+  const void* part = nullptr;            // double2 partials
+  double* x = nullptr;
+};
+int field_pair_create(evr_sg4_ctx* a, evr_sg4_ctx* b, int transpose, FieldPair** out);
+void field_pair_destroy(FieldPair* f);
+int field_pair_apply(FieldPair* f, void* stream);
+FieldPairView field_pair_view(const FieldPair* f);
+// Contexts, right-hand sides per context, complex shift and transpose flag
+// of a multi-context plan.
+void multi_shape(const evr_sg4_multi* m, std::vector<evr_sg4_ctx*>* ctxs, std::vector<int>* nrhs, int* cshift,
+                 int* transpose);
 
 }  // namespace evr
 

@@ -263,14 +263,29 @@ extern "C" int evr_sg4_basis_build_ho(int D, int L, int LB, int A_nb, int B_nb, 
                                       const double* Q0, const double* scaleQ, evr_sg4_basis** out) {
   if (!out) return set_error(EVR_ERR_ARG, "evr_sg4_basis_build_ho: out is NULL");
   *out = nullptr;
+  if (D < 1 || D > EVR_MAXD) return set_error(EVR_ERR_ARG, "evr_sg4_basis_build_ho: need 1 <= D <= %d", EVR_MAXD);
+  std::vector<int> a(D, A_nb), b(D, B_nb), c(D, A_nq), d(D, B_nq);
+  return evr_sg4_basis_build_ho_modes(D, L, LB, a.data(), b.data(), c.data(), d.data(), Q0, scaleQ, out);
+}
+
+extern "C" int evr_sg4_basis_build_ho_modes(int D, int L, int LB, const int* A_nb_m, const int* B_nb_m,
+                                            const int* A_nq_m, const int* B_nq_m, const double* Q0,
+                                            const double* scaleQ, evr_sg4_basis** out) {
+  if (!out) return set_error(EVR_ERR_ARG, "evr_sg4_basis_build_ho: out is NULL");
+  *out = nullptr;
   if (D < 1 || D > EVR_MAXD || L < 0 || LB < 0)
     return set_error(EVR_ERR_ARG, "evr_sg4_basis_build_ho: need 1 <= D <= %d, L >= 0, LB >= 0", EVR_MAXD);
-  if (A_nb < 1 || B_nb < 0 || A_nq < 1 || B_nq < 0)
-    return set_error(EVR_ERR_ARG, "evr_sg4_basis_build_ho: nb(0), nq(0) must be >= 1");
-  if (A_nb > A_nq || B_nb > B_nq)  // sub_read_data.f90:804 rejects nb > nq growth
-    return set_error(EVR_ERR_ARG, "evr_sg4_basis_build_ho: L_TO_nb must not exceed L_TO_nq");
-  if (A_nq + B_nq * L > EVR_MAXN)
-    return set_error(EVR_ERR_ARG, "evr_sg4_basis_build_ho: nq(L)=%d exceeds %d", A_nq + B_nq * L, EVR_MAXN);
+  if (!A_nb_m || !B_nb_m || !A_nq_m || !B_nq_m) return set_error(EVR_ERR_ARG, "evr_sg4_basis_build_ho: NULL rule");
+  for (int i = 0; i < D; ++i) {
+    const int A_nb = A_nb_m[i], B_nb = B_nb_m[i], A_nq = A_nq_m[i], B_nq = B_nq_m[i];
+    if (A_nb < 1 || B_nb < 0 || A_nq < 1 || B_nq < 0)
+      return set_error(EVR_ERR_ARG, "evr_sg4_basis_build_ho: nb(0), nq(0) must be >= 1 (mode %d)", i);
+    if (A_nb > A_nq || B_nb > B_nq)  // sub_read_data.f90:804 rejects nb > nq growth
+      return set_error(EVR_ERR_ARG, "evr_sg4_basis_build_ho: L_TO_nb must not exceed L_TO_nq (mode %d)", i);
+    if (A_nq + B_nq * L > EVR_MAXN)
+      return set_error(EVR_ERR_ARG, "evr_sg4_basis_build_ho: nq(L)=%d exceeds %d (mode %d)", A_nq + B_nq * L,
+                       EVR_MAXN, i);
+  }
   if (scaleQ)
     for (int i = 0; i < D; ++i)
       if (!(scaleQ[i] > 0.0)) return set_error(EVR_ERR_ARG, "evr_sg4_basis_build_ho: scaleQ must be > 0");
@@ -283,7 +298,7 @@ extern "C" int evr_sg4_basis_build_ho(int D, int L, int LB, int A_nb, int B_nb, 
   b->mats.resize((size_t)D * (L + 1));
   for (int i = 0; i < D; ++i)
     for (int l = 0; l <= L; ++l) {
-      int nb = A_nb + B_nb * l, nq = A_nq + B_nq * l;
+      int nb = A_nb_m[i] + B_nb_m[i] * l, nq = A_nq_m[i] + B_nq_m[i] * l;
       b->nb_of_l[i * (L + 1) + l] = nb;
       b->nq_of_l[i * (L + 1) + l] = nq;
       build_mode_level(b->mats[i * (L + 1) + l], nb, nq, Q0 ? Q0[i] : 0.0, scaleQ ? scaleQ[i] : 1.0);

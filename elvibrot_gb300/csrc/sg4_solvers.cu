@@ -1,9 +1,13 @@
 // sg4_solvers.cu -- the callers of the SG4 H.psi on the device: block
 // Davidson (sub_propagation_Davidson, SRC/sub_propagation/
-// sub_module_Davidson.f90:59-767) and the exact diagonal used as its
-// preconditioner.  Host C++ drives the iteration; every vector operation and
+// sub_module_Davidson.f90:59-767) with the exact diagonal as preconditioner,
+// Chebyshev propagation (march_cheby; single context, replayed from a CUDA
+// graph at fixed order, and many contexts in lock-step), and field-driven
+// RK4 with the adjoint optimal-control gradient (march_RK4_field, fcn_field,
+// build_field).  Host C++ drives the iterations; every vector operation and
 // every H.psi stays on the GPU (cuBLAS DGEMM for the small dense products of
-// the subspace), only the m x m projected matrix goes to the host.
+// the Davidson subspace), only m x m projected matrices and scalars go to
+// the host.
 #include <cublas_v2.h>
 #include <cuda_runtime.h>
 
@@ -14,6 +18,7 @@
 
 #include "evr_sg4.h"
 #include "sg4_internal.h"
+#include "sg4_reduce.cuh"
 
 namespace evr {
 
@@ -411,6 +416,72 @@ __global__ void cdot_cols_kernel(const double2* a, const double2* b, long long N
   }
 }
 
+// One fixed-order step, enqueued on s (recorded once as a CUDA graph and
+// replayed): save <- psi, the recurrence of order npoly on w1/w2, |w|^2 of
+// the last term into hb[0] (pinned), psi = out e^{-i E0 dt}, and the
+// autocorrelation <psi0|psi> into hb[1..].
+namespace evr {
+struct ChebyStep {
+  evr_sg4_ctx* c;
+  int nrhs;
+  long long N, n;
+  double *w1, *w2, *h, *out, *save, *nrm, *acb, *psi;
+  const double* P0;
+  double* hb;
+  bool autocorr;
+};
+}  // namespace evr
+
+static int enqueue_cheby_step(const ChebyStep& st, const std::vector<double>& cf, double E0, double Esc, double ph,
+                              cudaStream_t s) {
+  const int G = 2 * 152, B = 256;
+  const long long n = st.n;
+  double *a = st.w1, *b = st.w2;
+  CUDA_TRY_S(cudaMemcpyAsync(st.save, st.psi, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
+  CUDA_TRY_S(cudaMemcpyAsync(a, st.save, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
+  cscale_kernel<<<G, B, 0, s>>>((double2*)st.out, (const double2*)a, n, cf[0], 0.0);
+  int rc = evr_sg4_apply(st.c, EVR_APPLY_COMPLEX, st.nrhs, a, st.N, st.h, st.N, E0, Esc, s);
+  if (rc) return rc;
+  CUDA_TRY_S(cudaMemsetAsync(b, 0, (size_t)n * 16, s));
+  cheby_update_kernel<<<G, B, 0, s>>>((double2*)b, (const double2*)st.h, (double2*)st.out, n, 0.0, 0.0, -1.0, cf[1],
+                                      nullptr);
+  const int npoly = (int)cf.size();
+  for (int k = 3; k <= npoly; ++k) {
+    if ((rc = evr_sg4_apply(st.c, EVR_APPLY_COMPLEX, st.nrhs, b, st.N, st.h, st.N, E0, Esc, s))) return rc;
+    const bool last = k == npoly;
+    if (last) CUDA_TRY_S(cudaMemsetAsync(st.nrm, 0, 8, s));
+    cheby_update_kernel<<<G, B, 0, s>>>((double2*)a, (const double2*)st.h, (double2*)st.out, n, 1.0, 0.0, -2.0,
+                                        cf[k - 1], last ? st.nrm : nullptr);
+    std::swap(a, b);
+  }
+  if (npoly >= 3) CUDA_TRY_S(cudaMemcpyAsync(st.hb, st.nrm, 8, cudaMemcpyDeviceToHost, s));
+  cscale_kernel<<<G, B, 0, s>>>((double2*)st.psi, (const double2*)st.out, n, std::cos(ph), std::sin(ph));
+  if (st.autocorr) {
+    cdot_cols_kernel<<<st.nrhs, 256, 0, s>>>((const double2*)st.P0, (const double2*)st.psi, st.N, st.N,
+                                             (double2*)st.acb);
+    CUDA_TRY_S(cudaMemcpyAsync(st.hb + 1, st.acb, (size_t)st.nrhs * 16, cudaMemcpyDeviceToHost, s));
+  }
+  CUDA_TRY_S(cudaGetLastError());
+  return EVR_OK;
+}
+
+namespace evr {
+struct GraphGuard {
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t cs = nullptr;
+  double* hb = nullptr;
+  void reset() {
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
+  }
+  ~GraphGuard() {
+    reset();
+    if (cs) cudaStreamDestroy(cs);
+    if (hb) cudaFreeHost(hb);
+  }
+};
+}  // namespace evr
+
 extern "C" int evr_sg4_cheby_propagate(evr_sg4_ctx* c, const evr_cheby_opts* o, int nrhs, double* psi,
                                        const double* psi0, double* autocorr, int* npoly_used, void* stream) {
   if (!c || !o || !psi || nrhs < 1) return set_error(EVR_ERR_ARG, "cheby: NULL argument or nrhs < 1");
@@ -452,7 +523,31 @@ extern "C" int evr_sg4_cheby_propagate(evr_sg4_ctx* c, const evr_cheby_opts* o, 
     return EVR_OK;
   };
   if ((rc = autocorr_at(0))) return rc;
+  // fixed order: once a step has run eagerly, the step is recorded as a CUDA
+  // graph and replayed; a replayed step that diverges is undone from `save`
+  // and redone eagerly (with Hmax raised), after which the graph is recorded again
+  const bool use_graph = o->poly_tol <= 0.0 && !o->no_graph;
+  GraphGuard gg;
+  std::vector<double> gcf;
+  if (use_graph) {
+    CUDA_TRY_S(cudaStreamCreateWithFlags(&gg.cs, cudaStreamNonBlocking));
+    CUDA_TRY_S(cudaMallocHost(&gg.hb, (size_t)(1 + 2 * nrhs) * 8));
+  }
+  const ChebyStep cst{c, nrhs, N, n, w1.p, w2.p, h.p, out.p, save.p, nrm.p, acb.p, psi, (const double*)P0,
+                      gg.hb, autocorr != nullptr};
   for (int step = 0; step < o->nsteps; ++step) {
+    if (gg.exec) {
+      CUDA_TRY_S(cudaGraphLaunch(gg.exec, s));
+      CUDA_TRY_S(cudaStreamSynchronize(s));
+      const double norm_exit = o->npoly >= 3 ? std::fabs(gg.hb[0] * gcf[o->npoly - 1]) : 0.0;
+      if (norm_exit <= 1e15) {
+        if (autocorr) memcpy(autocorr + (size_t)2 * nrhs * (step + 1), gg.hb + 1, (size_t)nrhs * 16);
+        used = std::max(used, o->npoly);
+        continue;
+      }
+      CUDA_TRY_S(cudaMemcpyAsync(psi, save.p, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));  // undo
+      gg.reset();
+    }
     CUDA_TRY_S(cudaMemcpyAsync(save.p, psi, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
     bool ok = false;
     for (int attempt = 0; attempt < 10 && !ok; ++attempt) {
@@ -505,6 +600,29 @@ extern "C" int evr_sg4_cheby_propagate(evr_sg4_ctx* c, const evr_cheby_opts* o, 
     }
     if (!ok) return set_error(EVR_ERR_NUMERIC, "cheby: step %d did not converge after 10 Hmax increases", step);
     if ((rc = autocorr_at(step + 1))) return rc;
+    if (use_graph && step + 1 < o->nsteps) {  // record the step with the bounds that worked
+      const double dE = Hmax - Hmin, gE0 = Hmin + 0.5 * dE;
+      bessel_j(0.5 * dE * o->dt, o->npoly, J);
+      gcf.assign(o->npoly, 0.0);
+      gcf[0] = J[0];
+      for (int k = 1; k < o->npoly; ++k) gcf[k] = 2.0 * J[k];
+      CUDA_TRY_S(cudaStreamSynchronize(s));
+      cudaGraph_t graph = nullptr;
+      CUDA_TRY_S(cudaStreamBeginCapture(gg.cs, cudaStreamCaptureModeRelaxed));
+      rc = enqueue_cheby_step(cst, gcf, gE0, 0.5 * dE, -gE0 * o->dt, gg.cs);
+      cudaError_t ec = cudaStreamEndCapture(gg.cs, &graph);
+      if (rc) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+      }
+      if (ec != cudaSuccess) return set_error(EVR_ERR_CUDA, "cheby: graph capture: %s", cudaGetErrorString(ec));
+      ec = cudaGraphInstantiate(&gg.exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (ec != cudaSuccess) {
+        gg.exec = nullptr;
+        return set_error(EVR_ERR_CUDA, "cheby: graph instantiate: %s", cudaGetErrorString(ec));
+      }
+    }
   }
   CUDA_TRY_S(cudaStreamSynchronize(s));
   if (npoly_used) *npoly_used = used;
@@ -525,114 +643,181 @@ extern "C" int evr_sg4_cheby_propagate(evr_sg4_ctx* c, const evr_cheby_opts* o, 
 //   sb_i = A^dagger kb_i = i (H0^T - E mu^T) kb_i,  lambda_{k-1} = l + sum sb_i,
 //   dJ/dE_k = sum_i 2 Re(kb_i^dagger (i mu s_i)),
 // s_i the stage inputs of step k.  psi is checkpointed every `checkpoint`
-// field intervals and each segment is recomputed (keeping its stages and
-// mu s_i) before its backward sweep, so the gradient costs about three
-// forward propagations.  Each field interval dt is integrated with nsub RK4
-// steps of dt/nsub (E held over the interval), which keeps fixed-step RK4
-// accurate when dt times the spectral range is too large for one step.
+// field intervals and each segment is recomputed (keeping its stage inputs)
+// before its backward sweep.  Each field interval dt is integrated with nsub
+// RK4 steps of dt/nsub (E held over the interval), which keeps fixed-step
+// RK4 accurate when dt times the spectral range is too large for one step.
 // The reference's control update (build_field, SRC/sub_propagation/
 // sub_control.f90:907-1010) uses the continuous-time form of the same
 // derivative, -2 Im(S* <chi(t)|mu|psi(t)>).
 // ------------------------------------------------------------------------
 
-// k = -i (h1 - E h2)  [sign = -1]   or   k = +i (h1 - E h2)  [sign = +1]
-__global__ void field_f_kernel(double2* k, const double2* h1, const double2* h2, long long n, double E, double sign) {
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
-    const double2 a = h1[e], b = h2[e];
-    const double re = a.x - E * b.x, im = a.y - E * b.y;
-    k[e] = make_double2(-sign * im, sign * re);  // sign * i * (re + i im)
+// The two operators of a stage (H0 and mu, or both transposed) run in one
+// persistent launch (field_pair_apply); the kernels below join their chunk
+// partials in the same order as evr_sg4_hpsi and fuse the stage arithmetic.
+struct StageIn {
+  const double2* part;         // [2][n_chunks][2] (s, c) partials, H0 first
+  const long long* fun_chunk;  // [N+1]
+  long long nch2;              // 2 n_chunks: offset of mu's partials
+  long long N;
+  double2* x;                  // stage input, overwritten by the next stage's input
+  double E, E0, h;
+};
+
+__device__ __forceinline__ void stage_sums(const StageIn& a, long long n, double2 xv, double& re, double& im,
+                                           double& mr, double& mi) {
+  const long long c0 = a.fun_chunk[n], c1 = a.fun_chunk[n + 1];
+  double hr = join_chunks(a.part, c0, c1, 2, 0), hi = join_chunks(a.part, c0, c1, 2, 1);
+  mr = join_chunks(a.part + a.nch2, c0, c1, 2, 0);
+  mi = join_chunks(a.part + a.nch2, c0, c1, 2, 1);
+  if (a.E0 != 0.0) {  // (H0 - E0) x, as the scaled H.psi writes it
+    hr = hr - a.E0 * xv.x;
+    hi = hi - a.E0 * xv.y;
+  }
+  re = hr - a.E * mr;
+  im = hi - a.E * mi;
+}
+
+__device__ __forceinline__ double2 cmul(double2 t, double cr, double ci) {
+  return make_double2(cr * t.x - ci * t.y, cr * t.y + ci * t.x);
+}
+
+// forward stage i of an RK4 step y -> y (h = step):
+//   k = -i ((H0 - E0) x - E mu x);  [rec = x]
+//   i=1: acc = y + h/6 k, x = y + h/2 k     i=2: acc += h/3 k, x = y + h/2 k
+//   i=3: acc += h/3 k,    x = y + h k       i=4: y = (acc + h/6 k) e^{-i E0 h}, x = y
+__global__ void __launch_bounds__(256) rk_stage_kernel(StageIn a, int stage, double2* y, double2* acc, double2* rec,
+                                                       double cr, double ci) {
+  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < a.N; n += (long long)gridDim.x * blockDim.x) {
+    const double2 xv = a.x[n];
+    double re, im, mr, mi;
+    stage_sums(a, n, xv, re, im, mr, mi);
+    const double2 k = make_double2(im, -re);  // -i (re + i im)
+    if (rec) rec[n] = xv;
+    const double2 yv = y[n];
+    const double h = a.h;
+    if (stage == 1) {
+      acc[n] = make_double2(fma(h / 6.0, k.x, yv.x), fma(h / 6.0, k.y, yv.y));
+      a.x[n] = make_double2(fma(0.5 * h, k.x, yv.x), fma(0.5 * h, k.y, yv.y));
+    } else if (stage < 4) {
+      const double2 ac = acc[n];
+      acc[n] = make_double2(fma(h / 3.0, k.x, ac.x), fma(h / 3.0, k.y, ac.y));
+      const double c = stage == 2 ? 0.5 * h : h;
+      a.x[n] = make_double2(fma(c, k.x, yv.x), fma(c, k.y, yv.y));
+    } else {
+      const double2 ac = acc[n];
+      double2 t = make_double2(fma(h / 6.0, k.x, ac.x), fma(h / 6.0, k.y, ac.y));
+      if (a.E0 != 0.0) t = cmul(t, cr, ci);
+      y[n] = t;
+      a.x[n] = t;
+    }
   }
 }
 
-// out = x + a y   (complex vectors, real a)
-__global__ void zaxpy_kernel(double2* out, const double2* x, double a, const double2* y, long long n) {
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
-    const double2 u = x[e], v = y[e];
-    out[e] = make_double2(fma(a, v.x, u.x), fma(a, v.y, u.y));
-  }
-}
-
-// acc[0] += -2 Im(a^dagger b) = -2 sum (a.x b.y - a.y b.x)  (one block, deterministic)
-__global__ void grad_term_kernel(const double2* a, const double2* b, long long n, double* acc) {
-  double s = 0.0;
-  for (long long e = threadIdx.x; e < n; e += blockDim.x) {
-    const double2 x = a[e], y = b[e];
-    s = fma(x.x, y.y, fma(-x.y, y.x, s));
+// adjoint stage i (taken 4, 3, 2, 1) of one RK4 step, costate l (phased):
+//   sb = +i ((H0^T - E0) kb - E mu^T kb),  kb = x;
+//   gpart[block] = -2 Im((mu^T kb)^dagger s_i) = -2 Im(kb^dagger mu s_i), s_i the stage input;
+//   i=4: yb = l + sb, x = h/3 l + h sb       i=3: yb += sb, x = h/3 l + h/2 sb
+//   i=2: yb += sb, x = h/6 l + h/2 sb        i=1: l = (yb + sb) e^{+i E0 h}, x = h/6 l
+// (the last form also prepares the previous step's stage 4)
+__global__ void __launch_bounds__(256) rk_adjoint_stage_kernel(StageIn a, int stage, double2* l, double2* yb,
+                                                               const double2* s, double* gpart, double cr,
+                                                               double ci) {
+  double g = 0.0;
+  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < a.N; n += (long long)gridDim.x * blockDim.x) {
+    const double2 xv = a.x[n];
+    double re, im, mr, mi;
+    stage_sums(a, n, xv, re, im, mr, mi);
+    const double2 sb = make_double2(-im, re);  // +i (re + i im)
+    const double2 sv = s[n];
+    g = fma(mr, sv.y, fma(-mi, sv.x, g));
+    const double2 lv = l[n];
+    const double h = a.h;
+    if (stage == 4) {
+      yb[n] = make_double2(fma(1.0, sb.x, lv.x), fma(1.0, sb.y, lv.y));
+      a.x[n] = make_double2(fma(h, sb.x, (h / 3.0) * lv.x), fma(h, sb.y, (h / 3.0) * lv.y));
+    } else if (stage > 1) {
+      const double2 b = yb[n];
+      yb[n] = make_double2(fma(1.0, sb.x, b.x), fma(1.0, sb.y, b.y));
+      const double c = stage == 3 ? h / 3.0 : h / 6.0;
+      a.x[n] = make_double2(fma(0.5 * h, sb.x, c * lv.x), fma(0.5 * h, sb.y, c * lv.y));
+    } else {
+      const double2 b = yb[n];
+      double2 t = make_double2(fma(1.0, sb.x, b.x), fma(1.0, sb.y, b.y));
+      if (a.E0 != 0.0) t = cmul(t, cr, ci);
+      l[n] = t;
+      a.x[n] = make_double2((h / 6.0) * t.x, (h / 6.0) * t.y);
+    }
   }
   __shared__ double sh[32];
-  for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  for (int off = 16; off > 0; off >>= 1) g += __shfl_down_sync(0xffffffffu, g, off);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = g;
   __syncthreads();
   if (threadIdx.x == 0) {
     double t = 0.0;
     for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += sh[k];
-    acc[0] += -2.0 * t;
+    gpart[blockIdx.x] = -2.0 * t;
+  }
+}
+
+// l = lambda e^{+i E0 h}, x = h/6 l: the start of the backward sweep
+__global__ void rk_adjoint_start_kernel(double2* l, const double2* lam, double2* x, long long N, double h, double cr,
+                                        double ci, int phase) {
+  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < N; n += (long long)gridDim.x * blockDim.x) {
+    double2 t = lam[n];
+    if (phase) t = cmul(t, cr, ci);
+    l[n] = t;
+    x[n] = make_double2((h / 6.0) * t.x, (h / 6.0) * t.y);
+  }
+}
+
+// g[k] = sum of the stage partials of field interval k: nsub steps x 4 stages x nblk blocks, in that order
+__global__ void rk_grad_sum_kernel(const double* gpart, int nsteps, int nsub, int nblk, double* g) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nsteps; k += gridDim.x * blockDim.x) {
+    double t = 0.0;
+    const double* q = gpart + (size_t)k * nsub * 4 * nblk;
+    for (int e = 0; e < nsub * 4 * nblk; ++e) t += q[e];
+    g[k] = t;
   }
 }
 
 namespace evr {
 
-struct FieldOps {
-  evr_sg4_ctx* H0;
-  evr_sg4_ctx* mu;
-  double E0;   // energy shift of fcn_field's sub_scaledOpPsi(WP, dWP, para_H%E0, ONE)
-  long long N;
-  cudaStream_t s;
-  double* h1;  // scratch N complex
-  double* h2;
+// RK4 steps driven by a FieldPair (forward operators), fused per stage
+struct FwdSweep {
+  FieldPair* fp;
+  FieldPairView v;
+  double* y;    // device complex N
+  double* acc;
+  int nblk;
 };
 
-// k = -i (H0 x - E mu x); optionally keeps mu x in mux
-static int field_f(FieldOps& f, const double* x, double* k, double E, double* mux) {
-  double* m = mux ? mux : f.h2;
-  int rc = evr_sg4_apply(f.H0, EVR_APPLY_COMPLEX, 1, x, f.N, f.h1, f.N, f.E0, 1.0, f.s);
-  if (rc) return rc;
-  if ((rc = evr_sg4_apply(f.mu, EVR_APPLY_COMPLEX, 1, x, f.N, m, f.N, 0.0, 1.0, f.s))) return rc;
-  field_f_kernel<<<64, 256, 0, f.s>>>((double2*)k, (const double2*)f.h1, (const double2*)m, f.N, E, -1.0);
+static int rk4_step_fused(FwdSweep& w, double E, double E0, double h, double* rec, cudaStream_t s) {
+  StageIn a{(const double2*)w.v.part, w.v.fun_chunk, 2 * w.v.n_chunks, w.v.N, (double2*)w.v.x, E, E0, h};
+  const double cr = std::cos(E0 * h), ci = -std::sin(E0 * h);
+  for (int stage = 1; stage <= 4; ++stage) {
+    int rc = field_pair_apply(w.fp, s);
+    if (rc) return rc;
+    rk_stage_kernel<<<w.nblk, 256, 0, s>>>(a, stage, (double2*)w.y, (double2*)w.acc,
+                                           rec ? (double2*)rec + (size_t)(stage - 1) * w.v.N : nullptr, cr, ci);
+  }
   CUDA_TRY_S(cudaGetLastError());
   return EVR_OK;
 }
 
-// sb = i (H0^T kb - E mu^T kb)
-static int field_fadj(FieldOps& f, const double* kb, double* sb, double E) {
-  int rc = evr_sg4_apply(f.H0, EVR_APPLY_COMPLEX | EVR_APPLY_TRANSPOSE, 1, kb, f.N, f.h1, f.N, f.E0, 1.0, f.s);
-  if (rc) return rc;
-  if ((rc = evr_sg4_apply(f.mu, EVR_APPLY_COMPLEX | EVR_APPLY_TRANSPOSE, 1, kb, f.N, f.h2, f.N, 0.0, 1.0, f.s)))
-    return rc;
-  field_f_kernel<<<64, 256, 0, f.s>>>((double2*)sb, (const double2*)f.h1, (const double2*)f.h2, f.N, E, +1.0);
-  CUDA_TRY_S(cudaGetLastError());
-  return EVR_OK;
-}
-
-// one RK4 step y -> y (in place); st (if given) receives s1..s4 then mu s1..mu s4
-static int rk4_step(FieldOps& f, double* y, double E, double dt, double* st, double* k, double* acc, double* sbuf) {
-  const long long n = f.N;
-  auto S = [&](int i) { return st ? st + (size_t)i * 2 * n : sbuf; };
-  auto M = [&](int i) { return st ? st + (size_t)(4 + i) * 2 * n : nullptr; };
-  // acc = y ; s1 = y
-  CUDA_TRY_S(cudaMemcpyAsync(acc, y, (size_t)n * 16, cudaMemcpyDeviceToDevice, f.s));
-  double* s1 = S(0);
-  if (st) CUDA_TRY_S(cudaMemcpyAsync(s1, y, (size_t)n * 16, cudaMemcpyDeviceToDevice, f.s));
-  int rc = field_f(f, st ? s1 : y, k, E, M(0));                          // k1
-  if (rc) return rc;
-  zaxpy_kernel<<<64, 256, 0, f.s>>>((double2*)acc, (const double2*)acc, dt / 6.0, (const double2*)k, n);
-  double* s2 = S(1);
-  zaxpy_kernel<<<64, 256, 0, f.s>>>((double2*)s2, (const double2*)y, 0.5 * dt, (const double2*)k, n);
-  if ((rc = field_f(f, s2, k, E, M(1)))) return rc;                      // k2
-  zaxpy_kernel<<<64, 256, 0, f.s>>>((double2*)acc, (const double2*)acc, dt / 3.0, (const double2*)k, n);
-  double* s3 = st ? S(2) : s2;
-  zaxpy_kernel<<<64, 256, 0, f.s>>>((double2*)s3, (const double2*)y, 0.5 * dt, (const double2*)k, n);
-  if ((rc = field_f(f, s3, k, E, M(2)))) return rc;                      // k3
-  zaxpy_kernel<<<64, 256, 0, f.s>>>((double2*)acc, (const double2*)acc, dt / 3.0, (const double2*)k, n);
-  double* s4 = st ? S(3) : s3;
-  zaxpy_kernel<<<64, 256, 0, f.s>>>((double2*)s4, (const double2*)y, dt, (const double2*)k, n);
-  if ((rc = field_f(f, s4, k, E, M(3)))) return rc;                      // k4
-  zaxpy_kernel<<<64, 256, 0, f.s>>>((double2*)y, (const double2*)acc, dt / 6.0, (const double2*)k, n);
-  if (f.E0 != 0.0)  // WP = WP exp(-i E0 dt) (march_RK4_field :533-535)
-    cscale_kernel<<<64, 256, 0, f.s>>>((double2*)y, (const double2*)y, n, std::cos(f.E0 * dt), -std::sin(f.E0 * dt));
-  CUDA_TRY_S(cudaGetLastError());
-  return EVR_OK;
-}
+struct PairGuard {
+  FieldPair* p = nullptr;
+  ~PairGuard() { field_pair_destroy(p); }
+};
+struct StreamGuard {
+  cudaStream_t s = nullptr;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  ~StreamGuard() {
+    for (cudaEvent_t e : ev)
+      if (e) cudaEventDestroy(e);
+    if (s) cudaStreamDestroy(s);
+  }
+};
 
 }  // namespace evr
 
@@ -651,6 +836,8 @@ static int check_field_args(evr_sg4_ctx* H0, evr_sg4_ctx* mu, const evr_rk4_opts
   return EVR_OK;
 }
 
+static int join_blocks(long long N) { return (int)std::max<long long>(1, std::min<long long>((N + 255) / 256, 1024)); }
+
 extern "C" int evr_sg4_rk4_field(evr_sg4_ctx* H0, evr_sg4_ctx* mu, const evr_rk4_opts* o, const double* E, double* psi,
                                  void* stream) {
   long long N = 0;
@@ -658,96 +845,260 @@ extern "C" int evr_sg4_rk4_field(evr_sg4_ctx* H0, evr_sg4_ctx* mu, const evr_rk4
   if (rc) return rc;
   if (!psi) return set_error(EVR_ERR_ARG, "rk4: psi is NULL");
   cudaStream_t s = (cudaStream_t)stream;
-  DevBuf h1, h2, k, acc, sb;
-  for (DevBuf* b : {&h1, &h2, &k, &acc, &sb}) CUDA_TRY_S(cudaMalloc(&b->p, (size_t)N * 16));
-  FieldOps f{H0, mu, o->E0, N, s, h1.p, h2.p};
-  const int nsub = o->nsub;
+  PairGuard fp;
+  if ((rc = field_pair_create(H0, mu, 0, &fp.p))) return rc;
+  DevBuf acc;
+  CUDA_TRY_S(cudaMalloc(&acc.p, (size_t)N * 16));
+  FwdSweep w{fp.p, field_pair_view(fp.p), psi, acc.p, join_blocks(N)};
+  CUDA_TRY_S(cudaMemcpyAsync(w.v.x, psi, (size_t)N * 16, cudaMemcpyDeviceToDevice, s));
+  const double hs = o->dt / o->nsub;
   for (int st = 0; st < o->nsteps; ++st)
-    for (int u = 0; u < nsub; ++u)
-      if ((rc = rk4_step(f, psi, E[st], o->dt / nsub, nullptr, k.p, acc.p, sb.p))) return rc;
+    for (int u = 0; u < o->nsub; ++u)
+      if ((rc = rk4_step_fused(w, E[st], o->E0, hs, nullptr, s))) return rc;
   CUDA_TRY_S(cudaStreamSynchronize(s));
   return EVR_OK;
 }
 
+// Optimal-control gradient.  Stream A runs the forward sweep (checkpoints
+// every C field intervals, the stages of the last segment kept), then the
+// backward sweep segment by segment; stream B recomputes segment k-1 from
+// its checkpoint (keeping its stage inputs) while stream A runs the adjoint
+// of segment k, with two stage buffers alternating between them.  Both
+// streams' launches are small, so they share the SMs.
 extern "C" int evr_sg4_oc_gradient(evr_sg4_ctx* H0, evr_sg4_ctx* mu, const evr_rk4_opts* o, const double* E,
                                    const double* psi0, const double* target, double* J, double* grad, void* stream) {
   long long N = 0;
   int rc = check_field_args(H0, mu, o, E, &N);
   if (rc) return rc;
   if (!psi0 || !target || !J || !grad) return set_error(EVR_ERR_ARG, "oc_gradient: NULL argument");
-  cudaStream_t s = (cudaStream_t)stream;
-  const int C = o->checkpoint, ns = o->nsteps, nseg = (ns + C - 1) / C;
+  cudaStream_t sA = (cudaStream_t)stream;
+  StreamGuard sg;
+  CUDA_TRY_S(cudaStreamCreateWithFlags(&sg.s, cudaStreamNonBlocking));
+  for (cudaEvent_t& e : sg.ev) CUDA_TRY_S(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  cudaStream_t sB = sg.s;
+  const int C = o->checkpoint, ns = o->nsteps, nseg = (ns + C - 1) / C, nsub = o->nsub;
+  const double hs = o->dt / nsub;
   const size_t vb = (size_t)N * 16;
-  DevBuf h1, h2, k, acc, sb, y, ck, st, lam, yb, kb1, kb2, kb3, kb4, sv, g, ov;
-  for (DevBuf* b : {&h1, &h2, &k, &acc, &sb, &y, &lam, &yb, &kb1, &kb2, &kb3, &kb4, &sv})
-    CUDA_TRY_S(cudaMalloc(&b->p, vb));
-  CUDA_TRY_S(cudaMalloc(&ck.p, vb * (nseg + 1)));            // checkpoints
-  const int nsub = o->nsub;
-  const double hs = o->dt / nsub;                            // RK4 step inside a field interval
-  CUDA_TRY_S(cudaMalloc(&st.p, vb * 8 * (size_t)C * nsub));  // stages of one segment
+  const int nblk = join_blocks(N);
+  PairGuard fwd, adj;
+  if ((rc = field_pair_create(H0, mu, 0, &fwd.p)) || (rc = field_pair_create(H0, mu, 1, &adj.p))) return rc;
+  DevBuf y, acc, ck, rec, lam, l, yb, gpart, g, ov;
+  for (DevBuf* b : {&y, &acc, &lam, &l, &yb}) CUDA_TRY_S(cudaMalloc(&b->p, vb));
+  CUDA_TRY_S(cudaMalloc(&ck.p, vb * nseg));                                // checkpoints
+  const size_t seg_rec = (size_t)C * nsub * 4 * 2 * N;                    // doubles: stage inputs of a segment
+  CUDA_TRY_S(cudaMalloc(&rec.p, seg_rec * 2 * 8));                         // two alternating segment buffers
+  CUDA_TRY_S(cudaMalloc(&gpart.p, (size_t)ns * nsub * 4 * nblk * 8));
   CUDA_TRY_S(cudaMalloc(&g.p, (size_t)ns * 8));
   CUDA_TRY_S(cudaMalloc(&ov.p, 16));
-  CUDA_TRY_S(cudaMemsetAsync(g.p, 0, (size_t)ns * 8, s));
-  FieldOps f{H0, mu, o->E0, N, s, h1.p, h2.p};
-  // forward sweep, keeping psi at the start of every segment
-  CUDA_TRY_S(cudaMemcpyAsync(y.p, psi0, vb, cudaMemcpyDeviceToDevice, s));
+  FwdSweep w{fwd.p, field_pair_view(fwd.p), y.p, acc.p, nblk};
+  auto rec_of = [&](int seg, int stp, int u) {
+    return rec.p + (size_t)(seg & 1) * seg_rec + ((size_t)(stp - seg * C) * nsub + u) * 4 * 2 * N;
+  };
+  // forward sweep (stream A)
+  CUDA_TRY_S(cudaMemcpyAsync(y.p, psi0, vb, cudaMemcpyDeviceToDevice, sA));
+  CUDA_TRY_S(cudaMemcpyAsync(w.v.x, psi0, vb, cudaMemcpyDeviceToDevice, sA));
   for (int stp = 0; stp < ns; ++stp) {
-    if (stp % C == 0) CUDA_TRY_S(cudaMemcpyAsync(ck.p + (size_t)(stp / C) * 2 * N, y.p, vb, cudaMemcpyDeviceToDevice, s));
+    const int seg = stp / C;
+    if (stp % C == 0) CUDA_TRY_S(cudaMemcpyAsync(ck.p + (size_t)seg * 2 * N, y.p, vb, cudaMemcpyDeviceToDevice, sA));
     for (int u = 0; u < nsub; ++u)
-      if ((rc = rk4_step(f, y.p, E[stp], hs, nullptr, k.p, acc.p, sb.p))) return rc;
+      if ((rc = rk4_step_fused(w, E[stp], o->E0, hs, seg == nseg - 1 ? rec_of(seg, stp, u) : nullptr, sA))) return rc;
   }
   // S = <target|psi_N>, J = |S|^2, lambda_N = S target
-  cdot_cols_kernel<<<1, 256, 0, s>>>((const double2*)target, (const double2*)y.p, N, N, (double2*)ov.p);
+  cdot_cols_kernel<<<1, 256, 0, sA>>>((const double2*)target, (const double2*)y.p, N, N, (double2*)ov.p);
   double2 S;
-  CUDA_TRY_S(cudaMemcpyAsync(&S, ov.p, 16, cudaMemcpyDeviceToHost, s));
-  CUDA_TRY_S(cudaStreamSynchronize(s));
+  CUDA_TRY_S(cudaMemcpyAsync(&S, ov.p, 16, cudaMemcpyDeviceToHost, sA));
+  CUDA_TRY_S(cudaStreamSynchronize(sA));  // also: the forward pair and its buffers are free for stream B
   *J = S.x * S.x + S.y * S.y;
-  cscale_kernel<<<64, 256, 0, s>>>((double2*)lam.p, (const double2*)target, N, S.x, S.y);
-  // backward sweep, segment by segment
+  cscale_kernel<<<64, 256, 0, sA>>>((double2*)lam.p, (const double2*)target, N, S.x, S.y);
+  const FieldPairView av = field_pair_view(adj.p);
+  const double cr = std::cos(o->E0 * hs), ci = std::sin(o->E0 * hs);  // e^{+i E0 h}
+  rk_adjoint_start_kernel<<<nblk, 256, 0, sA>>>((double2*)l.p, (const double2*)lam.p, (double2*)av.x, N, hs, cr, ci,
+                                                o->E0 != 0.0);
+  CUDA_TRY_S(cudaGetLastError());
+  cudaEvent_t ready[2] = {sg.ev[0], sg.ev[1]}, freed[2] = {sg.ev[2], sg.ev[3]};
+  StageIn a{(const double2*)av.part, av.fun_chunk, 2 * av.n_chunks, N, (double2*)av.x, 0.0, o->E0, hs};
   for (int seg = nseg - 1; seg >= 0; --seg) {
-    const int a = seg * C, b = std::min(ns, a + C);
-    CUDA_TRY_S(cudaMemcpyAsync(y.p, ck.p + (size_t)seg * 2 * N, vb, cudaMemcpyDeviceToDevice, s));
-    for (int stp = a; stp < b; ++stp)  // recompute, keeping s_i and mu s_i of every RK4 step
-      for (int u = 0; u < nsub; ++u)
-        if ((rc = rk4_step(f, y.p, E[stp], hs, st.p + ((size_t)(stp - a) * nsub + u) * 8 * 2 * N, k.p, acc.p,
-                           sb.p)))
-          return rc;
-    for (int sub = (b - a) * nsub - 1; sub >= 0; --sub) {
-      const int stp = a + sub / nsub;
-      const double* sts = st.p + (size_t)sub * 8 * 2 * N;
-      auto MU = [&](int i) { return (const double2*)(sts + (size_t)(4 + i) * 2 * N); };
-      const double h = hs, Ek = E[stp];
-      double* gk = g.p + stp;
-      const double2* L = (const double2*)lam.p;
-      // the step ends with the phase exp(-i E0 h): its adjoint multiplies l by exp(+i E0 h)
-      if (o->E0 != 0.0)
-        cscale_kernel<<<64, 256, 0, s>>>((double2*)lam.p, (const double2*)lam.p, N, std::cos(o->E0 * h),
-                                         std::sin(o->E0 * h));
-      // yb = l; kb4 = h/6 l
-      CUDA_TRY_S(cudaMemcpyAsync(yb.p, lam.p, vb, cudaMemcpyDeviceToDevice, s));
-      cscale_kernel<<<64, 256, 0, s>>>((double2*)kb4.p, L, N, h / 6.0, 0.0);
-      if ((rc = field_fadj(f, kb4.p, sv.p, Ek))) return rc;  // sb4
-      grad_term_kernel<<<1, 256, 0, s>>>((const double2*)kb4.p, MU(3), N, gk);
-      zaxpy_kernel<<<64, 256, 0, s>>>((double2*)yb.p, (const double2*)yb.p, 1.0, (const double2*)sv.p, N);
-      cscale_kernel<<<64, 256, 0, s>>>((double2*)kb3.p, L, N, h / 3.0, 0.0);
-      zaxpy_kernel<<<64, 256, 0, s>>>((double2*)kb3.p, (const double2*)kb3.p, h, (const double2*)sv.p, N);
-      if ((rc = field_fadj(f, kb3.p, sv.p, Ek))) return rc;  // sb3
-      grad_term_kernel<<<1, 256, 0, s>>>((const double2*)kb3.p, MU(2), N, gk);
-      zaxpy_kernel<<<64, 256, 0, s>>>((double2*)yb.p, (const double2*)yb.p, 1.0, (const double2*)sv.p, N);
-      cscale_kernel<<<64, 256, 0, s>>>((double2*)kb2.p, L, N, h / 3.0, 0.0);
-      zaxpy_kernel<<<64, 256, 0, s>>>((double2*)kb2.p, (const double2*)kb2.p, 0.5 * h, (const double2*)sv.p, N);
-      if ((rc = field_fadj(f, kb2.p, sv.p, Ek))) return rc;  // sb2
-      grad_term_kernel<<<1, 256, 0, s>>>((const double2*)kb2.p, MU(1), N, gk);
-      zaxpy_kernel<<<64, 256, 0, s>>>((double2*)yb.p, (const double2*)yb.p, 1.0, (const double2*)sv.p, N);
-      cscale_kernel<<<64, 256, 0, s>>>((double2*)kb1.p, L, N, h / 6.0, 0.0);
-      zaxpy_kernel<<<64, 256, 0, s>>>((double2*)kb1.p, (const double2*)kb1.p, 0.5 * h, (const double2*)sv.p, N);
-      if ((rc = field_fadj(f, kb1.p, sv.p, Ek))) return rc;  // sb1
-      grad_term_kernel<<<1, 256, 0, s>>>((const double2*)kb1.p, MU(0), N, gk);
-      zaxpy_kernel<<<64, 256, 0, s>>>((double2*)lam.p, (const double2*)yb.p, 1.0, (const double2*)sv.p, N);
-      CUDA_TRY_S(cudaGetLastError());
+    if (seg > 0) {  // stream B: recompute segment seg-1 into the other buffer
+      const int ps = seg - 1;
+      if (seg + 1 < nseg) CUDA_TRY_S(cudaStreamWaitEvent(sB, freed[ps & 1], 0));
+      CUDA_TRY_S(cudaMemcpyAsync(y.p, ck.p + (size_t)ps * 2 * N, vb, cudaMemcpyDeviceToDevice, sB));
+      CUDA_TRY_S(cudaMemcpyAsync(w.v.x, y.p, vb, cudaMemcpyDeviceToDevice, sB));
+      for (int stp = ps * C; stp < std::min(ns, (ps + 1) * C); ++stp)
+        for (int u = 0; u < nsub; ++u)
+          if ((rc = rk4_step_fused(w, E[stp], o->E0, hs, rec_of(ps, stp, u), sB))) return rc;
+      CUDA_TRY_S(cudaEventRecord(ready[ps & 1], sB));
     }
+    if (seg < nseg - 1) CUDA_TRY_S(cudaStreamWaitEvent(sA, ready[seg & 1], 0));
+    const int a0 = seg * C, b0 = std::min(ns, a0 + C);
+    for (int stp = b0 - 1; stp >= a0; --stp) {  // stream A: adjoint of segment seg
+      a.E = E[stp];
+      for (int u = nsub - 1; u >= 0; --u) {
+        const double2* st = (const double2*)rec_of(seg, stp, u);
+        double* gp = gpart.p + ((size_t)stp * nsub + (nsub - 1 - u)) * 4 * nblk;
+        for (int stage = 4; stage >= 1; --stage) {
+          if ((rc = field_pair_apply(adj.p, sA))) return rc;
+          rk_adjoint_stage_kernel<<<nblk, 256, 0, sA>>>(a, stage, (double2*)l.p, (double2*)yb.p,
+                                                        st + (size_t)(stage - 1) * N, gp + (4 - stage) * nblk, cr,
+                                                        ci);
+        }
+      }
+    }
+    CUDA_TRY_S(cudaGetLastError());
+    CUDA_TRY_S(cudaEventRecord(freed[seg & 1], sA));
   }
-  CUDA_TRY_S(cudaMemcpyAsync(grad, g.p, (size_t)ns * 8, cudaMemcpyDeviceToHost, s));
+  rk_grad_sum_kernel<<<(ns + 255) / 256, 256, 0, sA>>>(gpart.p, ns, nsub, nblk, g.p);
+  CUDA_TRY_S(cudaMemcpyAsync(grad, g.p, (size_t)ns * 8, cudaMemcpyDeviceToHost, sA));
+  CUDA_TRY_S(cudaStreamSynchronize(sA));
+  CUDA_TRY_S(cudaStreamSynchronize(sB));
+  return EVR_OK;
+}
+
+// ------------------------------------------------------------------------
+// Chebyshev propagation of every context of a complex multi-context plan in
+// lock-step (the batched uneven-instance workload): each expansion order is
+// ONE evr_sg4_multi_hpsi over all contexts still in their step, with each
+// context's own (E0, Esc) fused, followed by the per-context recurrence
+// update.  Per context the arithmetic is that of evr_sg4_cheby_propagate
+// with a fixed order (march_cheby, sub_module_propa_march.f90:4145-4437); a
+// context whose step diverges (> 1e15) redoes the step with its Hmax raised
+// by (Hmax-Hmin)/10 (:4362), alone with the other diverged contexts.
+// ------------------------------------------------------------------------
+extern "C" int evr_sg4_multi_cheby_propagate(evr_sg4_multi* m, const evr_cheby_opts* o, double* const* psi,
+                                             double* const* autocorr, int* npoly_used, void* stream) {
+  if (!m || !o || !psi) return set_error(EVR_ERR_ARG, "multi_cheby: NULL argument");
+  std::vector<evr_sg4_ctx*> ctxs;
+  std::vector<int> nv;
+  int cshift = 0, transpose = 0;
+  multi_shape(m, &ctxs, &nv, &cshift, &transpose);
+  const int n = (int)ctxs.size();
+  if (!cshift || transpose) return set_error(EVR_ERR_ARG, "multi_cheby: the plan must be complex, not transposed");
+  const double dt = o[0].dt;
+  const int npoly = o[0].npoly, nsteps = o[0].nsteps;
+  for (int k = 0; k < n; ++k) {
+    if (!psi[k]) return set_error(EVR_ERR_ARG, "multi_cheby: psi[%d] is NULL", k);
+    if (!(o[k].Hmax > o[k].Hmin) || !(o[k].dt > 0) || o[k].npoly < 2 || o[k].nsteps < 0)
+      return set_error(EVR_ERR_ARG, "multi_cheby: context %d needs Hmax > Hmin, dt > 0, npoly >= 2", k);
+    if (o[k].dt != dt || o[k].npoly != npoly || o[k].nsteps != nsteps || o[k].poly_tol > 0.0)
+      return set_error(EVR_ERR_ARG, "multi_cheby: dt, npoly, nsteps must agree and poly_tol be <= 0 (fixed order)");
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  std::vector<long long> N(n), len(n), off(n + 1, 0);
+  for (int k = 0; k < n; ++k) {
+    long long sz[8];
+    int rc = evr_sg4_ctx_sizes(ctxs[k], sz);
+    if (rc) return rc;
+    N[k] = sz[0];
+    len[k] = N[k] * nv[k];  // complex elements
+    off[k + 1] = off[k] + len[k];
+  }
+  // per context: w1, w2, h, out, psi0 (complex), carved from one pool
+  DevBuf pool, nrm, acb;
+  const long long tot = off[n];
+  CUDA_TRY_S(cudaMalloc(&pool.p, (size_t)tot * 5 * 16));
+  CUDA_TRY_S(cudaMalloc(&nrm.p, (size_t)n * 8));
+  const int max_nrhs = *std::max_element(nv.begin(), nv.end());
+  CUDA_TRY_S(cudaMalloc(&acb.p, (size_t)max_nrhs * 16));
+  auto buf = [&](int which, int k) { return (double2*)pool.p + which * tot + off[k]; };
+  std::vector<double2*> w1(n), w2(n);
+  for (int k = 0; k < n; ++k) {
+    w1[k] = buf(0, k);
+    w2[k] = buf(1, k);
+    CUDA_TRY_S(cudaMemcpyAsync(buf(4, k), psi[k], (size_t)len[k] * 16, cudaMemcpyDeviceToDevice, s));
+  }
+  const int G = 2 * 152, B = 256;
+  auto autocorr_at = [&](int step) -> int {
+    if (!autocorr) return EVR_OK;
+    for (int k = 0; k < n; ++k) {
+      if (!autocorr[k]) continue;
+      const int nr = nv[k];
+      cdot_cols_kernel<<<nr, 256, 0, s>>>(buf(4, k), (const double2*)psi[k], N[k], N[k], (double2*)acb.p);
+      CUDA_TRY_S(cudaGetLastError());
+      CUDA_TRY_S(cudaMemcpyAsync(autocorr[k] + (size_t)2 * nr * step, acb.p, (size_t)nr * 16, cudaMemcpyDeviceToHost,
+                                 s));
+      CUDA_TRY_S(cudaStreamSynchronize(s));  // acb is reused by the next context
+    }
+    return EVR_OK;
+  };
+  int rc = autocorr_at(0);
+  if (rc) return rc;
+  std::vector<double> Hmin(n), Hmax(n), E0(n), Esc(n), hnrm(n);
+  for (int k = 0; k < n; ++k) {
+    Hmin[k] = o[k].Hmin;
+    Hmax[k] = o[k].Hmax;
+  }
+  std::vector<std::vector<double>> cf(n);
+  std::vector<double> J;
+  std::vector<const double*> src(n);
+  std::vector<double*> dst(n);
+  std::vector<long long> ld(N.begin(), N.end());
+  std::vector<char> pending(n);
+  for (int step = 0; step < nsteps; ++step) {
+    std::fill(pending.begin(), pending.end(), 1);
+    for (int attempt = 0; attempt < 10; ++attempt) {
+      for (int k = 0; k < n; ++k) {
+        src[k] = nullptr;
+        if (!pending[k]) continue;
+        const double dE = Hmax[k] - Hmin[k], r = 0.5 * dE * dt;
+        E0[k] = Hmin[k] + 0.5 * dE;
+        Esc[k] = 0.5 * dE;
+        bessel_j(r, npoly, J);
+        cf[k].assign(npoly, 0.0);
+        cf[k][0] = J[0];
+        for (int q = 1; q < npoly; ++q) cf[k][q] = 2.0 * J[q];
+        w1[k] = buf(0, k);
+        w2[k] = buf(1, k);
+        CUDA_TRY_S(cudaMemcpyAsync(w1[k], psi[k], (size_t)len[k] * 16, cudaMemcpyDeviceToDevice, s));
+        cscale_kernel<<<G, B, 0, s>>>(buf(3, k), w1[k], len[k], cf[k][0], 0.0);
+        CUDA_TRY_S(cudaMemsetAsync(w2[k], 0, (size_t)len[k] * 16, s));
+      }
+      // w2 = -i Hs w1, out += c_2 w2 ; then w3 = w1 - 2i Hs w2, out += c_k w3
+      for (int ord = 2; ord <= npoly; ++ord) {
+        for (int k = 0; k < n; ++k) {
+          src[k] = pending[k] ? (const double*)(ord == 2 ? w1[k] : w2[k]) : nullptr;
+          dst[k] = (double*)buf(2, k);
+        }
+        if ((rc = evr_sg4_multi_hpsi(m, src.data(), ld.data(), dst.data(), ld.data(), E0.data(), Esc.data(), s)))
+          return rc;
+        const bool last = ord == npoly;
+        if (last) CUDA_TRY_S(cudaMemsetAsync(nrm.p, 0, (size_t)n * 8, s));
+        for (int k = 0; k < n; ++k) {
+          if (!pending[k]) continue;
+          if (ord == 2) {
+            cheby_update_kernel<<<G, B, 0, s>>>(w2[k], buf(2, k), buf(3, k), len[k], 0.0, 0.0, -1.0, cf[k][1],
+                                                last ? nrm.p + k : nullptr);
+          } else {
+            cheby_update_kernel<<<G, B, 0, s>>>(w1[k], buf(2, k), buf(3, k), len[k], 1.0, 0.0, -2.0,
+                                                cf[k][ord - 1], last ? nrm.p + k : nullptr);
+            std::swap(w1[k], w2[k]);
+          }
+        }
+        CUDA_TRY_S(cudaGetLastError());
+      }
+      CUDA_TRY_S(cudaMemcpyAsync(hnrm.data(), nrm.p, (size_t)n * 8, cudaMemcpyDeviceToHost, s));
+      CUDA_TRY_S(cudaStreamSynchronize(s));
+      bool any = false;
+      for (int k = 0; k < n; ++k) {
+        if (!pending[k]) continue;
+        const double norm_exit = std::fabs(hnrm[k] * cf[k][npoly - 1]);
+        if (!(norm_exit <= 1e15)) {
+          Hmax[k] += 0.1 * (Hmax[k] - Hmin[k]);
+          any = true;
+          continue;
+        }
+        const double ph = -E0[k] * dt;  // psi = out exp(-i E0 dt)
+        cscale_kernel<<<G, B, 0, s>>>((double2*)psi[k], buf(3, k), len[k], std::cos(ph), std::sin(ph));
+        pending[k] = 0;
+      }
+      CUDA_TRY_S(cudaGetLastError());
+      if (!any) break;
+    }
+    for (int k = 0; k < n; ++k)
+      if (pending[k])
+        return set_error(EVR_ERR_NUMERIC, "multi_cheby: context %d, step %d did not converge after 10 Hmax increases",
+                         k, step);
+    if ((rc = autocorr_at(step + 1))) return rc;
+  }
   CUDA_TRY_S(cudaStreamSynchronize(s));
+  if (npoly_used) *npoly_used = npoly;
   return EVR_OK;
 }

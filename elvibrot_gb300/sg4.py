@@ -74,7 +74,8 @@ class DavidsonOpts(ctypes.Structure):
 
 class ChebyOpts(ctypes.Structure):
     _fields_ = [("Hmin", ctypes.c_double), ("Hmax", ctypes.c_double), ("dt", ctypes.c_double),
-                ("npoly", ctypes.c_int), ("nsteps", ctypes.c_int), ("poly_tol", ctypes.c_double)]
+                ("npoly", ctypes.c_int), ("nsteps", ctypes.c_int), ("poly_tol", ctypes.c_double),
+                ("no_graph", ctypes.c_int)]
 
 
 class RK4Opts(ctypes.Structure):
@@ -97,6 +98,7 @@ def _declare(L):
     sig = {
         "evr_sg4_desc_sizes": [ctypes.POINTER(Desc), ctypes.POINTER(ll)],
         "evr_sg4_basis_build_ho": [ctypes.c_int] * 7 + [dp, dp, ctypes.POINTER(vp)],
+        "evr_sg4_basis_build_ho_modes": [ctypes.c_int] * 3 + [ip] * 4 + [dp, dp, ctypes.POINTER(vp)],
         "evr_sg4_basis_desc": [vp, ctypes.POINTER(Desc)],
         "evr_sg4_basis_grid_points": [vp, dp],
         "evr_sg4_create": [ctypes.POINTER(Desc), ctypes.POINTER(vp)],
@@ -116,6 +118,18 @@ def _declare(L):
         "evr_sg4_cheby_propagate": [vp, ctypes.POINTER(ChebyOpts), ctypes.c_int, vp, vp, dp,
                                     ctypes.POINTER(ctypes.c_int), vp],
         "evr_sg4_diagonal": [vp, vp, vp],
+        "evr_sg4_set_field_budget": [vp, ll],
+        "evr_sg4_field_slices": [vp, ctypes.POINTER(ll)],
+        "evr_sg4_tune": [vp, ctypes.c_int, ctypes.c_int, ip, dp],
+        "evr_sg4_hpsi_multi": [ctypes.c_int, ctypes.POINTER(vp), ip, ctypes.POINTER(vp), ctypes.POINTER(ll),
+                               ctypes.POINTER(vp), ctypes.POINTER(ll), dp, dp, ctypes.c_int, vp],
+        "evr_sg4_multi_create": [ctypes.c_int, ctypes.POINTER(vp), ip, ctypes.c_int, ctypes.POINTER(vp)],
+        "evr_sg4_multi_hpsi": [vp, ctypes.POINTER(vp), ctypes.POINTER(ll), ctypes.POINTER(vp), ctypes.POINTER(ll),
+                               dp, dp, vp],
+        "evr_sg4_multi_last_launches": [vp, ctypes.POINTER(ll)],
+        "evr_sg4_multi_destroy": [vp],
+        "evr_sg4_multi_cheby_propagate": [vp, ctypes.POINTER(ChebyOpts), ctypes.POINTER(vp), ctypes.POINTER(vp),
+                                          ctypes.POINTER(ctypes.c_int), vp],
         "evr_sg4_davidson": [vp, ctypes.POINTER(DavidsonOpts), vp, ctypes.c_int, vp, dp, vp, dp,
                              ctypes.POINTER(ctypes.c_int), vp],
     }
@@ -147,23 +161,33 @@ def _ip(a):
 class SG4Basis:
     """SG4 basis of D harmonic-oscillator modes (nb(l) = A_nb + B_nb l, nq(l) = A_nq + B_nq l)."""
 
-    def __init__(self, D: int, L: int, LB: Optional[int] = None, A_nb: int = 1, B_nb: int = 1,
-                 A_nq: int = 2, B_nq: int = 1, Q0: Optional[Sequence[float]] = None,
-                 scaleQ: Optional[Sequence[float]] = None):
+    def __init__(self, D: int, L: int, LB: Optional[int] = None, A_nb=1, B_nb=1, A_nq=2, B_nq=1,
+                 Q0: Optional[Sequence[float]] = None, scaleQ: Optional[Sequence[float]] = None, nb0: int = 1):
+        """A_nb, B_nb, A_nq, B_nq: one rule for every mode or a sequence of D rules;
+        nb0: channels (electronic states) of the vectors."""
         self.D, self.L = int(D), int(L)
         self.LB = self.L if LB is None else int(LB)
         self.A_nb, self.B_nb, self.A_nq, self.B_nq = A_nb, B_nb, A_nq, B_nq
         self.Q0 = np.zeros(D) if Q0 is None else np.ascontiguousarray(Q0, dtype=np.float64)
         self.scaleQ = np.ones(D) if scaleQ is None else np.ascontiguousarray(scaleQ, dtype=np.float64)
         h = ctypes.c_void_p()
-        check(lib().evr_sg4_basis_build_ho(self.D, self.L, self.LB, A_nb, B_nb, A_nq, B_nq,
-                                           _dp(self.Q0), _dp(self.scaleQ), ctypes.byref(h)))
+        if all(np.ndim(v) == 0 for v in (A_nb, B_nb, A_nq, B_nq)):
+            check(lib().evr_sg4_basis_build_ho(self.D, self.L, self.LB, int(A_nb), int(B_nb), int(A_nq), int(B_nq),
+                                               _dp(self.Q0), _dp(self.scaleQ), ctypes.byref(h)))
+        else:
+            rule = lambda v: np.ascontiguousarray(np.broadcast_to(np.asarray(v, dtype=np.int32), (self.D,)))
+            self._rules = [rule(v) for v in (A_nb, B_nb, A_nq, B_nq)]
+            check(lib().evr_sg4_basis_build_ho_modes(self.D, self.L, self.LB, *[_ip(r) for r in self._rules],
+                                                     _dp(self.Q0), _dp(self.scaleQ), ctypes.byref(h)))
         self._h = h
         self.desc = Desc()
         check(lib().evr_sg4_basis_desc(self._h, ctypes.byref(self.desc)))
+        self.desc.nb0 = int(nb0)
         z = (ctypes.c_longlong * 8)()
         check(lib().evr_sg4_desc_sizes(ctypes.byref(self.desc), z))
         self.N, self.nb_SG, self.sum_nb, self.sum_nq, self.max_nb, self.max_nq = [int(v) for v in z[:6]]
+        self.nb0 = int(nb0)
+        self.nvec = self.nb0 * self.N      # length of a vector (nb0 channel blocks of N)
 
     def __del__(self):
         if getattr(self, "_h", None) and _lib is not None:
@@ -208,7 +232,7 @@ class SG4Tables:
     matrices are column-major: RGB nq x nb, RBGwrho nb x nq, d1GG/d2GG nq x nq.
     """
 
-    def __init__(self, D, L, LB, nb_of_l, nq_of_l, x, RGB, RBGwrho, d1GG, d2GG, tab_l, weight, map_, N):
+    def __init__(self, D, L, LB, nb_of_l, nq_of_l, x, RGB, RBGwrho, d1GG, d2GG, tab_l, weight, map_, N, nb0=1):
         self.D, self.L, self.LB = int(D), int(L), int(LB)
         i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32).ravel()
         f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64).ravel()
@@ -216,12 +240,14 @@ class SG4Tables:
                           RBGwrho=f64(RBGwrho), d1GG=f64(d1GG), d2GG=f64(d2GG), tab_l=i32(tab_l),
                           weight=f64(weight), map=i32(map_))
         k = self._keep
-        self.desc = Desc(self.D, self.L, self.LB, 1, _ip(k["nb_of_l"]), _ip(k["nq_of_l"]), _dp(k["x"]),
+        self.desc = Desc(self.D, self.L, self.LB, int(nb0), _ip(k["nb_of_l"]), _ip(k["nq_of_l"]), _dp(k["x"]),
                          _dp(k["RGB"]), _dp(k["RBGwrho"]), _dp(k["d1GG"]), _dp(k["d2GG"]),
                          len(k["weight"]), _ip(k["tab_l"]), _dp(k["weight"]), _ip(k["map"]), int(N))
         z = (ctypes.c_longlong * 8)()
         check(lib().evr_sg4_desc_sizes(ctypes.byref(self.desc), z))
         self.N, self.nb_SG, self.sum_nb, self.sum_nq, self.max_nb, self.max_nq = [int(v) for v in z[:6]]
+        self.nb0 = int(nb0)
+        self.nvec = self.nb0 * self.N
 
 
 @dataclass
@@ -255,12 +281,14 @@ class ParamOp:
                  V_poly: Optional[Polynomial] = None, G: Optional[np.ndarray] = None,
                  G0: Optional[np.ndarray] = None, G1: Optional[np.ndarray] = None,
                  Jac: Optional[np.ndarray] = None, sqRho: Optional[np.ndarray] = None,
-                 F2: Optional[np.ndarray] = None, F1: Optional[np.ndarray] = None):
+                 F2: Optional[np.ndarray] = None, F1: Optional[np.ndarray] = None, field_budget: int = 0):
         self.basis = basis
         self.type_op = int(type_op)
         h = ctypes.c_void_p()
         check(lib().evr_sg4_create(ctypes.byref(basis.desc), ctypes.byref(h)))
         self._h = h
+        if field_budget:
+            check(lib().evr_sg4_set_field_budget(h, int(field_budget)))
         self.set_operator(V=V, V_poly=V_poly, G=G, G0=G0, G1=G1, Jac=Jac, sqRho=sqRho, F2=F2, F1=F1)
 
     def set_operator(self, V=None, V_poly=None, G=None, G0=None, G1=None, Jac=None, sqRho=None, F2=None, F1=None):
@@ -283,6 +311,20 @@ class ParamOp:
             _lib.evr_sg4_destroy(self._h)
             self._h = None
 
+    def tune(self, nrhs: int, complex_: bool = False):
+        """Times H.psi for each cap on the right-hand sides per work item and keeps
+        the fastest (evr_sg4_tune); returns (cap, ms)."""
+        r, t = ctypes.c_int(), ctypes.c_double()
+        check(lib().evr_sg4_tune(self._h, int(nrhs), 2 if complex_ else 0, ctypes.byref(r), ctypes.byref(t)))
+        return r.value, t.value
+
+    @property
+    def field_slices(self) -> int:
+        """Slices the analytic operator fields are evaluated in per H.psi (0: resident)."""
+        n = ctypes.c_longlong()
+        check(lib().evr_sg4_field_slices(self._h, ctypes.byref(n)))
+        return n.value
+
     @property
     def flops_per_rhs(self) -> float:
         f = ctypes.c_double()
@@ -299,7 +341,7 @@ class ParamOp:
     def hpsi_dev(self, psi, out, E0: float = 0.0, Esc: float = 1.0, stream: int = 0, plain: bool = False,
                  transpose: bool = False):
         import torch
-        N = self.basis.N
+        N = self.basis.nvec
         if psi.dtype not in (torch.float64, torch.complex128) or not psi.is_cuda:
             raise EVRError(1, "psi must be a CUDA float64/complex128 tensor")
         cplx = psi.dtype == torch.complex128
@@ -325,7 +367,7 @@ class ParamOp:
     def diagonal(self):
         """Exact diag(H) as a CUDA tensor (the Davidson preconditioner)."""
         import torch
-        d = torch.empty(self.basis.N, dtype=torch.float64, device="cuda")
+        d = torch.empty(self.basis.nvec, dtype=torch.float64, device="cuda")
         check(lib().evr_sg4_diagonal(self._h, d.data_ptr(), 0))
         return d
 
@@ -335,7 +377,7 @@ class ParamOp:
         (CUDA tensor nev x N), residual norms, iterations); raises EVRError
         when max_it is reached."""
         import torch
-        N = self.basis.N
+        N = self.basis.nvec
         o = DavidsonOpts(nev, block, max_subspace, max_it, conv_resi, 1 if symmetrize else 0)
         ev = np.zeros(nev)
         rs = np.zeros(nev)
@@ -348,7 +390,7 @@ class ParamOp:
         return ev, vec, rs, its.value
 
     def cheby_propagate(self, psi, Hmin: float, Hmax: float, dt: float, npoly: int, nsteps: int,
-                        poly_tol: float = 0.0, psi0=None):
+                        poly_tol: float = 0.0, psi0=None, graph: bool = True):
         """Propagates the CUDA complex128 tensor psi (nrhs, N) in place
         (march_cheby); returns (autocorrelation [(nsteps+1), nrhs], npoly used)."""
         import torch
@@ -358,7 +400,7 @@ class ParamOp:
         nrhs = P.shape[0]
         ac = np.zeros((nsteps + 1) * nrhs * 2)
         used = ctypes.c_int()
-        o = ChebyOpts(Hmin, Hmax, dt, npoly, nsteps, poly_tol)
+        o = ChebyOpts(Hmin, Hmax, dt, npoly, nsteps, poly_tol, 0 if graph else 1)
         check(lib().evr_sg4_cheby_propagate(self._h, ctypes.byref(o), nrhs, P.data_ptr(),
                                             psi0.data_ptr() if psi0 is not None else None, _dp(ac),
                                             ctypes.byref(used), 0))
@@ -386,7 +428,7 @@ class ParamOp:
 
     def hpsi_host(self, psi: np.ndarray, E0: float = 0.0, Esc: float = 1.0) -> np.ndarray:
         """psi (N,) or (N, nrhs) host float64; returns the same shape (copies in/out)."""
-        N = self.basis.N
+        N = self.basis.nvec
         a = np.asarray(psi, dtype=np.float64)
         one = a.ndim == 1
         P = np.asfortranarray(a.reshape(N, -1))
@@ -416,7 +458,7 @@ def sub_TabOpPsi(Psi, para_Op: ParamOp, E0: float = 0.0, Esc: float = 1.0):
     if a.size == 0:
         raise EVRError(1, "size(Psi) = 0")
     if np.iscomplexobj(a):
-        return para_Op.hpsi_host(a.real, E0, Esc) + 1j * para_Op.hpsi_host(a.imag, 0.0 if E0 == 0 else E0, Esc)
+        return para_Op.hpsi_host(a.real, E0, Esc) + 1j * para_Op.hpsi_host(a.imag, E0, Esc)
     return para_Op.hpsi_host(a, E0, Esc)
 
 
@@ -428,6 +470,112 @@ def sub_OpPsi(Psi, para_Op: ParamOp):
 def sub_scaledOpPsi(Psi, para_Op: ParamOp, E0: float, Esc: float):
     """(H Psi - E0 Psi) / Esc (sub_OpPsi.f90:2821-2864), fused into the H.psi launch."""
     return sub_TabOpPsi(Psi, para_Op, E0=E0, Esc=Esc)
+
+
+def _check_blocks(ops, psis, outs, dtype):
+    n = len(ops)
+    if n == 0 or len(psis) != n or len(outs) != n:
+        raise EVRError(1, "ops, psis and outs must be non-empty lists of equal length")
+    rows = []
+    for op, P, O in zip(ops, psis, outs):
+        P2 = P if P.dim() == 2 else P.unsqueeze(0)
+        O2 = O if O.dim() == 2 else O.unsqueeze(0)
+        if (not P2.is_cuda or P2.dtype != dtype or P2.shape[-1] != op.basis.nvec or O2.shape != P2.shape
+                or O2.dtype != dtype or not P2.is_contiguous() or not O2.is_contiguous()):
+            raise EVRError(1, f"every psi/out must be a contiguous CUDA (nrhs, N) {dtype} tensor")
+        rows.append(P2.shape[0])
+    return rows
+
+
+class MultiOp:
+    """Several independent ParamOps applied in one persistent launch per call
+    (evr_sg4_multi_*).  ``nrhs[k]`` vectors per operator, real or complex.
+    No reference counterpart: ElVibRot applies one para_Op per sub_TabOpPsi
+    call (sub_OpPsi.f90:705)."""
+
+    def __init__(self, ops, nrhs, complex_: bool = False, transpose: bool = False):
+        self.ops = list(ops)
+        self.nrhs = [int(r) for r in nrhs]
+        self.complex_ = complex_
+        n = len(self.ops)
+        self._h = ctypes.c_void_p()
+        flags = (1 if transpose else 0) | (2 if complex_ else 0)
+        check(lib().evr_sg4_multi_create(n, (ctypes.c_void_p * n)(*[op._h for op in self.ops]),
+                                         (ctypes.c_int * n)(*self.nrhs), flags, ctypes.byref(self._h)))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value and _lib is not None:
+            _lib.evr_sg4_multi_destroy(h)
+            self._h = None
+
+    def _dtype(self):
+        import torch
+        return torch.complex128 if self.complex_ else torch.float64
+
+    def hpsi(self, psis, outs, E0=None, Esc=None, stream: int = 0):
+        """outs[k] = (H_k psis[k] - E0[k] psis[k]) / Esc[k]; a None psi skips operator k."""
+        n = len(self.ops)
+        if len(psis) != n or len(outs) != n:
+            raise EVRError(1, f"hpsi: {len(psis)} psis and {len(outs)} outs for {n} operators")
+        act = [k for k in range(n) if psis[k] is not None]
+        rows = _check_blocks([self.ops[k] for k in act], [psis[k] for k in act], [outs[k] for k in act],
+                             self._dtype())
+        for k, r in zip(act, rows):
+            if r != self.nrhs[k]:
+                raise EVRError(1, f"operator {k}: {r} vectors, the plan has {self.nrhs[k]}")
+        VP, LL = ctypes.c_void_p * n, ctypes.c_longlong * n
+        pp = VP(*[psis[k].data_ptr() if psis[k] is not None else None for k in range(n)])
+        hp = VP(*[outs[k].data_ptr() if psis[k] is not None else None for k in range(n)])
+        ld = LL(*[op.basis.nvec for op in self.ops])
+        e0 = (ctypes.c_double * n)(*([0.0] * n if E0 is None else E0))
+        es = (ctypes.c_double * n)(*([1.0] * n if Esc is None else Esc))
+        check(lib().evr_sg4_multi_hpsi(self._h, pp, ld, hp, ld, e0, es, stream))
+        return outs
+
+    def last_launches(self) -> int:
+        v = ctypes.c_longlong()
+        check(lib().evr_sg4_multi_last_launches(self._h, ctypes.byref(v)))
+        return v.value
+
+    def cheby_propagate(self, psis, Hmin, Hmax, dt: float, npoly: int, nsteps: int, stream: int = 0):
+        """Fixed-order Chebyshev propagation of every operator's complex packets
+        in lock-step; returns the autocorrelations [(nsteps+1) x nrhs_k] per operator."""
+        import torch
+        if not self.complex_:
+            raise EVRError(1, "cheby_propagate needs a complex plan")
+        n = len(self.ops)
+        rows = _check_blocks(self.ops, psis, psis, torch.complex128)
+        if rows != self.nrhs:
+            raise EVRError(1, "psis do not match the plan's nrhs")
+        opts = (ChebyOpts * n)(*[ChebyOpts(float(Hmin[k]), float(Hmax[k]), dt, npoly, nsteps, 0.0, 0)
+                                 for k in range(n)])
+        ac = [np.zeros((nsteps + 1, r), dtype=np.complex128) for r in rows]
+        used = ctypes.c_int()
+        VP = ctypes.c_void_p * n
+        check(lib().evr_sg4_multi_cheby_propagate(self._h, opts, VP(*[P.data_ptr() for P in psis]),
+                                                  VP(*[a.ctypes.data for a in ac]), ctypes.byref(used), stream))
+        return ac
+
+
+def hpsi_multi(ops, psis, outs, E0=None, Esc=None, transpose: bool = False, stream: int = 0):
+    """One-shot H_k psi_k for several independent operators in one persistent
+    launch (evr_sg4_hpsi_multi); all psis float64 or all complex128."""
+    import torch
+    n = len(ops)
+    dtype = psis[0].dtype if n else None
+    if dtype not in (torch.float64, torch.complex128):
+        raise EVRError(1, "hpsi_multi: psis must be float64 or complex128 CUDA tensors")
+    nrhs = _check_blocks(ops, psis, outs, dtype)
+    VP, LL = ctypes.c_void_p * n, ctypes.c_longlong * n
+    ld = LL(*[op.basis.nvec for op in ops])
+    e0 = (ctypes.c_double * n)(*([0.0] * n if E0 is None else E0))
+    es = (ctypes.c_double * n)(*([1.0] * n if Esc is None else Esc))
+    flags = (1 if transpose else 0) | (2 if dtype == torch.complex128 else 0)
+    check(lib().evr_sg4_hpsi_multi(n, VP(*[op._h for op in ops]), (ctypes.c_int * n)(*nrhs),
+                                   VP(*[P.data_ptr() for P in psis]), ld, VP(*[O.data_ptr() for O in outs]), ld,
+                                   e0, es, flags, stream))
+    return outs
 
 
 def fp64_peak_tflops() -> float:

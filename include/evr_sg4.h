@@ -58,7 +58,9 @@ typedef struct {
   int D;                    /* number of modes */
   int L;                    /* Smolyak grid level (L_SparseGrid) */
   int LB;                   /* basis level (L_SparseBasis) */
-  int nb0;                  /* channels (only 1 is supported) */
+  int nb0;                  /* channels (electronic states, nb_be), 1..8: a vector is nb0
+                               blocks of N (RvecB((ie-1)*Max_nDI + iB)); nb0 > 1 takes
+                               operator types 0 and 1 with V as a grid */
   const int* nb_of_l;       /* [D*(L+1)] */
   const int* nq_of_l;       /* [D*(L+1)] */
   const double* x;          /* sum over (i,l) of nq */
@@ -90,6 +92,10 @@ int evr_sg4_desc_sizes(const evr_sg4_desc* d, long long* out);
  * ---------------------------------------------------------------------- */
 int evr_sg4_basis_build_ho(int D, int L, int LB, int A_nb, int B_nb, int A_nq, int B_nq,
                            const double* Q0, const double* scaleQ, evr_sg4_basis** out);
+/* The same with one rule per mode (arrays of D): the reference reads
+ * L_TO_nq_A/B (and L_TO_nb) per primitive basis (&basis_nD). */
+int evr_sg4_basis_build_ho_modes(int D, int L, int LB, const int* A_nb, const int* B_nb, const int* A_nq,
+                                 const int* B_nq, const double* Q0, const double* scaleQ, evr_sg4_basis** out);
 /* Fills *d with pointers into the basis' own storage (valid until free). */
 int evr_sg4_basis_desc(const evr_sg4_basis* b, evr_sg4_desc* d);
 /* Coordinates of every term grid point: Q[sum_nq*D], point-major
@@ -112,7 +118,10 @@ int evr_sg4_destroy(evr_sg4_ctx* c);
  *   type 10 : y = -1/2 sum_i d_i(Jac sum_j G_ji d_j(s x)) / (Jac s) + V.x,
  *             s = sqRhoOVERJac                                  (CASE 10 :1546)
  * V is a grid (sum_nq values, OpGrid%Grid layout, terms concatenated) or a
- * polynomial sum_t coef_t prod_i Q_i^expo_ti evaluated on the device.
+ * polynomial sum_t coef_t prod_i Q_i^expo_ti evaluated on the device.  With
+ * nb0 > 1 channels V is the electronic matrix on the grid:
+ * V_grid[(a*nb0 + b)*sum_nq + point] couples channel b into channel a
+ * (OpGrid(iterm)%Grid(:,a,b)), and the derivative terms act on every channel.
  * G (type 10) is a grid GGiq(iq,j,i) per term, concatenated (sum_nq*D*D),
  * or the affine form G_ij(Q) = G0_ij + sum_k G1_ijk Q_k ([D*D], [D*D*D],
  * row-major ijk); neither = identity.  Jac / sqRho grids: NULL = 1.
@@ -140,6 +149,7 @@ int evr_sg4_set_operator(evr_sg4_ctx* c, const evr_sg4_op_desc* op);
 /* ------------------------------------------------------------------------
  * H.psi on device pointers (batched persistent kernel, the fast path):
  *   hpsi(:,r) = (H psi(:,r) - E0 psi(:,r)) / Esc,  r = 1..nrhs
+ * A column holds the nb0 channel blocks of N (ld >= nb0*N).
  * E0 = 0, Esc = 1 is sub_TabOpPsi; other values are sub_scaledOpPsi
  * (sub_OpPsi.f90:2821-2864).  psi and hpsi must not overlap.
  * ---------------------------------------------------------------------- */
@@ -196,7 +206,35 @@ int evr_sg4_hpsi_host(evr_sg4_ctx* c, int nrhs, const double* psi, long long ldp
 int evr_sg4_hpsi_noalloc(evr_sg4_ctx* c, int nrhs, const double* psi, long long ldpsi, double* hpsi,
                          long long ldh, double E0, double Esc, void* stream);
 
-/* Sizes of a context: out[0..7] as evr_sg4_desc_sizes. */
+/* Device budget (bytes) for the operator fields of a context, applied by the
+ * next evr_sg4_set_operator.  When fields given in analytic form (V as a
+ * polynomial, G0/G1 affine) would exceed it, only their coefficients stay on
+ * the device and every H.psi evaluates them per slice of consecutive Smolyak
+ * terms (as much as fits the budget) just before that slice's work items run,
+ * as the reference builds them term by term inside its term loop when they
+ * are not kept in memory (get_OpGrid_type10_OF_ONEDP_FOR_SG4,
+ * SRC/sub_Operator/sub_OpPsi_SG4.f90:2536, called at :1553).  The per-term
+ * contributions and their ordered accumulation are unchanged, so results are
+ * bit-identical to resident fields.  Grids passed as arrays are always
+ * resident.  0 (the default): resident.  evr_sg4_hpsi/_cplx/_apply (not
+ * _plain) and everything built on them accept streamed contexts; the
+ * per-term path, the multi-context plans and evr_sg4_hpsi_noalloc return
+ * EVR_ERR_STATE. */
+int evr_sg4_set_field_budget(evr_sg4_ctx* c, long long bytes);
+/* Number of field slices of the current operator (0: resident fields). */
+int evr_sg4_field_slices(const evr_sg4_ctx* c, long long* nslices);
+
+/* Autotuner (the counterpart of Tune_SG4threads_HPsi, SRC/sub_main/vib.f90:2013,
+ * which times H.psi for each OpenMP thread count): times H.psi on nrhs
+ * vectors (flags: EVR_APPLY_COMPLEX or 0) for each cap on the right-hand
+ * sides one work item carries (1, 2, 4, ..., 32; larger blocks reuse the 1-D
+ * matrices and fields more, smaller ones balance better) and keeps the
+ * fastest for this context.  best_rmax/best_ms may be NULL.  Results do not
+ * depend on the cap. */
+int evr_sg4_tune(evr_sg4_ctx* c, int nrhs, int flags, int* best_rmax, double* best_ms);
+
+/* Sizes of a context: out[0..7] as evr_sg4_desc_sizes, except out[0] = the
+ * length of a vector, nb0 * N. */
 int evr_sg4_ctx_sizes(const evr_sg4_ctx* c, long long* out);
 
 /* ------------------------------------------------------------------------
@@ -245,9 +283,49 @@ typedef struct {
   int npoly;           /* expansion order */
   int nsteps;          /* number of steps */
   double poly_tol;     /* convergence of the expansion, <= 0: fixed order */
+  int no_graph;        /* fixed order: 0 replays each step as a CUDA graph recorded
+                          once (no host work between launches); 1 launches eagerly */
 } evr_cheby_opts;
 int evr_sg4_cheby_propagate(evr_sg4_ctx* c, const evr_cheby_opts* o, int nrhs, double* psi, const double* psi0,
                             double* autocorr, int* npoly_used, void* stream);
+
+/* Several independent Hamiltonians (contexts of any D, L and operator type)
+ * applied in ONE persistent launch: the (context, term, rhs block) items of
+ * all of them are merged into one cost-sorted work list, followed by each
+ * context's ordered accumulation (1 + 2n launches).  No counterpart in the
+ * reference, which applies one para_Op per sub_TabOpPsi call
+ * (SRC/sub_Operator/sub_OpPsi.f90:705); this batches its independent
+ * Hamiltonians (the uneven-instance workload) on one GPU.
+ *
+ * evr_sg4_multi_create fixes the contexts, nrhs[k] per context and the flags
+ * (EVR_APPLY_COMPLEX, EVR_APPLY_TRANSPOSE); the plan owns the per-call
+ * scratch, so the contexts stay usable on their own.  Calling
+ * evr_sg4_set_operator with another operator type on a context invalidates
+ * the plan (evr_sg4_multi_hpsi returns EVR_ERR_STATE).
+ * evr_sg4_multi_hpsi: per context k, psi[k] (ld ldpsi[k], device) ->
+ * hpsi[k] (ld ldh[k]), scaled by E0[k], Esc[k] (NULL arrays: 0 and 1);
+ * psi[k] == NULL skips context k in this call.  A plan is used from one
+ * stream at a time. */
+typedef struct evr_sg4_multi evr_sg4_multi;
+int evr_sg4_multi_create(int n, evr_sg4_ctx* const* ctxs, const int* nrhs, int flags, evr_sg4_multi** out);
+int evr_sg4_multi_hpsi(evr_sg4_multi* m, const double* const* psi, const long long* ldpsi, double* const* hpsi,
+                       const long long* ldh, const double* E0, const double* Esc, void* stream);
+int evr_sg4_multi_last_launches(const evr_sg4_multi* m, long long* n);
+int evr_sg4_multi_destroy(evr_sg4_multi* m);
+/* Chebyshev propagation (evr_sg4_cheby_propagate's fixed-order form) of the
+ * packets of every context of a plan created with EVR_APPLY_COMPLEX, in
+ * lock-step: each expansion order is ONE evr_sg4_multi_hpsi over all
+ * contexts.  o[k]: options of context k (own Hmin, Hmax; dt, npoly, nsteps
+ * equal for all, poly_tol <= 0).  A context whose step diverges redoes it
+ * with Hmax raised by (Hmax-Hmin)/10, up to 10 times.  psi[k]: device
+ * interleaved complex128 N_k x nrhs_k, propagated in place; autocorr[k]: host
+ * complex [(nsteps+1) x nrhs_k] = <psi_k(0) | psi_k(t_j)>, or NULL. */
+int evr_sg4_multi_cheby_propagate(evr_sg4_multi* m, const evr_cheby_opts* o, double* const* psi,
+                                  double* const* autocorr, int* npoly_used, void* stream);
+/* One-shot form: create, apply, synchronize the stream, destroy. */
+int evr_sg4_hpsi_multi(int n, evr_sg4_ctx* const* ctxs, const int* nrhs, const double* const* psi,
+                       const long long* ldpsi, double* const* hpsi, const long long* ldh, const double* E0,
+                       const double* Esc, int flags, void* stream);
 
 /* Field-driven RK4 propagation of one complex packet (march_RK4_field,
  * SRC/sub_propagation/sub_module_propa_march.f90:397-548; fcn_field
@@ -277,7 +355,9 @@ int evr_sg4_oc_gradient(evr_sg4_ctx* H0, evr_sg4_ctx* mu, const evr_rk4_opts* o,
                         const double* psi0, const double* target, double* J, double* grad, void* stream);
 
 /* Algorithmic FP64 operation count of one H.psi per right-hand side for the
- * current operator (flop, counted from the term sizes). */
+ * current operator (flop, counted from the term sizes, with the basis<->grid
+ * passes in the mode order the kernels use, which never needs more
+ * multiply-adds than the reference's order 1..D). */
 int evr_sg4_flops_per_rhs(const evr_sg4_ctx* c, double* flops);
 
 /* Number of kernel launches the last hpsi call issued. */

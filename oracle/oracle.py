@@ -35,6 +35,8 @@ def lib():
         ip = ctypes.POINTER(ctypes.c_int)
         L.orc_create.restype = ctypes.c_void_p
         L.orc_create.argtypes = [ctypes.c_int] * 7 + [dp, dp]
+        L.orc_create_modes.restype = ctypes.c_void_p
+        L.orc_create_modes.argtypes = [ctypes.c_int] * 3 + [ip] * 4 + [dp, dp]
         L.orc_destroy.argtypes = [ctypes.c_void_p]
         L.orc_sizes.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]
         L.orc_tables.argtypes = [ctypes.c_void_p, ip, dp, ip, ip]
@@ -76,15 +78,19 @@ def gauss_hermite(nq: int):
 
 
 class OracleSG4:
-    """The oracle's SG4 basis + operator action (one HO basis per mode)."""
+    """The oracle's SG4 basis + operator action (one HO basis per mode).
+
+    A_nb, B_nb, A_nq, B_nq: one rule for every mode, or a sequence of D rules."""
 
     def __init__(self, D, L, LB=None, A_nb=1, B_nb=1, A_nq=2, B_nq=1, Q0=None, scaleQ=None):
         self.D, self.L = D, L
         self.LB = L if LB is None else LB
         self.Q0 = np.zeros(D) if Q0 is None else np.ascontiguousarray(Q0, dtype=np.float64)
         self.scaleQ = np.ones(D) if scaleQ is None else np.ascontiguousarray(scaleQ, dtype=np.float64)
-        self.A_nb, self.B_nb, self.A_nq, self.B_nq = A_nb, B_nb, A_nq, B_nq
-        self.h = lib().orc_create(D, L, self.LB, A_nb, B_nb, A_nq, B_nq, _dp(self.Q0), _dp(self.scaleQ))
+        rule = lambda v: np.ascontiguousarray(np.broadcast_to(np.asarray(v, dtype=np.int32), (D,)))
+        self.A_nb, self.B_nb, self.A_nq, self.B_nq = rule(A_nb), rule(B_nb), rule(A_nq), rule(B_nq)
+        self.h = lib().orc_create_modes(D, L, self.LB, _ip(self.A_nb), _ip(self.B_nb), _ip(self.A_nq),
+                                        _ip(self.B_nq), _dp(self.Q0), _dp(self.scaleQ))
         if not self.h:
             raise ValueError("orc_create failed")
         z = (ctypes.c_longlong * 8)()
@@ -104,11 +110,11 @@ class OracleSG4:
         lib().orc_tables(self.h, _ip(tab_l), _dp(w), _ip(m), _ip(p))
         return tab_l.reshape(self.nb_SG, self.D), w, m, p.reshape(self.N, self.D)
 
-    def nb_nq(self, l):
-        return self.A_nb + self.B_nb * l, self.A_nq + self.B_nq * l
+    def nb_nq(self, l, mode=0):
+        return (int(self.A_nb[mode] + self.B_nb[mode] * l), int(self.A_nq[mode] + self.B_nq[mode] * l))
 
     def basis1d(self, mode, l):
-        nb, nq = self.nb_nq(l)
+        nb, nq = self.nb_nq(l, mode)
         out = dict(x=np.zeros(nq), w=np.zeros(nq), d0=np.zeros(nq * nb), d1=np.zeros(nq * nb),
                    d2=np.zeros(nq * nb), bgw=np.zeros(nq * nb), d1gg=np.zeros(nq * nq), d2gg=np.zeros(nq * nq))
         lib().orc_basis1d(self.h, mode, l, *[_dp(out[k]) for k in ("x", "w", "d0", "d1", "d2", "bgw", "d1gg", "d2gg")])
@@ -153,7 +159,7 @@ def oracle_tables(O: "OracleSG4"):
     for i in range(D):
         for l in range(L + 1):
             b = O.basis1d(i, l)
-            nb, nq = O.nb_nq(l)
+            nb, nq = O.nb_nq(l, i)
             nb_of_l.append(nb)
             nq_of_l.append(nq)
             xs.append(b["x"])

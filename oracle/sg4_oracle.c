@@ -314,6 +314,19 @@ static long long enum_type5p(int D, const int* nDsize, const int* i_to_l, int ld
 /* ------------------------------------------------------------------------ */
 orc_sg4* orc_create(int D, int L, int LB, int A_nb, int B_nb, int A_nq, int B_nq,
                     const double* Q0, const double* scaleQ) {
+  if (D < 1 || D > ORC_MAXD) return NULL;
+  int a[ORC_MAXD], b[ORC_MAXD], c[ORC_MAXD], d[ORC_MAXD];
+  for (int i = 0; i < D; ++i) {
+    a[i] = A_nb;
+    b[i] = B_nb;
+    c[i] = A_nq;
+    d[i] = B_nq;
+  }
+  return orc_create_modes(D, L, LB, a, b, c, d, Q0, scaleQ);
+}
+
+orc_sg4* orc_create_modes(int D, int L, int LB, const int* A_nb, const int* B_nb, const int* A_nq,
+                          const int* B_nq, const double* Q0, const double* scaleQ) {
   if (D < 1 || D > ORC_MAXD || L < 0 || LB < 0) return NULL;
   orc_sg4* s = (orc_sg4*)calloc(1, sizeof(orc_sg4));
   s->D = D;
@@ -325,7 +338,7 @@ orc_sg4* orc_create(int D, int L, int LB, int A_nb, int B_nb, int A_nq, int B_nq
   s->b = (orc_basis1*)calloc((size_t)D * (L + 1), sizeof(orc_basis1));
   for (int m = 0; m < D; ++m)
     for (int l = 0; l <= L; ++l) {
-      int nb = lin_n(A_nb, B_nb, l), nq = lin_n(A_nq, B_nq, l);
+      int nb = lin_n(A_nb[m], B_nb[m], l), nq = lin_n(A_nq[m], B_nq[m], l);
       s->nb_of_l[m * (L + 1) + l] = nb;
       s->nq_of_l[m * (L + 1) + l] = nq;
       build_basis1(&s->b[m * (L + 1) + l], nb, nq, Q0 ? Q0[m] : 0.0, scaleQ ? scaleQ[m] : 1.0);
@@ -340,7 +353,7 @@ orc_sg4* orc_create(int D, int L, int LB, int A_nb, int B_nb, int A_nq, int B_nq
   s->i_to_l = (int*)malloc(sizeof(int) * D * s->nbmax_mode);
   for (int m = 0; m < D; ++m)
     for (int n = 1; n <= s->nbmax_mode; ++n)
-      s->i_to_l[m * s->nbmax_mode + n - 1] = l_of_n(A_nb, B_nb, n, L);
+      s->i_to_l[m * s->nbmax_mode + n - 1] = l_of_n(A_nb[m], B_nb[m], n, L);
   s->N = enum_type5p(D, nDsize, s->i_to_l, s->nbmax_mode, LB, &s->packed);
 
   /* Smolyak terms, nDindex type -5: l_i in [0..L], Lmin <= sum l <= L, first

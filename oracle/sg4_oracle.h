@@ -31,6 +31,10 @@ typedef struct orc_sg4 orc_sg4;
  * Restates RecSparseGrid_ForDP_type4 (SRC/sub_Basis/sub_quadra_SparseBasis.f90:922-1434). */
 orc_sg4* orc_create(int D, int L, int LB, int A_nb, int B_nb, int A_nq, int B_nq,
                     const double* Q0, const double* scaleQ);
+/* The same with one nb/nq rule per mode (arrays of D), as the reference reads
+ * L_TO_nq_A/B per primitive basis (&basis_nD). */
+orc_sg4* orc_create_modes(int D, int L, int LB, const int* A_nb, const int* B_nb, const int* A_nq,
+                          const int* B_nq, const double* Q0, const double* scaleQ);
 void orc_destroy(orc_sg4* s);
 
 /* sizes[0..7] = N (packed size), nb_SG, sum_nb, sum_nq, max_nb_term, max_nq_term, D, L */

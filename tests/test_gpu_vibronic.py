@@ -1,0 +1,142 @@
+"""Several channels (electronic states, nb0 > 1) through the GPU path.
+
+A vector holds nb0 blocks of the packed basis (RvecB((ie-1)*Max_nDI + iB));
+the operator's V is an nb0 x nb0 matrix on the grid and the derivative terms
+act on every channel.  The oracle builds the same H block by block (T + V_aa
+on the diagonal, V_ab off it, each applied per Smolyak term), which is how the
+CPU test pins it to the reference's 2-state pyrazine autocorrelation; here the
+GPU operator must match that H to 1e-12 and its Chebyshev propagation must
+reproduce the reference's autocorrelation to the reference's 1e-8.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from elvibrot_gb300 import EVRError, ParamOp, SG4Basis
+from oracle.oracle import OracleSG4
+
+from test_oracle_golden import pyrazine_model, pyrazine_oracle
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def need_cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def oracle_blocks(O, Vm, F2, type_op):
+    """Dense nb0 N x nb0 N H from the oracle, one block per channel pair."""
+    nb0 = Vm.shape[0]
+    I = np.eye(O.N)
+    rows = []
+    for a in range(nb0):
+        row = []
+        for b in range(nb0):
+            if a == b and type_op == 1:
+                row.append(O.hpsi(I, type_op=1, V=Vm[a, a], F2=F2.ravel()))
+            else:
+                row.append(O.hpsi(I, type_op=0, V=Vm[a, b]))
+        rows.append(row)
+    return np.block(rows)
+
+
+def gpu_dense(op, n, cplx=False, transpose=False):
+    E = torch.eye(n, dtype=torch.complex128 if cplx else torch.float64, device="cuda")
+    if cplx:
+        E = E * (0.6 + 0.8j)
+    out = torch.empty_like(E)
+    op.hpsi_dev(E.contiguous(), out, transpose=transpose)
+    torch.cuda.synchronize()
+    H = out.cpu().numpy().T
+    return H / (0.6 + 0.8j) if cplx else H
+
+
+def pyrazine_gpu(g):
+    A, B = g["L_TO_nq_A"], g["L_TO_nq_B"]
+    basis = SG4Basis(g["D"], g["L"], g["LB"], A_nb=A, B_nb=B, A_nq=A, B_nq=B, nb0=2)
+    O = pyrazine_oracle(g)
+    V11, V22, V12, F2 = pyrazine_model(g, O)
+    Vm = np.array([[V11, V12], [V12, V22]])
+    return basis, O, Vm, F2
+
+
+def test_pyrazine_operator_matches_oracle_blocks():
+    need_cuda()
+    g = json.load(open(os.path.join(GOLD, "pyrazine12d.json")))
+    basis, O, Vm, F2 = pyrazine_gpu(g)
+    assert basis.N == O.N and basis.nvec == 2 * O.N
+    np.testing.assert_allclose(basis.grid_points(), O.grid_points(), rtol=0, atol=1e-14)
+    op = ParamOp(basis, 1, V=Vm.reshape(4, -1), F2=F2)
+    Href = oracle_blocks(O, Vm, F2, 1)
+    scale = np.max(np.abs(Href))
+    for cplx, tr in ((False, False), (True, False), (False, True)):
+        H = gpu_dense(op, basis.nvec, cplx, tr)
+        ref = Href.T if tr else Href
+        err = np.max(np.abs(H - ref)) / scale
+        print(f"pyrazine nb0=2 cplx={cplx} transpose={tr}: {err:.2e}")
+        assert err <= 1e-12
+
+
+def test_pyrazine_chebyshev_autocorrelation_golden():
+    need_cuda()
+    g = json.load(open(os.path.join(GOLD, "pyrazine12d.json")))
+    basis, O, Vm, F2 = pyrazine_gpu(g)
+    op = ParamOp(basis, 1, V=Vm.reshape(4, -1), F2=F2)
+    w = np.linalg.eigvals(oracle_blocks(O, Vm, F2, 1)).real
+    ac = g["autocorr"]
+    t = np.array(ac["t_au"])
+    psi = torch.zeros((1, basis.nvec), dtype=torch.complex128, device="cuda")
+    psi[0, basis.N] = complex(*g["psi0"]["coef"])   # channel 2, all modes in their first function
+    margin = 0.05 * (w.max() - w.min())
+    got, used = op.cheby_propagate(psi, w.min() - margin, w.max() + margin, float(t[1] - t[0]), npoly=300,
+                                   nsteps=len(t) - 1, poly_tol=1e-16)
+    got = np.asarray(got)[:, 0]
+    err = max(np.max(np.abs(got.real - ac["re"])), np.max(np.abs(got.imag - ac["im"])))
+    print(f"GPU Chebyshev pyrazine autocorrelation: max error {err:.2e} (npoly used {used})")
+    assert err <= g["criterion"]
+
+
+def test_three_channels_random_coupling():
+    need_cuda()
+    D, L, nb0 = 4, 4, 3
+    basis = SG4Basis(D, L, L, 1, 1, 2, 1, nb0=nb0)
+    O = OracleSG4(D, L, L, 1, 1, 2, 1)
+    Q = O.grid_points()
+    rng = np.random.default_rng(31)
+    Vm = np.empty((nb0, nb0, len(Q)))
+    for a in range(nb0):
+        for b in range(nb0):
+            c = rng.normal(size=D + 1)
+            Vm[a, b] = c[0] + Q @ c[1:] + (0.5 * (Q * Q).sum(axis=1) if a == b else 0.0)
+    F2 = -0.5 * np.diag(rng.uniform(0.5, 1.5, size=D))
+    for type_op in (0, 1):
+        op = ParamOp(basis, type_op, V=Vm.reshape(nb0 * nb0, -1), F2=F2 if type_op == 1 else None)
+        Href = oracle_blocks(O, Vm, F2, type_op)
+        scale = np.max(np.abs(Href))
+        for cplx, tr in ((False, False), (True, True)):
+            H = gpu_dense(op, basis.nvec, cplx, tr)
+            ref = Href.T if tr else Href
+            assert np.max(np.abs(H - ref)) / scale <= 1e-12, (type_op, cplx, tr)
+        # a block of 5 vectors (odd, so the last work items hold one channel group)
+        P = torch.from_numpy(rng.normal(size=(5, basis.nvec))).cuda()
+        out = torch.empty_like(P)
+        op.hpsi_dev(P, out, E0=0.3, Esc=1.5)
+        want = (Href @ P.cpu().numpy().T - 0.3 * P.cpu().numpy().T) / 1.5
+        assert np.max(np.abs(out.cpu().numpy().T - want)) / np.max(np.abs(want)) <= 1e-12
+
+
+def test_channels_reject_type10_and_polynomial_v():
+    need_cuda()
+    from elvibrot_gb300 import Polynomial
+    basis = SG4Basis(3, 3, 3, 1, 1, 2, 1, nb0=2)
+    with pytest.raises(EVRError):
+        ParamOp(basis, 10, V=np.zeros(4 * basis.sum_nq))
+    with pytest.raises(EVRError):
+        ParamOp(basis, 1, V_poly=Polynomial(np.array([1.0]), np.zeros((1, 3), dtype=np.int32)),
+                F2=-0.5 * np.eye(3))

@@ -95,3 +95,55 @@ def test_type10_invariances():
         off += nq
     h2 = o.hpsi(psi, type_op=10, V=V, G=G)
     assert np.max(np.abs(h2 - h0)) <= 1e-14 * np.max(np.abs(h0))
+
+
+def pyrazine_model(g, O):
+    """The 2-state pyrazine model of Working_tests/MPI_tests/12D_propagation_S0
+    (sub_system_pyrazine.f: V11, V22, V12 on the oracle's grid points, in
+    hartree; calc_f2_f1Q.f90: Tdef2(i,i) = -1/2 omega_i)."""
+    ev = g["eV_to_hartree"]
+    w, k1, k2 = (np.array(g[k]) for k in ("omega_eV", "kappa1_eV", "kappa2_eV"))
+    Q = O.grid_points()
+    v0 = 0.5 * (Q * Q) @ w
+    V11 = (v0 - g["delta_eV"] + Q @ k1) * ev
+    V22 = (v0 + g["delta_eV"] + Q @ k2) * ev
+    V12 = g["lambda_eV"] * Q[:, 0] * ev
+    F2 = np.diag(-0.5 * w * ev)
+    return V11, V22, V12, F2
+
+
+def pyrazine_oracle(g):
+    A, B = g["L_TO_nq_A"], g["L_TO_nq_B"]
+    return OracleSG4(g["D"], g["L"], g["LB"], A_nb=A, B_nb=B, A_nq=A, B_nq=B)   # Hm: nb(l) = nq(l)
+
+
+def test_pyrazine_autocorrelation_golden():
+    """H of the nb0=2 vibronic system from the oracle: the electronic blocks
+    are T + V11, V12, V21 = V12, T + V22, each applied per Smolyak term as the
+    reference does with V(:,ie,je); exp(-iHt) psi0 then reproduces the
+    reference's 61-point autocorrelation to its own criterion (1e-8)."""
+    from scipy.linalg import expm
+    g = json.load(open(os.path.join(GOLD, "pyrazine12d.json")))
+    O = pyrazine_oracle(g)
+    assert O.N == 1 + sum(g["L_TO_nq_B"])      # ground state + one excited mode (LB = 1)
+    V11, V22, V12, F2 = pyrazine_model(g, O)
+    I = np.eye(O.N)
+    H11 = O.hpsi(I, type_op=1, V=V11, F2=F2.ravel())
+    H22 = O.hpsi(I, type_op=1, V=V22, F2=F2.ravel())
+    H12 = O.hpsi(I, type_op=0, V=V12)
+    H = np.block([[H11, H12], [H12, H22]])
+    psi0 = np.zeros(2 * O.N, dtype=complex)
+    assert g["psi0"]["nDval"] == [1] * 12 and g["psi0"]["i_e"] == 2
+    psi0[O.N + 0] = complex(*g["psi0"]["coef"])    # packed index 1 = all modes in their first function
+    ac = g["autocorr"]
+    t = np.array(ac["t_au"])
+    U1 = expm(-1j * H * (t[1] - t[0]))
+    psi = psi0.copy()
+    got = []
+    for k in range(len(t)):
+        got.append(np.vdot(psi0, psi))
+        psi = U1 @ psi
+    got = np.array(got)
+    err = max(np.max(np.abs(got.real - ac["re"])), np.max(np.abs(got.imag - ac["im"])))
+    print(f"pyrazine 12-D L=1 autocorrelation: max error {err:.2e} over {len(t)} times")
+    assert err <= g["criterion"]
