@@ -193,6 +193,217 @@ def bench_oc_gradient():
             "J": J, "E0": E0, "Hmax_estimate": Hmax, "norm_after_forward": float(torch.linalg.vector_norm(P).item())}
 
 
+def coherent_packets(D, L, scaleQ, nrhs, shift=1.0):
+    """(nrhs, N) complex packets: coherent states of mode 1 displaced by `shift`
+    along Q1 (momentum 0.25 j in the dimensionless units of packet j), the other
+    modes in their ground state, in the packed basis (sum n_i <= L, last index
+    fastest, so (n, 0, ..., 0) sits after every tuple whose first index is < n)."""
+    from math import comb, factorial
+    N = comb(L + D, D)
+    pos = [0]
+    for m in range(L):
+        pos.append(pos[-1] + comb(L - m + D - 1, D - 1))
+    out = np.zeros((nrhs, N), dtype=np.complex128)
+    for j in range(nrhs):
+        a = scaleQ[0] * shift * (1.0 + 0.25j * j) / np.sqrt(2.0)
+        c = np.array([a ** n / np.sqrt(float(factorial(n))) for n in range(L + 1)])
+        out[j, pos] = c / np.linalg.norm(c)
+    return out
+
+
+def bench_uneven(seconds_cap=90.0):
+    """Uneven-instance batching: 64 seeded Hamiltonians (D in 3..9, L in 4..10,
+    type 1), 8 complex packets each.  Times one merged H.psi over all of them
+    (evr_sg4_multi_hpsi) against one evr_sg4_hpsi_cplx launch per instance,
+    and one order-30 Chebyshev step of dt = 10 a.u. in lock-step."""
+    import torch
+    from elvibrot_gb300 import MultiOp
+    from elvibrot_gb300.configs import uneven_instances
+    t0 = time.perf_counter()
+    models = uneven_instances(64)
+    ops = [m.operator() for m in models]
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    n = len(ops)
+    nrhs = 8
+    flops = sum(op.flops_per_rhs for op in ops) * 2 * nrhs
+    # spectral bounds by power iteration on H and on Hmax - H (one real vector per instance)
+    p1 = MultiOp(ops, [1] * n)
+    g = torch.Generator(device="cpu").manual_seed(5)
+    v = [torch.randn((1, op.basis.N), generator=g, dtype=torch.float64).cuda() for op in ops]
+    hv = [torch.empty_like(x) for x in v]
+    top = np.zeros(n)
+    for _ in range(40):
+        v = [x / torch.linalg.vector_norm(x) for x in v]
+        p1.hpsi(v, hv)
+        top = np.array([float((a * b).sum()) for a, b in zip(v, hv)])
+        v, hv = hv, v
+    Hmax = top * 1.1
+    v = [torch.randn((1, op.basis.N), generator=g, dtype=torch.float64).cuda() for op in ops]
+    low = np.zeros(n)
+    for _ in range(40):                                  # (H - E0) psi / Esc with Esc = -1: (Hmax - H) psi
+        v = [x / torch.linalg.vector_norm(x) for x in v]
+        p1.hpsi(v, hv, E0=list(Hmax), Esc=[-1.0] * n)
+        low = Hmax - np.array([float((a * b).sum()) for a, b in zip(v, hv)])
+        v, hv = hv, v
+    Hmin = low - 0.1 * (Hmax - low)
+    psis = [torch.from_numpy(coherent_packets(m.D, m.L, m.scaleQ, nrhs)).cuda() for m in models]
+    outs = [torch.empty_like(P) for P in psis]
+    plan = MultiOp(ops, [nrhs] * n, complex_=True)
+    plan.hpsi(psis, outs)                                # warm
+    torch.cuda.synchronize()
+    reps = 3
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(reps):
+        plan.hpsi(psis, outs)
+    b.record()
+    torch.cuda.synchronize()
+    multi_s = a.elapsed_time(b) / 1e3 / reps
+    ref = [torch.empty_like(P) for P in psis]
+    for op, P, O in zip(ops, psis, ref):                  # warm the per-instance work lists
+        op.hpsi_dev(P, O)
+    torch.cuda.synchronize()
+    a.record()
+    for op, P, O in zip(ops, psis, ref):
+        op.hpsi_dev(P, O)
+    b.record()
+    torch.cuda.synchronize()
+    seq_s = a.elapsed_time(b) / 1e3
+    same = all(torch.equal(x, y) for x, y in zip(outs, ref))
+    res = {"workload": "64 uneven type-1 instances (D 3..9, L 4..10, sum N %d), 8 complex packets each"
+                       % sum(op.basis.N for op in ops),
+           "setup_s": setup_s, "flops_per_multi_hpsi": flops,
+           "multi_hpsi_s": multi_s, "per_instance_launches_s": seq_s, "multi_over_per_instance": seq_s / multi_s,
+           "multi_tflops": flops / multi_s / 1e12, "bitwise_equal_to_per_instance": bool(same)}
+    if 29 * multi_s < seconds_cap:
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        ac = plan.cheby_propagate(psis, list(Hmin), list(Hmax), 10.0, 30, 1)
+        torch.cuda.synchronize()
+        step_s = time.perf_counter() - t1
+        norms = [float(torch.linalg.vector_norm(P, dim=1).sub(1.0).abs().max()) for P in psis]
+        res.update({"cheby_order": 30, "cheby_dt": 10.0, "cheby_step_s": step_s,
+                    "cheby_200_steps_s_estimate": 200 * step_s, "max_norm_drift": max(norms),
+                    "autocorr_t10_first": [float(ac[0][1, 0].real), float(ac[0][1, 0].imag)]})
+    return res
+
+
+def bench_cheby_graph(nsteps=200):
+    """Fixed-order Chebyshev (order 30, dt = 10 a.u.) of one complex packet on the
+    4-D L=7 type-1 system: every step eagerly launched vs replayed from a CUDA
+    graph recorded once (the launch-bound regime of small operators)."""
+    import torch
+    from elvibrot_gb300.configs import config
+    m = config(3)["model"]
+    op = m.operator()
+    N = op.basis.N
+    v = torch.randn((1, N), dtype=torch.float64, device="cuda")
+    hv = torch.empty_like(v)
+    top = 1.0
+    for _ in range(60):
+        v /= torch.linalg.vector_norm(v)
+        op.hpsi_dev(v, hv)
+        top = float((v * hv).sum().item())
+        v, hv = hv, v
+    Hmin, Hmax = 0.0, 1.1 * top
+    g = torch.Generator(device="cpu").manual_seed(3)
+    P0 = torch.randn((1, N), generator=g, dtype=torch.complex128).cuda()
+    P0 /= torch.linalg.vector_norm(P0)
+    res = {"workload": f"4-D SG4 L=7 type 1, 1 complex packet, order 30, dt 10 a.u., {nsteps} steps"}
+    out = {}
+    for graph in (False, True):
+        P = P0.clone()
+        op.cheby_propagate(P, Hmin, Hmax, 10.0, npoly=30, nsteps=3, graph=graph)   # warm
+        P = P0.clone()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        op.cheby_propagate(P, Hmin, Hmax, 10.0, npoly=30, nsteps=nsteps, graph=graph)
+        torch.cuda.synchronize()
+        res["graph_s" if graph else "eager_s"] = time.perf_counter() - t0
+        out[graph] = P
+    res["eager_over_graph"] = res["eager_s"] / res["graph_s"]
+    res["bit_identical"] = bool(torch.equal(out[False], out[True]))
+    return res
+
+
+def _terms_array(D, L):
+    """Smolyak terms l (|l| in [max(0, L-D+1), L]) as an int array, and their grid sizes prod(l+2)."""
+    Lmin = max(0, L - D + 1)
+    rows = []
+
+    def rec(prefix, rem):
+        if len(prefix) == D - 1:
+            for v in range(rem + 1):
+                if L - rem + v >= Lmin:
+                    rows.append(prefix + (v,))
+            return
+        for v in range(rem + 1):
+            rec(prefix + (v,), rem - v)
+    rec((), L)
+    l = np.array(rows, dtype=np.int64)
+    return l, np.prod(l + 2, axis=1).astype(np.float64)
+
+
+def type10_flops_per_rhs(D, L):
+    """evr_sg4_flops_per_rhs for a type-10 operator with V and G (nb = l+1, nq = l+2): the
+    basis<->grid passes in the kernel's mode order (larger l first, ties by index) plus the grid work."""
+    l, q = _terms_array(D, L)
+    nb, nq = (l + 1).astype(np.float64), (l + 2).astype(np.float64)
+    order = np.argsort(-l, axis=1, kind="stable")
+    f = np.zeros(len(l))
+    rows = np.arange(len(l))
+    for direction in (0, 1):
+        cur = (nb if direction == 0 else nq).copy()
+        seq = range(D) if direction == 0 else range(D - 1, -1, -1)
+        for k in seq:
+            i = order[:, k]
+            rest = np.prod(cur, axis=1) / cur[rows, i]
+            f += 2.0 * nb[rows, i] * nq[rows, i] * rest
+            cur[rows, i] = (nq if direction == 0 else nb)[rows, i]
+    f += 4.0 * q * nq.sum(axis=1) + 2.0 * D * D * q + q + 4.0 * q + 2.0 * np.prod(nb, axis=1)
+    return float(f.sum())
+
+
+def bench_streamed_12d(L=6, nrhs=32, budget_gib=64):
+    """The 12-D workload shape (type 10 with Q-dependent G, 32 complex packets)
+    at Smolyak level L: its V and G (sum_nq x 145 doubles) exceed the device,
+    so they are evaluated per slice of Smolyak terms inside every H.psi.
+    Times one H.psi and extrapolates to L=10 by the flop count."""
+    import torch
+    from elvibrot_gb300.configs import SEED0, make_model
+    m = make_model(12, L, 10, SEED0 + 4)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    op = m.operator(field_budget=budget_gib << 30)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    N, snq = op.basis.N, op.basis.sum_nq
+    g = torch.Generator(device="cpu").manual_seed(4)
+    P = (torch.randn((nrhs, N), generator=g, dtype=torch.float64)
+         + 1j * torch.randn((nrhs, N), generator=g, dtype=torch.float64)).cuda()
+    P /= torch.linalg.vector_norm(P, dim=1, keepdim=True)
+    O = torch.empty_like(P)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    op.hpsi_dev(P, O)
+    b.record()
+    torch.cuda.synchronize()
+    t = a.elapsed_time(b) / 1e3
+    flops = op.flops_per_rhs * 2 * nrhs
+    D = 12
+    vmul = sum(int(np.sum(e)) for e in m.V.expo)
+    field_flops = snq * (2.0 * D ** 3 + vmul + len(m.V.coef))               # affine G, V polynomial
+    fL, f10 = type10_flops_per_rhs(D, L), type10_flops_per_rhs(D, 10)
+    return {"workload": f"12-D SG4 L={L} type 10, Q-dependent G, {nrhs} complex packets, fields streamed",
+            "N": N, "sum_nq": snq, "field_bytes_resident": snq * 8 * (1 + D * D), "field_budget": budget_gib << 30,
+            "slices": op.field_slices, "setup_s": setup_s, "hpsi_s": t, "hpsi_flops": flops,
+            "flops_per_rhs_check": [op.flops_per_rhs, fL],
+            "field_eval_flops": field_flops, "tflops_hpsi_only": flops / t / 1e12,
+            "tflops_with_fields": (flops + field_flops) / t / 1e12,
+            "L10_hpsi_s_estimate": t * f10 / fL, "L10_sum_nq": float(_terms_array(D, 10)[1].sum())}
+
+
 def run_ours(args, ws, rank, local):
     import torch
     import torch.distributed as dist
@@ -277,8 +488,17 @@ def run_ours(args, ws, rank, local):
     # callers of the path: Davidson on the same operator, OC gradient on the 4-D L=7 system
     extras = {}
     if not args.no_extras:
-        extras["davidson"] = bench_davidson(op)
-        extras["oc_gradient"] = bench_oc_gradient()
+        want = set(args.extras.split(","))
+        if "davidson" in want:
+            extras["davidson"] = bench_davidson(op)
+        if "oc" in want:
+            extras["oc_gradient"] = bench_oc_gradient()
+        if "uneven" in want:
+            extras["uneven_instances"] = bench_uneven()
+        if "graph" in want:
+            extras["cheby_graph"] = bench_cheby_graph()
+        if "stream12" in want:
+            extras["streamed_12d"] = bench_streamed_12d()
 
     flops = op.flops_per_rhs * nrhs
     achieved = flops / (ms_step / 1e3) / 1e12
@@ -313,7 +533,7 @@ def run_ours(args, ws, rank, local):
                                  "frac": alg_bytes / (ms_step / 1e3) / 1e9 / hbm_peak,
                                  "alg_bytes_per_launch": alg_bytes}},
             "plain": {"value": plain_value, "unit": UNIT, "steps": plain_steps,
-                      "launches_per_step": 1 + b.nb_SG, "batched_over_plain": value / ws / plain_value},
+                      "launches_per_step": 2 + b.nb_SG, "batched_over_plain": value / ws / plain_value},
             "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cpu_threads, "kind": "port",
                              "sample": f"{cpu_steps} full 20-RHS H.psi of the same workload in {cpu_dt:.2f} s "
                                        f"(C/OpenMP restatement, OpenMP static over Smolyak terms)"},
@@ -358,7 +578,10 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--no-extras", action="store_true", help="skip the Davidson and OC-gradient timings")
+    ap.add_argument("--no-extras", action="store_true", help="skip the timings of the callers")
+    ap.add_argument("--extras", default="davidson,oc,uneven,graph,stream12",
+                    help="callers to time: davidson, oc (optimal-control gradient), uneven (64-instance batching), "
+                         "graph (Chebyshev steps replayed from a CUDA graph), stream12 (12-D type 10, streamed fields)")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if ws > 1:
