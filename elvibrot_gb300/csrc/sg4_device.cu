@@ -15,10 +15,11 @@
 // result to a contribution buffer that two small kernels then sum per packed
 // function in Smolyak-term order (compensated, deterministic, no atomics).
 // GB300's FP64 pipe (~1.2 TFLOP/s measured) is the binding resource, so the
-// kernel is organised to keep it busy: four CTAs per SM so some compute while
-// the others gather or synchronise, right-hand sides batched per item so the
-// 1-D matrices and the operator fields are loaded once per point, and no
-// FP64 work spent on anything but the algorithm's own multiply-adds.
+// kernel is organised to keep it busy: several CTAs per SM (four, or eight
+// for D <= 6) so some compute while the others gather or synchronise,
+// right-hand sides batched per item so the 1-D matrices and the operator
+// fields are loaded once per point, and no FP64 work spent on anything but
+// the algorithm's own multiply-adds.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -92,15 +93,28 @@ int desc_sizes(const evr_sg4_desc* d, DescSizes* z) {
 #ifndef EVR_FUSED_MAXD
 #define EVR_FUSED_MAXD 12  // type-10 items with D <= 12 use the fused grid passes
 #endif
-// persistent H.psi launch: threads per CTA and resident CTAs per SM.  Four
-// 128-thread CTAs (55 KB of shared memory each, 128 registers a thread) beat
-// two 256-thread ones by 0.7 % on the 6-D benchmark and let the ~600 items of
-// a small operator run in one wave.
+// Persistent H.psi launch geometry, chosen per work plan.  Wide: four
+// 128-thread CTAs per SM (55 KB of shared memory and 128 registers a thread
+// each), fused type-10 passes up to D = 12; it beat two 256-thread CTAs by
+// 0.7 % on the 6-D benchmark and lets the ~600 items of a small operator run
+// in one wave.  Narrow, for D <= 6 and plans of at least EVR_NARROW_WAVES
+// waves of items: EVR_NARROW_CTAS CTAs per SM (less shared memory and fewer
+// registers each, the fused passes instantiated only up to D = 6): more
+// resident warps keep the FP64 pipe busier on large operators (+5 % on the
+// 6-D benchmark), while a small operator's one wave of items finishes sooner
+// with the wide kernel's longer register budget.
 #ifndef EVR_CTA_THREADS
 #define EVR_CTA_THREADS 128
 #endif
-#ifndef EVR_CTAS_PER_SM
-#define EVR_CTAS_PER_SM 4
+#define EVR_WIDE_CTAS 4
+#define EVR_WIDE_FMAX 12
+#ifndef EVR_NARROW_CTAS
+#define EVR_NARROW_CTAS 8
+#endif
+#define EVR_NARROW_FMAX 6
+#define EVR_NARROW_WAVES 4
+#ifndef EVR_NARROW_INC
+#define EVR_NARROW_INC 0  // the narrow kernel takes the point digits from divisions
 #endif
 
 struct TermInfo {
@@ -329,7 +343,61 @@ __device__ double* transform(const KParams& p, const ItemShared& it, bool to_gri
 // (DerivOp_TO_RDP_OF_SmolaykRep); the same products, with two barriers
 // instead of 2D+2 and no phi arrays.  For H^T the matrices are transposed
 // and c (= -1/2/(Jac s)) and s trade places (done by the caller).
+// Position of element e = j*nqt + q of an item (q's digits along the modes,
+// mode 1 fastest, and the right-hand side j), advanced by a fixed stride with
+// mixed-radix carries so the loops over the grid do no integer division.
 template <int DD>
+struct GridPos {
+  int dig[DD], sdig[DD];
+  int e, j, sj;
+  __device__ __forceinline__ void init(const int* nq, int nqt, int e0, int stride) {
+    e = e0;
+    j = e0 / nqt;
+    int q = e0 - j * nqt;
+    sj = stride / nqt;
+    int s = stride - sj * nqt;
+#pragma unroll
+    for (int i = 0; i < DD; ++i) {
+      dig[i] = q % nq[i];
+      q /= nq[i];
+      sdig[i] = s % nq[i];
+      s /= nq[i];
+    }
+  }
+  __device__ __forceinline__ void advance(const int* nq, int stride) {
+    e += stride;
+    int carry = 0;
+#pragma unroll
+    for (int i = 0; i < DD; ++i) {
+      const int d = dig[i] + sdig[i] + carry;  // <= 2 nq - 1
+      carry = d >= nq[i];
+      dig[i] = carry ? d - nq[i] : d;
+    }
+    j += sj + carry;
+  }
+};
+
+// The point's digits come from GridPos (INC, fewer instructions) or from
+// divisions of the element index (fewer registers: the narrow geometry's
+// 64-register budget spills less without the digit arrays).
+template <int DD, bool INC>
+__device__ __forceinline__ void point_digits(GridPos<DD>& gp, const int* nq, int nqt, int e, int* idx, int& q) {
+  if constexpr (INC) {
+    q = e - gp.j * nqt;
+#pragma unroll
+    for (int i = 0; i < DD; ++i) idx[i] = gp.dig[i];
+  } else {
+    q = e % nqt;
+    int rem = q;
+#pragma unroll
+    for (int i = 0; i < DD; ++i) {
+      idx[i] = rem % nq[i];
+      rem /= nq[i];
+    }
+  }
+}
+
+template <int DD, bool INC>
 __device__ void type10_fused(const KParams& p, const ItemShared& it, const double* x, double* O, double* U,
                              int NQR) {
   const int nqt = it.nq_t;
@@ -349,18 +417,13 @@ __device__ void type10_fused(const KParams& p, const ItemShared& it, const doubl
   const long long GD = (long long)DD * DD;
   const long long si = p.transpose ? nqt : (long long)nqt * DD;  // G offset step of the output index
   const long long sj = p.transpose ? (long long)nqt * DD : nqt;  // ... and of the input index
+  GridPos<DD> gp;
+  if constexpr (INC) gp.init(nq, nqt, threadIdx.x, blockDim.x);
   for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
-    const int q = e % nqt;
+    int idx[DD], q;
+    point_digits<DD, INC>(gp, nq, nqt, e, idx, q);
+    if constexpr (INC) gp.advance(nq, blockDim.x);
     const double* xr = x + (e - q);
-    int idx[DD];
-    {
-      int rem = q;
-#pragma unroll
-      for (int i = 0; i < DD; ++i) {
-        idx[i] = rem % nq[i];
-        rem /= nq[i];
-      }
-    }
     double phi[DD];
 #pragma unroll
     for (int j = 0; j < DD; ++j) {
@@ -386,17 +449,11 @@ __device__ void type10_fused(const KParams& p, const ItemShared& it, const doubl
     }
   }
   __syncthreads();
+  if constexpr (INC) gp.init(nq, nqt, threadIdx.x, blockDim.x);
   for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
-    const int q = e % nqt;
-    int idx[DD];
-    {
-      int rem = q;
-#pragma unroll
-      for (int i = 0; i < DD; ++i) {
-        idx[i] = rem % nq[i];
-        rem /= nq[i];
-      }
-    }
+    int idx[DD], q;
+    point_digits<DD, INC>(gp, nq, nqt, e, idx, q);
+    if constexpr (INC) gp.advance(nq, blockDim.x);
     double acc[DD];
 #pragma unroll
     for (int i = 0; i < DD; ++i) {
@@ -416,12 +473,13 @@ __device__ void type10_fused(const KParams& p, const ItemShared& it, const doubl
   __syncthreads();
 }
 
+template <int FMAX>
 __device__ void type10_fused_dispatch(const KParams& p, const ItemShared& it, const double* x, double* O, double* U,
                                       int NQR) {
   switch (p.D) {
 #define EVR_T10(n)                                                        \
   case n:                                                                 \
-    if constexpr (n <= EVR_FUSED_MAXD) type10_fused<n>(p, it, x, O, U, NQR); \
+    if constexpr (n <= FMAX) type10_fused<n, (FMAX > EVR_NARROW_FMAX) || EVR_NARROW_INC>(p, it, x, O, U, NQR); \
     break;
     EVR_T10(1) EVR_T10(2) EVR_T10(3) EVR_T10(4) EVR_T10(5) EVR_T10(6) EVR_T10(7) EVR_T10(8) EVR_T10(9)
     EVR_T10(10) EVR_T10(11) EVR_T10(12)
@@ -446,6 +504,7 @@ __device__ void store_contrib(const KParams& p, const ItemShared& it, const doub
   __syncthreads();
 }
 
+template <int FMAX>
 __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int term, int rhs0) {
   if (threadIdx.x == 0) {
     const TermInfo& T = p.terms[term];
@@ -544,7 +603,7 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ter
       __syncthreads();
     }
     y = Y;
-  } else if (D <= EVR_FUSED_MAXD) {
+  } else if (D <= FMAX) {
     // CASE 10 through the fused grid passes; buffers: the transform pair
     // {X, T}, then U_1..U_D.  O (= the free transform buffer) starts as V.x.
     double* O = (x == X) ? T : X;
@@ -560,7 +619,7 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ter
       }
     }
     __syncthreads();
-    type10_fused_dispatch(p, it, x, O, U, NQR);
+    type10_fused_dispatch<FMAX>(p, it, x, O, U, NQR);
     double* yb = transform(p, it, false, O, x);
     store_contrib(p, it, yb);
     return;
@@ -626,7 +685,8 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ter
   store_contrib(p, it, yb);
 }
 
-__global__ void __launch_bounds__(EVR_CTA_THREADS, EVR_CTAS_PER_SM) hpsi_batched_kernel(KParams p) {
+template <int MINB, int FMAX>
+__global__ void __launch_bounds__(EVR_CTA_THREADS, MINB) hpsi_batched_kernel(KParams p) {
   extern __shared__ double smem[];
   __shared__ ItemShared it;
   __shared__ int next;
@@ -637,7 +697,7 @@ __global__ void __launch_bounds__(EVR_CTA_THREADS, EVR_CTAS_PER_SM) hpsi_batched
     __syncthreads();
     if (idx >= p.n_items) break;
     const Item itm = p.items[idx];
-    run_item(p, it, smem, itm.term, itm.rhs0);
+    run_item<FMAX>(p, it, smem, itm.term, itm.rhs0);
   }
 }
 
@@ -645,7 +705,8 @@ __global__ void __launch_bounds__(EVR_CTA_THREADS, EVR_CTAS_PER_SM) hpsi_batched
 // whose parameter block is copied to shared memory before the item runs.
 // With a counter the CTAs pull items until the list is empty; without one
 // (the per-term path) CTA b runs item item_base + b.
-__global__ void __launch_bounds__(EVR_CTA_THREADS, EVR_CTAS_PER_SM) hpsi_multi_kernel(const KParams* __restrict__ ps,
+template <int MINB, int FMAX>
+__global__ void __launch_bounds__(EVR_CTA_THREADS, MINB) hpsi_multi_kernel(const KParams* __restrict__ ps,
                                                               const MItem* __restrict__ items, int n_items,
                                                               int item_base, unsigned int* counter) {
   extern __shared__ double smem[];
@@ -665,8 +726,45 @@ __global__ void __launch_bounds__(EVR_CTA_THREADS, EVR_CTAS_PER_SM) hpsi_multi_k
       for (int w = threadIdx.x; w < (int)(sizeof(KParams) / sizeof(int)); w += blockDim.x) dst[w] = src[w];
     }
     __syncthreads();
-    run_item(sp, it, smem, m.term, m.rhs0);
+    run_item<FMAX>(sp, it, smem, m.term, m.rhs0);
   }
+}
+
+// the two geometries' kernels (geo 1: narrow, D <= EVR_NARROW_FMAX)
+static void launch_batched(int geo, unsigned grid, size_t smem, cudaStream_t s, const KParams& p) {
+  if (geo) hpsi_batched_kernel<EVR_NARROW_CTAS, EVR_NARROW_FMAX><<<grid, EVR_CTA_THREADS, smem, s>>>(p);
+  else hpsi_batched_kernel<EVR_WIDE_CTAS, EVR_WIDE_FMAX><<<grid, EVR_CTA_THREADS, smem, s>>>(p);
+}
+
+static void launch_multi(int geo, unsigned grid, size_t smem, cudaStream_t s, const KParams* ps, const MItem* items,
+                         int n_items, int item_base, unsigned int* counter) {
+  if (geo)
+    hpsi_multi_kernel<EVR_NARROW_CTAS, EVR_NARROW_FMAX><<<grid, EVR_CTA_THREADS, smem, s>>>(ps, items, n_items,
+                                                                                           item_base, counter);
+  else
+    hpsi_multi_kernel<EVR_WIDE_CTAS, EVR_WIDE_FMAX><<<grid, EVR_CTA_THREADS, smem, s>>>(ps, items, n_items, item_base,
+                                                                                       counter);
+}
+
+static int geo_ctas(int geo) { return geo ? EVR_NARROW_CTAS : EVR_WIDE_CTAS; }
+static int geo_smem_bytes(int geo) { return 220 * 1024 / geo_ctas(geo) / 8 * 8; }
+
+// dynamic shared memory of every geometry's kernels (set at context creation)
+static cudaError_t set_smem_attributes() {
+  cudaError_t e = cudaSuccess;
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(hpsi_batched_kernel<EVR_WIDE_CTAS, EVR_WIDE_FMAX>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, geo_smem_bytes(0));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(hpsi_multi_kernel<EVR_WIDE_CTAS, EVR_WIDE_FMAX>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, geo_smem_bytes(0));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(hpsi_batched_kernel<EVR_NARROW_CTAS, EVR_NARROW_FMAX>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, geo_smem_bytes(1));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(hpsi_multi_kernel<EVR_NARROW_CTAS, EVR_NARROW_FMAX>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, geo_smem_bytes(1));
+  return e;
 }
 
 __device__ __forceinline__ void neumaier_add(double& s, double& c, double x) {
@@ -845,9 +943,11 @@ struct evr_sg4_ctx {
   double* d_contrib = nullptr;       // [sum_nb][nrhs_v]
   size_t contrib_cap = 0;
   double* d_scratch = nullptr;
-  long long scratch_per_cta = 0;
+  long long scratch_per_cta = 0;     // doubles per CTA slab of the current plan
+  size_t scratch_cap = 0;            // doubles allocated
   int grid = 0;
   int smem_doubles = 0;
+  int geo = 0;                       // launch geometry (1: narrow, D <= EVR_NARROW_FMAX)
   int rmax = 32;                     // most right-hand sides per work item (evr_sg4_tune)
   // operator
   bool have_op = false;
@@ -1016,9 +1116,11 @@ extern "C" int evr_sg4_create(const evr_sg4_desc* d, evr_sg4_ctx** out) {
   fun_chunk[d->N] = (long long)chunk_q.size();
   c->n_chunks = (long long)chunk_q.size();
   chunk_q.push_back(inv_ptr[d->N]);
-  // launch geometry: EVR_CTAS_PER_SM persistent CTAs per SM sharing ~220 KB of shared memory
-  c->smem_doubles = 220 * 1024 / EVR_CTAS_PER_SM / 8;
-  c->grid = EVR_CTAS_PER_SM * c->num_sms;
+  // launch geometry: persistent CTAs per SM sharing ~220 KB of shared memory
+  // (wide until a work plan chooses otherwise)
+  c->geo = 0;
+  c->smem_doubles = geo_smem_bytes(0) / 8;
+  c->grid = geo_ctas(0) * c->num_sms;
   if ((rc = upload(&c->d_map, d->map, (size_t)z.sum_nb)) ||
       (rc = upload(&c->d_mats, mats.data(), mats.size())) ||
       (rc = upload(&c->d_mat_off, c->mat_off.data(), c->mat_off.size())) ||
@@ -1035,9 +1137,7 @@ extern "C" int evr_sg4_create(const evr_sg4_desc* d, evr_sg4_ctx** out) {
     free_ctx(c);
     return rc;
   }
-  e = cudaFuncSetAttribute(hpsi_batched_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, c->smem_doubles * 8);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(hpsi_multi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, c->smem_doubles * 8);
+  e = set_smem_attributes();
   if (e != cudaSuccess) {
     free_ctx(c);
     return set_error(EVR_ERR_CUDA, "evr_sg4_create: shared-memory attribute: %s", cudaGetErrorString(e));
@@ -1215,8 +1315,8 @@ extern "C" int evr_sg4_set_operator(evr_sg4_ctx* c, const evr_sg4_op_desc* op) {
 // Work list of one H.psi over nrhs_v virtual right-hand sides: (term, rhs
 // block) items in term order with their costs, and the term table with each
 // term's block size r for this nrhs_v (the context itself is not modified).
-static void plan_work(const evr_sg4_ctx* c, int nrhs_v, std::vector<TermInfo>& terms, std::vector<Item>& items,
-                      std::vector<float>& cost, long long& max_need) {
+static void plan_work(const evr_sg4_ctx* c, int nrhs_v, int smem_doubles, std::vector<TermInfo>& terms,
+                      std::vector<Item>& items, std::vector<float>& cost, long long& max_need) {
   const int nbuf = nbuf_for(c->type, c->D);
   const int Rmax = c->rmax;
   max_need = 0;
@@ -1226,7 +1326,7 @@ static void plan_work(const evr_sg4_ctx* c, int nrhs_v, std::vector<TermInfo>& t
   for (long long t = 0; t < c->nb_SG; ++t) {
     TermInfo& T = terms[t];
     long long per = (long long)nbuf * T.nq;
-    int r = (int)std::min<long long>(std::min(nrhs_v, Rmax), std::max<long long>(1, c->smem_doubles / per));
+    int r = (int)std::min<long long>(std::min(nrhs_v, Rmax), std::max<long long>(1, smem_doubles / per));
     if (c->nb0 > 1) {  // whole channel groups (both halves of complex columns): 2 nb0 columns
       const int g = 2 * c->nb0;
       r = std::max(g, r / g * g);
@@ -1243,12 +1343,22 @@ static void plan_work(const evr_sg4_ctx* c, int nrhs_v, std::vector<TermInfo>& t
   }
 }
 
+// Geometry of a plan with n_wide items planned for the wide kernel.
+static int choose_geo(int D, size_t n_wide, int num_sms) {
+  return D <= EVR_NARROW_FMAX && n_wide >= (size_t)EVR_NARROW_WAVES * geo_ctas(0) * num_sms ? 1 : 0;
+}
+
 // The same list sorted by decreasing cost (the persistent kernel then ends
-// balanced), with each term's block size written into c->terms.
+// balanced), with each term's block size written into c->terms; chooses the
+// launch geometry (c->geo, c->smem_doubles, c->grid) for this plan.
 static void plan_items(evr_sg4_ctx* c, int nrhs_v, std::vector<Item>& items, std::vector<Item>& sorted,
                        long long& max_need) {
   std::vector<float> cost;
-  plan_work(c, nrhs_v, c->terms, items, cost, max_need);
+  plan_work(c, nrhs_v, geo_smem_bytes(0) / 8, c->terms, items, cost, max_need);
+  c->geo = choose_geo(c->D, items.size(), c->num_sms);
+  c->smem_doubles = geo_smem_bytes(c->geo) / 8;
+  c->grid = geo_ctas(c->geo) * c->num_sms;
+  if (c->geo) plan_work(c, nrhs_v, c->smem_doubles, c->terms, items, cost, max_need);
   std::vector<int> order(items.size());
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
@@ -1302,12 +1412,13 @@ static int build_items(evr_sg4_ctx* c, int nrhs_v) {
   c->n_items = (int)items.size();
   // global scratch for terms that do not fit in shared memory
   long long per_cta = max_need > c->smem_doubles ? max_need : 0;
-  if (per_cta > c->scratch_per_cta) {
+  if ((size_t)per_cta * c->grid > c->scratch_cap) {
     if (c->d_scratch) cudaFree(c->d_scratch);
     c->d_scratch = nullptr;
     CUDA_TRY(cudaMalloc(&c->d_scratch, (size_t)per_cta * c->grid * 8));
-    c->scratch_per_cta = per_cta;
+    c->scratch_cap = (size_t)per_cta * c->grid;
   }
+  c->scratch_per_cta = per_cta;
   size_t pneed = (size_t)c->n_chunks * nrhs_v * 2;
   if (pneed > c->part_cap) {
     if (c->d_part) cudaFree(c->d_part);
@@ -1419,14 +1530,14 @@ static int hpsi_common(evr_sg4_ctx* c, int nrhs, int cshift, const double* psi, 
       q.items = c->d_items + c->slice_item[k];
       q.n_items = c->slice_item[k + 1] - c->slice_item[k];
       q.fbase = g0;
-      hpsi_batched_kernel<<<c->grid, EVR_CTA_THREADS, smem, s>>>(q);
+      launch_batched(c->geo, c->grid, smem, s, q);
       CUDA_TRY(cudaGetLastError());
       launches += 2;
     }
   } else if (!plain) {
     CUDA_TRY(cudaMemsetAsync(c->d_counter, 0, sizeof(unsigned int), s));
     p.items = c->d_items;
-    hpsi_batched_kernel<<<c->grid, EVR_CTA_THREADS, smem, s>>>(p);
+    launch_batched(c->geo, c->grid, smem, s, p);
     CUDA_TRY(cudaGetLastError());
     launches = 1;
   } else {
@@ -1434,7 +1545,7 @@ static int hpsi_common(evr_sg4_ctx* c, int nrhs, int cshift, const double* psi, 
     CUDA_TRY(cudaMemcpyAsync(c->d_params, &p, sizeof(KParams), cudaMemcpyHostToDevice, s));
     for (long long t = 0; t < c->nb_SG; ++t) {  // one launch per Smolyak term
       const int b0 = c->term_item_start[t], b1 = c->term_item_start[t + 1];
-      hpsi_multi_kernel<<<b1 - b0, EVR_CTA_THREADS, smem, s>>>(c->d_params, c->d_plain_items, b1, b0, nullptr);
+      launch_multi(c->geo, b1 - b0, smem, s, c->d_params, c->d_plain_items, b1, b0, nullptr);
       ++launches;
     }
     CUDA_TRY(cudaGetLastError());
@@ -1706,7 +1817,7 @@ extern "C" int evr_sg4_hpsi_noalloc(evr_sg4_ctx* c, int nrhs, const double* psi,
   p.contrib = (double*)(base + off_contrib);
   p.gscratch = per_cta ? (double*)(base + off_slabs) : nullptr;
   p.scratch_per_cta = per_cta;
-  hpsi_batched_kernel<<<grid, EVR_CTA_THREADS, (size_t)c->smem_doubles * 8, s>>>(p);
+  launch_batched(c->geo, grid, (size_t)c->smem_doubles * 8, s, p);
   CUDA_TRY(cudaGetLastError());
   int rc = launch_reduce(c, p.contrib, (double2*)(base + off_part), nrhs_v, 0, psi, ldpsi, hpsi, ldh, E0, Esc, s);
   if (rc) return rc;
@@ -1726,6 +1837,7 @@ extern "C" int evr_sg4_hpsi_noalloc(evr_sg4_ctx* c, int nrhs, const double* psi,
 // ------------------------------------------------------------------------
 struct evr_sg4_multi {
   int n = 0, cshift = 0, transpose = 0, grid = 0, smem_doubles = 0;
+  int geo = 1;                   // narrow only when every context is
   std::vector<evr_sg4_ctx*> ctxs;
   std::vector<int> nrhs_v, type;
   std::vector<TermInfo*> d_terms;
@@ -1776,7 +1888,6 @@ extern "C" int evr_sg4_multi_create(int n, evr_sg4_ctx* const* ctxs, const int* 
   m->n = n;
   m->cshift = (flags & EVR_APPLY_COMPLEX) ? 1 : 0;
   m->transpose = (flags & EVR_APPLY_TRANSPOSE) ? 1 : 0;
-  m->grid = ctxs[0]->grid;
   m->ctxs.assign(ctxs, ctxs + n);
   m->nrhs_v.resize(n);
   m->type.resize(n);
@@ -1787,19 +1898,34 @@ extern "C" int evr_sg4_multi_create(int n, evr_sg4_ctx* const* ctxs, const int* 
   std::vector<float> allcost;
   long long max_need = 0;
   auto fail = [&](int rc) { free_multi(m); return rc; };
+  // geometry: narrow only if every context has D <= 6 and the merged wide
+  // plan has enough waves of items
+  size_t n_wide = 0;
+  int dmax = 0;
+  for (int k = 0; k < n; ++k) {
+    evr_sg4_ctx* c = ctxs[k];
+    std::vector<TermInfo> terms;
+    std::vector<Item> items;
+    std::vector<float> cost;
+    long long need = 0;
+    plan_work(c, (nrhs[k] * c->nb0) << m->cshift, geo_smem_bytes(0) / 8, terms, items, cost, need);
+    n_wide += items.size();
+    dmax = std::max(dmax, c->D);
+  }
+  m->geo = choose_geo(dmax, n_wide, ctxs[0]->num_sms);
+  m->smem_doubles = geo_smem_bytes(m->geo) / 8;
+  m->grid = geo_ctas(m->geo) * ctxs[0]->num_sms;
   for (int k = 0; k < n; ++k) {
     evr_sg4_ctx* c = ctxs[k];
     const int nv = (nrhs[k] * c->nb0) << m->cshift;
     m->nrhs_v[k] = nv;
     m->type[k] = c->type;
-    m->grid = std::min(m->grid, c->grid);
-    m->smem_doubles = std::max(m->smem_doubles, c->smem_doubles);
     std::vector<TermInfo> terms;
     std::vector<Item> items;
     std::vector<float> cost;
     long long need = 0;
-    plan_work(c, nv, terms, items, cost, need);
-    if (need > c->smem_doubles) max_need = std::max(max_need, need);
+    plan_work(c, nv, m->smem_doubles, terms, items, cost, need);
+    if (need > m->smem_doubles) max_need = std::max(max_need, need);
     for (size_t q = 0; q < items.size(); ++q) {
       all.push_back(MItem{k, items[q].term, items[q].rhs0, 0});
       allcost.push_back(cost[q]);
@@ -1859,6 +1985,7 @@ extern "C" int evr_sg4_multi_hpsi(evr_sg4_multi* m, const double* const* psi, co
     KParams& p = params[k];
     p = make_params(c, m->nrhs_v[k], m->cshift, psi[k], ldpsi[k] << m->cshift, hpsi[k], ldh[k] << m->cshift, 1.0);
     p.transpose = m->transpose;
+    p.smem_doubles = m->smem_doubles;  // the plan's geometry, not the context's own last plan
     p.terms = m->d_terms[k];
     p.contrib = m->d_contrib[k];
     p.gscratch = m->d_scratch;
@@ -1882,10 +2009,7 @@ extern "C" int evr_sg4_multi_hpsi(evr_sg4_multi* m, const double* const* psi, co
   }
   CUDA_TRY(cudaMemcpyAsync(m->d_params, params.data(), (size_t)m->n * sizeof(KParams), cudaMemcpyHostToDevice, s));
   CUDA_TRY(cudaMemsetAsync(m->d_counter, 0, sizeof(unsigned int), s));
-  CUDA_TRY(cudaFuncSetAttribute(hpsi_multi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                m->smem_doubles * 8));
-  hpsi_multi_kernel<<<m->grid, EVR_CTA_THREADS, (size_t)m->smem_doubles * 8, s>>>(m->d_params, items, n_items, 0,
-                                                                                   m->d_counter);
+  launch_multi(m->geo, m->grid, (size_t)m->smem_doubles * 8, s, m->d_params, items, n_items, 0, m->d_counter);
   CUDA_TRY(cudaGetLastError());
   for (int k = 0; k < m->n; ++k) {
     if (!psi[k]) continue;
@@ -1983,6 +2107,7 @@ int evr::field_pair_create(evr_sg4_ctx* a, evr_sg4_ctx* b, int transpose, FieldP
   for (int k = 0; k < 2; ++k) {
     ps[k] = make_params(cs[k], 2, 1, f->x, 2 * a->N, nullptr, 2 * a->N, 1.0);
     ps[k].transpose = m->transpose;
+    ps[k].smem_doubles = m->smem_doubles;
     ps[k].terms = m->d_terms[k];
     ps[k].contrib = m->d_contrib[k];
     ps[k].gscratch = m->d_scratch;
@@ -1998,12 +2123,6 @@ int evr::field_pair_create(evr_sg4_ctx* a, evr_sg4_ctx* b, int transpose, FieldP
   }
   // enough CTAs for every item, so small operators leave SMs to other streams
   f->grid = (int)std::min<size_t>((size_t)m->grid, std::max<size_t>(1, m->sorted.size()));
-  if (cudaFuncSetAttribute(hpsi_multi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, m->smem_doubles * 8) !=
-      cudaSuccess) {
-    cudaGetLastError();
-    field_pair_destroy(f);
-    return set_error(EVR_ERR_CUDA, "field pair: shared-memory attribute");
-  }
   *out = f;
   return EVR_OK;
 }
@@ -2020,8 +2139,8 @@ int evr::field_pair_apply(FieldPair* f, void* stream) {
   cudaStream_t s = (cudaStream_t)stream;
   evr_sg4_multi* m = f->m;
   evr_sg4_ctx* c = m->ctxs[0];
-  hpsi_multi_kernel<<<f->grid, EVR_CTA_THREADS, (size_t)m->smem_doubles * 8, s>>>(
-      m->d_params, m->d_items, (int)m->sorted.size(), 0, m->d_counter);
+  launch_multi(m->geo, f->grid, (size_t)m->smem_doubles * 8, s, m->d_params, m->d_items, (int)m->sorted.size(), 0,
+               m->d_counter);
   const long long t1 = c->n_chunks * 4;
   const long long b1 = std::max<long long>(1, std::min<long long>((t1 + 255) / 256, 16LL * c->num_sms));
   pair_chunks_kernel<<<(unsigned)b1, 256, 0, s>>>(m->d_contrib[0], m->d_contrib[1], c->d_chunk_q, c->n_chunks,
