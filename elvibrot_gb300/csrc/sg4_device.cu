@@ -98,15 +98,18 @@ int desc_sizes(const evr_sg4_desc* d, DescSizes* z) {
 // each), fused type-10 passes up to D = 12; it beat two 256-thread CTAs by
 // 0.7 % on the 6-D benchmark and lets the ~600 items of a small operator run
 // in one wave.  Narrow, for D <= 6 and plans of at least EVR_NARROW_WAVES
-// waves of items: EVR_NARROW_CTAS CTAs per SM (less shared memory and fewer
-// registers each, the fused passes instantiated only up to D = 6): more
-// resident warps keep the FP64 pipe busier on large operators (+5 % on the
-// 6-D benchmark), while a small operator's one wave of items finishes sooner
-// with the wide kernel's longer register budget.
+// waves of items: EVR_NARROW_CTAS CTAs per SM (26.5 KB and 64 registers
+// each, the fused passes instantiated only up to D = 6): more resident warps
+// keep the FP64 pipe busier on large operators (8 CTAs: +7 % on the 6-D
+// benchmark; 7 and 6 CTAs, and four 256-thread CTAs, are within 3 %), while
+// a small operator's one wave of items finishes sooner with the wide
+// kernel's longer register budget.
 #ifndef EVR_CTA_THREADS
 #define EVR_CTA_THREADS 128
 #endif
+#ifndef EVR_WIDE_CTAS
 #define EVR_WIDE_CTAS 4
+#endif
 #define EVR_WIDE_FMAX 12
 #ifndef EVR_NARROW_CTAS
 #define EVR_NARROW_CTAS 8
@@ -193,6 +196,8 @@ struct KParams {
 struct ItemShared {
   int nb[EVR_MAXD], nq[EVR_MAXD];
   int ord[EVR_MAXD];          // basis->grid mode order
+  int pos[EVR_MAXD];          // rank of each mode in that order (inverse of ord)
+  int st[EVR_MAXD];           // grid stride of each mode (product of the nq before it)
   int mo[EVR_MAXD][4];
   long long off_nb, off_nq;
   int nb_t, nq_t, r, rhs0, term;
@@ -311,20 +316,22 @@ __device__ void grid_deriv(const KParams& p, const ItemShared& it, int i, int wh
 // modes are taken in the order that minimises multiply-adds: basis->grid in
 // ascending (nq-nb)/(nb*nq) (the modes that grow the array most go last),
 // grid->basis in the reverse order (they shrink it first).
+// The extents of the other modes at step k follow from their ranks in the
+// order (a mode already passed has its output size), read from the item's
+// shared block rather than kept in a per-thread array.
 __device__ double* transform(const KParams& p, const ItemShared& it, bool to_grid, double* a, double* b) {
-  int cur[EVR_MAXD];
-  for (int j = 0; j < p.D; ++j) cur[j] = to_grid ? it.nb[j] : it.nq[j];
   for (int k = 0; k < p.D; ++k) {
     const int i = it.ord[to_grid ? k : p.D - 1 - k];
-    const int nin = cur[i];
+    const int nin = to_grid ? it.nb[i] : it.nq[i];
     const int nout = to_grid ? it.nq[i] : it.nb[i];
     int S = 1, R = it.r;
     for (int j = 0; j < p.D; ++j) {
-      if (j < i) S *= cur[j];
-      else if (j > i) R *= cur[j];
+      const bool done = to_grid ? it.pos[j] < k : it.pos[j] > p.D - 1 - k;
+      const int c = (done == to_grid) ? it.nq[j] : it.nb[j];
+      if (j < i) S *= c;
+      else if (j > i) R *= c;
     }
     mode_pass(p.mats + it.mo[i][to_grid ? M_BG : M_GB], nin, nout, S, R, a, b, false, 1.0);
-    cur[i] = nout;
     __syncthreads();
     double* t = a;
     a = b;
@@ -338,7 +345,8 @@ __device__ double* transform(const KParams& p, const ItemShared& it, bool to_gri
 //   pass A, per point: phi_j = (d_j x)(point) for every mode j (D independent
 //     FMA chains over the mode fibres through the point), then
 //     U_i = Jac sum_j G_ji phi_j, stored;
-//   pass B, per point: O = c * sum_i (d_i U_i)(point) + O  (O holds V.x).
+//   pass B, per point: O = c * sum_i (d_i U_i)(point) + O  (O holds V.x), or,
+//     without Jac and rho, O = V.x - 1/2 sum_i (d_i U_i)(point) written over x.
 // The reference applies d_j to the whole grid mode by mode
 // (DerivOp_TO_RDP_OF_SmolaykRep); the same products, with two barriers
 // instead of 2D+2 and no phi arrays.  For H^T the matrices are transposed
@@ -380,8 +388,8 @@ struct GridPos {
 // The point's digits come from GridPos (INC, fewer instructions) or from
 // divisions of the element index (fewer registers: the narrow geometry's
 // 64-register budget spills less without the digit arrays).
-template <int DD, bool INC>
-__device__ __forceinline__ void point_digits(GridPos<DD>& gp, const int* nq, int nqt, int e, int* idx, int& q) {
+template <int DD, bool INC, class MS>
+__device__ __forceinline__ void point_digits(GridPos<DD>& gp, const MS& ms, int nqt, int e, int* idx, int& q) {
   if constexpr (INC) {
     q = e - gp.j * nqt;
 #pragma unroll
@@ -391,46 +399,70 @@ __device__ __forceinline__ void point_digits(GridPos<DD>& gp, const int* nq, int
     int rem = q;
 #pragma unroll
     for (int i = 0; i < DD; ++i) {
-      idx[i] = rem % nq[i];
-      rem /= nq[i];
+      const int n = ms.nq(i);
+      idx[i] = rem % n;
+      rem /= n;
     }
   }
 }
 
-template <int DD, bool INC>
-__device__ void type10_fused(const KParams& p, const ItemShared& it, const double* x, double* O, double* U,
-                             int NQR) {
-  const int nqt = it.nq_t;
-  const long long oq = it.off_nq;
-  int nq[DD], st[DD];
-  const double* Md[DD];
-  {
-    int stride = 1;
+// Per-mode sizes, grid strides and derivative matrices: in registers for the
+// wide geometry, read from the item's shared block for the narrow one (its
+// 64-register budget cannot hold 4 D values beside the point's digits and
+// the D partial sums; spilled copies would live in local memory that the
+// full shared-memory carve-out leaves almost no L1 for).
+template <int DD, bool REG>
+struct ModeSizes;
+template <int DD>
+struct ModeSizes<DD, true> {
+  int nq_[DD], st_[DD];
+  const double* Md_[DD];
+  __device__ __forceinline__ ModeSizes(const KParams& p, const ItemShared& it) {
 #pragma unroll
     for (int i = 0; i < DD; ++i) {
-      nq[i] = it.nq[i];
-      st[i] = stride;
-      stride *= nq[i];
-      Md[i] = p.mats + it.mo[i][M_D1];
+      nq_[i] = it.nq[i];
+      st_[i] = it.st[i];
+      Md_[i] = p.mats + it.mo[i][M_D1];
     }
   }
+  __device__ __forceinline__ int nq(int i) const { return nq_[i]; }
+  __device__ __forceinline__ int st(int i) const { return st_[i]; }
+  __device__ __forceinline__ const double* Md(int i) const { return Md_[i]; }
+};
+template <int DD>
+struct ModeSizes<DD, false> {
+  const volatile ItemShared& it;
+  const double* mats;
+  __device__ __forceinline__ ModeSizes(const KParams& p, const ItemShared& s) : it(s), mats(p.mats) {}
+  __device__ __forceinline__ int nq(int i) const { return it.nq[i]; }
+  __device__ __forceinline__ int st(int i) const { return it.st[i]; }
+  __device__ __forceinline__ const double* Md(int i) const { return mats + it.mo[i][M_D1]; }
+};
+
+template <int DD, bool INC>
+__device__ void type10_fused(const KParams& p, const ItemShared& it, const double* x, double* O, double* U,
+                             int NQR, bool inplace) {
+  const int nqt = it.nq_t;
+  const long long oq = it.off_nq;
+  const ModeSizes<DD, INC> ms(p, it);
   const long long GD = (long long)DD * DD;
   const long long si = p.transpose ? nqt : (long long)nqt * DD;  // G offset step of the output index
   const long long sj = p.transpose ? (long long)nqt * DD : nqt;  // ... and of the input index
   GridPos<DD> gp;
-  if constexpr (INC) gp.init(nq, nqt, threadIdx.x, blockDim.x);
+  if constexpr (INC) gp.init(ms.nq_, nqt, threadIdx.x, blockDim.x);
   for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
     int idx[DD], q;
-    point_digits<DD, INC>(gp, nq, nqt, e, idx, q);
-    if constexpr (INC) gp.advance(nq, blockDim.x);
+    point_digits<DD, INC>(gp, ms, nqt, e, idx, q);
+    if constexpr (INC) gp.advance(ms.nq_, blockDim.x);
     const double* xr = x + (e - q);
     double phi[DD];
 #pragma unroll
     for (int j = 0; j < DD; ++j) {
-      const double* fib = xr + (q - idx[j] * st[j]);
-      const double* row = Md[j] + idx[j] * nq[j];
+      const int n = ms.nq(j), sd = ms.st(j);
+      const double* fib = xr + (q - idx[j] * sd);
+      const double* row = ms.Md(j) + idx[j] * n;
       double a = 0.0;
-      for (int m = 0; m < nq[j]; ++m) a = fma(__ldg(row + m), fib[m * st[j]], a);
+      for (int m = 0; m < n; ++m) a = fma(__ldg(row + m), fib[m * sd], a);
       phi[j] = a;
     }
     const double jac = p.Jac ? __ldg(p.Jac + oq + q) : 1.0;
@@ -449,37 +481,44 @@ __device__ void type10_fused(const KParams& p, const ItemShared& it, const doubl
     }
   }
   __syncthreads();
-  if constexpr (INC) gp.init(nq, nqt, threadIdx.x, blockDim.x);
+  if constexpr (INC) gp.init(ms.nq_, nqt, threadIdx.x, blockDim.x);
   for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
     int idx[DD], q;
-    point_digits<DD, INC>(gp, nq, nqt, e, idx, q);
-    if constexpr (INC) gp.advance(nq, blockDim.x);
+    point_digits<DD, INC>(gp, ms, nqt, e, idx, q);
+    if constexpr (INC) gp.advance(ms.nq_, blockDim.x);
     double acc[DD];
 #pragma unroll
     for (int i = 0; i < DD; ++i) {
-      const double* fib = U + (long long)i * NQR + (e - idx[i] * st[i]);
-      const double* row = Md[i] + idx[i] * nq[i];
+      const int n = ms.nq(i), sd = ms.st(i);
+      const double* fib = U + (long long)i * NQR + (e - idx[i] * sd);
+      const double* row = ms.Md(i) + idx[i] * n;
       double a = 0.0;
-      for (int m = 0; m < nq[i]; ++m) a = fma(__ldg(row + m), fib[m * st[i]], a);
+      for (int m = 0; m < n; ++m) a = fma(__ldg(row + m), fib[m * sd], a);
       acc[i] = a;
     }
     double sum = 0.0;
 #pragma unroll
     for (int i = 0; i < DD; ++i) sum += acc[i];
-    const double cf = !p.transpose ? (p.cfac ? __ldg(p.cfac + oq + q) : -0.5)
-                                   : (p.sqRho ? __ldg(p.sqRho + oq + q) : 1.0);
-    O[e] = fma(cf, sum, O[e]);
+    if (inplace) {  // O is x: V.x + (-1/2) sum, both directions
+      const double vx = p.V ? __ldg(p.V + oq + q) * O[e] : 0.0;
+      O[e] = fma(-0.5, sum, vx);
+    } else {
+      const double cf = !p.transpose ? (p.cfac ? __ldg(p.cfac + oq + q) : -0.5)
+                                     : (p.sqRho ? __ldg(p.sqRho + oq + q) : 1.0);
+      O[e] = fma(cf, sum, O[e]);
+    }
   }
   __syncthreads();
 }
 
 template <int FMAX>
 __device__ void type10_fused_dispatch(const KParams& p, const ItemShared& it, const double* x, double* O, double* U,
-                                      int NQR) {
+                                      int NQR, bool inplace) {
   switch (p.D) {
 #define EVR_T10(n)                                                        \
   case n:                                                                 \
-    if constexpr (n <= FMAX) type10_fused<n, (FMAX > EVR_NARROW_FMAX) || EVR_NARROW_INC>(p, it, x, O, U, NQR); \
+    if constexpr (n <= FMAX)                                              \
+      type10_fused<n, (FMAX > EVR_NARROW_FMAX) || EVR_NARROW_INC>(p, it, x, O, U, NQR, inplace); \
     break;
     EVR_T10(1) EVR_T10(2) EVR_T10(3) EVR_T10(4) EVR_T10(5) EVR_T10(6) EVR_T10(7) EVR_T10(8) EVR_T10(9)
     EVR_T10(10) EVR_T10(11) EVR_T10(12)
@@ -541,6 +580,12 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ter
       }
       it.ord[j] = i;
     }
+    int stride = 1;
+    for (int k = 0; k < p.D; ++k) {
+      it.pos[it.ord[k]] = k;
+      it.st[k] = stride;
+      stride *= it.nq[k];
+    }
   }
   __syncthreads();
   const int D = p.D, r = it.r, nbt = it.nb_t, nqt = it.nq_t;
@@ -550,14 +595,16 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ter
   double* T = buf + NQR;
   const int* map = p.map + it.off_nb;
 
-  // gather (tabPackedBasis_TO_tabR_AT_iG)
+  // gather (tabPackedBasis_TO_tabR_AT_iG) into the buffer from which the D
+  // ping-pong passes of basis->grid end in X
+  double* G0 = (D & 1) ? T : X;
   for (int e = threadIdx.x; e < nbt * r; e += blockDim.x) {
     const int j = e / nbt, k = e - j * nbt;
     int n = __ldg(map + k);
-    X[e] = n > 0 ? p.psi[vaddr(p, it.rhs0 + j, n - 1, p.ldpsi)] : 0.0;
+    G0[e] = n > 0 ? p.psi[vaddr(p, it.rhs0 + j, n - 1, p.ldpsi)] : 0.0;
   }
   __syncthreads();
-  double* x = transform(p, it, true, X, T);
+  double* x = transform(p, it, true, G0, G0 == X ? T : X);
   double* y;
   const long long oq = it.off_nq;
 
@@ -604,23 +651,30 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ter
     }
     y = Y;
   } else if (D <= FMAX) {
-    // CASE 10 through the fused grid passes; buffers: the transform pair
-    // {X, T}, then U_1..U_D.  O (= the free transform buffer) starts as V.x.
-    double* O = (x == X) ? T : X;
-    double* U = buf + 2 * NQR;
-    for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
-      const int q = e % nqt;
-      const double xv = x[e];
-      O[e] = p.V ? __ldg(p.V + oq + q) * xv : 0.0;
-      if (!p.transpose) {
-        if (p.sqRho) x[e] = xv * __ldg(p.sqRho + oq + q);
-      } else {
-        x[e] = xv * (p.cfac ? __ldg(p.cfac + oq + q) : -0.5);
+    // CASE 10 through the fused grid passes; x is in X.  Without Jac and rho
+    // (D + 1 arrays) U_1..U_D follow X and pass B writes O = V.x + c.sum over
+    // x itself (each point is read and written by one thread; the -1/2 of
+    // H^T is applied there too: scaling by -1/2 is exact, so the result is
+    // the same bits as scaling x first).  Otherwise x is rescaled in place
+    // and O = V.x starts in T, with U_1..U_D after it (D + 2 arrays).
+    const bool inplace = p.nbuf == D + 1;
+    double* O = inplace ? x : T;
+    double* U = buf + (inplace ? 1 : 2) * NQR;
+    if (!inplace) {
+      for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
+        const int q = e % nqt;
+        const double xv = x[e];
+        O[e] = p.V ? __ldg(p.V + oq + q) * xv : 0.0;
+        if (!p.transpose) {
+          if (p.sqRho) x[e] = xv * __ldg(p.sqRho + oq + q);
+        } else {
+          x[e] = xv * (p.cfac ? __ldg(p.cfac + oq + q) : -0.5);
+        }
       }
+      __syncthreads();
     }
-    __syncthreads();
-    type10_fused_dispatch<FMAX>(p, it, x, O, U, NQR);
-    double* yb = transform(p, it, false, O, x);
+    type10_fused_dispatch<FMAX>(p, it, x, O, U, NQR, inplace);
+    double* yb = transform(p, it, false, O, inplace ? buf + NQR : x);
     store_contrib(p, it, yb);
     return;
   } else {
@@ -747,7 +801,10 @@ static void launch_multi(int geo, unsigned grid, size_t smem, cudaStream_t s, co
 }
 
 static int geo_ctas(int geo) { return geo ? EVR_NARROW_CTAS : EVR_WIDE_CTAS; }
-static int geo_smem_bytes(int geo) { return 220 * 1024 / geo_ctas(geo) / 8 * 8; }
+// dynamic shared memory per CTA: the SM's 228 KB split between the resident
+// CTAs, less 2 KB each for the static shared variables and the driver's
+// per-CTA reservation, so all of them fit (55 KB wide, 26.5 KB narrow)
+static int geo_smem_bytes(int geo) { return (228 * 1024 / geo_ctas(geo) - 2048) / 256 * 256; }
 
 // dynamic shared memory of every geometry's kernels (set at context creation)
 static cudaError_t set_smem_attributes() {
@@ -979,8 +1036,16 @@ struct evr_sg4_ctx {
   long long last_launches = 0;
 };
 
-static int nbuf_for(int type, int D) {
-  return type == 0 ? 2 : (type == 1 ? 4 : (D <= EVR_FUSED_MAXD ? D + 2 : D + 4));
+// Work arrays per item and grid point.  The fused type-10 passes need x and
+// U_1..U_D, plus a separate V.x array when x is rescaled in place (Jac or rho
+// given): without them pass B writes O over x (D + 1 arrays, so more items
+// keep their arrays in shared memory).
+static int nbuf_for(const evr_sg4_ctx* c) {
+  const int D = c->D;
+  if (c->type == 0) return 2;
+  if (c->type == 1) return 4;
+  if (D > EVR_FUSED_MAXD) return D + 4;
+  return (c->d_Jac || c->d_sqRho) ? D + 2 : D + 1;
 }
 
 static void free_ctx(evr_sg4_ctx* c) {
@@ -1317,7 +1382,7 @@ extern "C" int evr_sg4_set_operator(evr_sg4_ctx* c, const evr_sg4_op_desc* op) {
 // term's block size r for this nrhs_v (the context itself is not modified).
 static void plan_work(const evr_sg4_ctx* c, int nrhs_v, int smem_doubles, std::vector<TermInfo>& terms,
                       std::vector<Item>& items, std::vector<float>& cost, long long& max_need) {
-  const int nbuf = nbuf_for(c->type, c->D);
+  const int nbuf = nbuf_for(c);
   const int Rmax = c->rmax;
   max_need = 0;
   items.clear();
@@ -1479,7 +1544,7 @@ static KParams make_params(evr_sg4_ctx* c, int nrhs_v, int cshift, const double*
   p.F2 = c->d_F2;
   p.F1 = c->d_F1;
   p.type = c->type;
-  p.nbuf = nbuf_for(c->type, c->D);
+  p.nbuf = nbuf_for(c);
   p.smem_doubles = c->smem_doubles;
   p.gscratch = c->d_scratch;
   p.scratch_per_cta = c->scratch_per_cta;
@@ -1839,7 +1904,7 @@ struct evr_sg4_multi {
   int n = 0, cshift = 0, transpose = 0, grid = 0, smem_doubles = 0;
   int geo = 1;                   // narrow only when every context is
   std::vector<evr_sg4_ctx*> ctxs;
-  std::vector<int> nrhs_v, type;
+  std::vector<int> nrhs_v, type, nbuf;  // per context; type and work arrays per point fix the plan
   std::vector<TermInfo*> d_terms;
   std::vector<double*> d_contrib;
   std::vector<double*> d_part;
@@ -1891,6 +1956,7 @@ extern "C" int evr_sg4_multi_create(int n, evr_sg4_ctx* const* ctxs, const int* 
   m->ctxs.assign(ctxs, ctxs + n);
   m->nrhs_v.resize(n);
   m->type.resize(n);
+  m->nbuf.resize(n);
   m->d_terms.assign(n, nullptr);
   m->d_contrib.assign(n, nullptr);
   m->d_part.assign(n, nullptr);
@@ -1920,6 +1986,7 @@ extern "C" int evr_sg4_multi_create(int n, evr_sg4_ctx* const* ctxs, const int* 
     const int nv = (nrhs[k] * c->nb0) << m->cshift;
     m->nrhs_v[k] = nv;
     m->type[k] = c->type;
+    m->nbuf[k] = nbuf_for(c);
     std::vector<TermInfo> terms;
     std::vector<Item> items;
     std::vector<float> cost;
@@ -1975,7 +2042,7 @@ extern "C" int evr_sg4_multi_hpsi(evr_sg4_multi* m, const double* const* psi, co
   for (int k = 0; k < m->n; ++k) {
     evr_sg4_ctx* c = m->ctxs[k];
     if (!psi[k]) continue;  // context k is skipped in this call
-    if (!c->have_op || c->type != m->type[k] || c->streamed)
+    if (!c->have_op || c->type != m->type[k] || nbuf_for(c) != m->nbuf[k] || c->streamed)
       return set_error(EVR_ERR_STATE, "multi_hpsi: the operator of context %d changed since multi_create", k);
     if (!hpsi[k] || ldpsi[k] < c->nvec || ldh[k] < c->nvec)
       return set_error(EVR_ERR_ARG, "multi_hpsi: bad output or leading dimension for context %d", k);
