@@ -486,19 +486,16 @@ __device__ void type10_fused(const KParams& p, const ItemShared& it, const doubl
     int idx[DD], q;
     point_digits<DD, INC>(gp, ms, nqt, e, idx, q);
     if constexpr (INC) gp.advance(ms.nq_, blockDim.x);
-    double acc[DD];
+    // one FMA chain over the fibres of every mode (no partial sums to add:
+    // the FP64 pipe, not latency, bounds the kernel)
+    double sum = 0.0;
 #pragma unroll
     for (int i = 0; i < DD; ++i) {
       const int n = ms.nq(i), sd = ms.st(i);
       const double* fib = U + (long long)i * NQR + (e - idx[i] * sd);
       const double* row = ms.Md(i) + idx[i] * n;
-      double a = 0.0;
-      for (int m = 0; m < n; ++m) a = fma(__ldg(row + m), fib[m * sd], a);
-      acc[i] = a;
+      for (int m = 0; m < n; ++m) sum = fma(__ldg(row + m), fib[m * sd], sum);
     }
-    double sum = 0.0;
-#pragma unroll
-    for (int i = 0; i < DD; ++i) sum += acc[i];
     if (inplace) {  // O is x: V.x + (-1/2) sum, both directions
       const double vx = p.V ? __ldg(p.V + oq + q) * O[e] : 0.0;
       O[e] = fma(-0.5, sum, vx);
