@@ -798,10 +798,35 @@ static void launch_multi(int geo, unsigned grid, size_t smem, cudaStream_t s, co
 }
 
 static int geo_ctas(int geo) { return geo ? EVR_NARROW_CTAS : EVR_WIDE_CTAS; }
+// Static shared memory plus the 1 KB the driver reserves per CTA, rounded up
+// to 256 bytes (queried once): for the wide geometry the larger of its two
+// item kernels (the field-driven propagation and multi-context plans run the
+// multi-context kernel there; sized for the single-context kernel alone, it
+// kept three CTAs per SM instead of four and the RK4 forward ran 7 % slower);
+// for the narrow one the single-context kernel, whose eight CTAs per SM
+// carry the large operators (a narrow multi-context launch, with its larger
+// parameter block, keeps seven).
+template <class K1, class K2>
+static int slack_of(K1 k1, K2 k2, bool both) {
+  cudaFuncAttributes a, b;
+  if (cudaFuncGetAttributes(&a, k1) != cudaSuccess || cudaFuncGetAttributes(&b, k2) != cudaSuccess) {
+    cudaGetLastError();
+    return 4096;
+  }
+  const size_t st = both ? std::max(a.sharedSizeBytes, b.sharedSizeBytes) : a.sharedSizeBytes;
+  return (int)((st + 1024 + 255) / 256 * 256);
+}
+static int smem_slack(int geo) {
+  static const int wide = slack_of(hpsi_batched_kernel<EVR_WIDE_CTAS, EVR_WIDE_FMAX>,
+                                   hpsi_multi_kernel<EVR_WIDE_CTAS, EVR_WIDE_FMAX>, true);
+  static const int narrow = slack_of(hpsi_batched_kernel<EVR_NARROW_CTAS, EVR_NARROW_FMAX>,
+                                     hpsi_multi_kernel<EVR_NARROW_CTAS, EVR_NARROW_FMAX>, false);
+  return geo ? narrow : wide;
+}
+
 // dynamic shared memory per CTA: the SM's 228 KB split between the resident
-// CTAs, less 2 KB each for the static shared variables and the driver's
-// per-CTA reservation, so all of them fit (55 KB wide, 26.5 KB narrow)
-static int geo_smem_bytes(int geo) { return (228 * 1024 / geo_ctas(geo) - 2048) / 256 * 256; }
+// CTAs, less the slack above, so all of them fit (55 KB wide, 26.5 KB narrow)
+static int geo_smem_bytes(int geo) { return (228 * 1024 / geo_ctas(geo) - smem_slack(geo)) / 256 * 256; }
 
 // dynamic shared memory of every geometry's kernels (set at context creation)
 static cudaError_t set_smem_attributes() {
