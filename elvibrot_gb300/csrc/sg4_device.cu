@@ -94,7 +94,7 @@ int desc_sizes(const evr_sg4_desc* d, DescSizes* z) {
 #define EVR_FUSED_MAXD 12  // type-10 items with D <= 12 use the fused grid passes
 #endif
 // Persistent H.psi launch geometry, chosen per work plan.  Wide: four
-// 128-thread CTAs per SM (55 KB of shared memory and 128 registers a thread
+// 128-thread CTAs per SM (54.75 KB of shared memory and 128 registers a thread
 // each), fused type-10 passes up to D = 12; it beat two 256-thread CTAs by
 // 0.7 % on the 6-D benchmark and lets the ~600 items of a small operator run
 // in one wave.  Narrow, for D <= 6 and plans of at least EVR_NARROW_WAVES
@@ -279,9 +279,46 @@ __device__ __forceinline__ void mode_pass_t(const double* __restrict__ M, int no
   }
 }
 
+// Few fibres (when one thread per fibre leaves a longer critical path than
+// one thread per output element): one thread per output element, so the
+// threads share the pass evenly.  Each output is one FMA chain over the
+// fibre's inputs in the same order as above, so the bits are the same.  The
+// typical basis<->grid pass of a small term has one or two fibres per
+// thread; splitting made the 6-D benchmark 4.8 % faster.
+template <int NIN, int MODE>
+__device__ __forceinline__ void mode_pass_split(const double* __restrict__ M, int nout, int S, int R,
+                                                const double* in, double* out, double scale) {
+  const int nf = S * R;
+  for (int u = threadIdx.x; u < nf * nout; u += blockDim.x) {
+    const int k = u / nf, f = u - k * nf;
+    const int b = f / S, a = f - b * S;
+    const double* fi = in + a + S * NIN * b;
+    const double* Mk = M + k * NIN;
+    double s0 = 0.0;
+#pragma unroll
+    for (int m = 0; m < NIN; ++m) s0 = fma(__ldg(Mk + m), fi[S * m], s0);
+    double* fo = out + a + S * (k + nout * b);
+    if (MODE == 0) *fo = s0;
+    else if (MODE == 1) *fo += s0;
+    else *fo = fma(scale, s0, *fo);
+  }
+}
+
 template <int MODE>
 __device__ __noinline__ void mode_pass_m(const double* M, int nin, int nout, int S, int R, const double* in, double* out,
                             double scale) {
+  const int nf = S * R, T = blockDim.x;
+  if (nout > 1 && (nf * nout + T - 1) / T < ((nf + T - 1) / T) * nout) {
+    switch (nin) {
+#define EVR_CASE(n) \
+  case n:           \
+    mode_pass_split<n, MODE>(M, nout, S, R, in, out, scale); return;
+      EVR_CASE(1) EVR_CASE(2) EVR_CASE(3) EVR_CASE(4) EVR_CASE(5) EVR_CASE(6) EVR_CASE(7) EVR_CASE(8)
+      EVR_CASE(9) EVR_CASE(10) EVR_CASE(11) EVR_CASE(12) EVR_CASE(13) EVR_CASE(14) EVR_CASE(15) EVR_CASE(16)
+#undef EVR_CASE
+      default: return;
+    }
+  }
   switch (nin) {
 #define EVR_CASE(n) \
   case n:           \
@@ -825,7 +862,7 @@ static int smem_slack(int geo) {
 }
 
 // dynamic shared memory per CTA: the SM's 228 KB split between the resident
-// CTAs, less the slack above, so all of them fit (55 KB wide, 26.5 KB narrow)
+// CTAs, less the slack above, so all of them fit (54.75 KB wide, 26.5 KB narrow)
 static int geo_smem_bytes(int geo) { return (228 * 1024 / geo_ctas(geo) - smem_slack(geo)) / 256 * 256; }
 
 // dynamic shared memory of every geometry's kernels (set at context creation)
