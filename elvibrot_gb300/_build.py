@@ -17,7 +17,12 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libevrsg4.so")
 
-SOURCES = ["sg4_device.cu", "sg4_solvers.cu", "sg4_setup.cpp"]
+SOURCES = ["sg4_device.cu", "sg4_solvers.cu", "sg4_setup.cpp", "sg4_items.cu"]
+# translation units: (source, object, extra flags); the item kernels are
+# compiled once per launch geometry (wide, narrow, mid)
+UNITS = [("sg4_device.cu", "sg4_device.o", []), ("sg4_solvers.cu", "sg4_solvers.o", []),
+         ("sg4_setup.cpp", "sg4_setup.o", [])] + [
+    ("sg4_items.cu", f"sg4_items_g{g}.o", [f"-DEVR_GEO={g}"]) for g in range(3)]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -49,9 +54,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
     cc = nvcc()
     common = ["-O3", "-std=c++17", "-I", INCLUDE, "-I", CSRC, "-Xcompiler", "-fPIC,-O3"]
 
-    def compile_one(src):
-        obj = os.path.join(BUILD, src + ".o")
-        cmd = [cc, "-c", os.path.join(CSRC, src), "-o", obj] + common
+    def compile_one(unit):
+        src, name, flags = unit
+        obj = os.path.join(BUILD, name)
+        cmd = [cc, "-c", os.path.join(CSRC, src), "-o", obj] + common + flags
         if src.endswith(".cu"):
             cmd += ARCH + ["-lineinfo", "-Xptxas", "-v"] if verbose else ARCH + ["-lineinfo"]
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -61,8 +67,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
             print(r.stdout + r.stderr)
         return obj
 
-    with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        objs = list(ex.map(compile_one, SOURCES))
+    with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+        objs = list(ex.map(compile_one, UNITS))
     tmp = LIB + ".tmp"
     cmd = [cc, "-shared", "-o", tmp] + objs + ARCH + ["-lcudart", "-lcublas"]
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -89,797 +89,62 @@ int desc_sizes(const evr_sg4_desc* d, DescSizes* z) {
   return EVR_OK;
 }
 
-// ------------------------------------------------------------------ device
-#ifndef EVR_FUSED_MAXD
-#define EVR_FUSED_MAXD 12  // type-10 items with D <= 12 use the fused grid passes
-#endif
-// Persistent H.psi launch geometry, chosen per work plan.  Wide: four
-// 128-thread CTAs per SM (54.75 KB of shared memory and 128 registers a thread
-// each), fused type-10 passes up to D = 12; it beat two 256-thread CTAs by
-// 0.7 % on the 6-D benchmark and lets the ~600 items of a small operator run
-// in one wave.  Narrow, for D <= 6 and plans of at least EVR_NARROW_WAVES
-// waves of items: EVR_NARROW_CTAS CTAs per SM (26.5 KB and 64 registers
-// each, the fused passes instantiated only up to D = 6): more resident warps
-// keep the FP64 pipe busier on large operators (8 CTAs: +7 % on the 6-D
-// benchmark; 7 and 6 CTAs, and four 256-thread CTAs, are within 3 %), while
-// a small operator's one wave of items finishes sooner with the wide
-// kernel's longer register budget.
-#ifndef EVR_CTA_THREADS
-#define EVR_CTA_THREADS 128
-#endif
-#ifndef EVR_WIDE_CTAS
-#define EVR_WIDE_CTAS 4
-#endif
-#define EVR_WIDE_FMAX 12
-#ifndef EVR_NARROW_CTAS
-#define EVR_NARROW_CTAS 8
-#endif
-#define EVR_NARROW_FMAX 6
-#define EVR_NARROW_WAVES 4
-#ifndef EVR_NARROW_INC
-#define EVR_NARROW_INC 0  // the narrow kernel takes the point digits from divisions
-#endif
+}  // namespace evr
 
-struct TermInfo {
-  long long off_nb;   // into map
-  long long off_nq;   // into the operator fields
-  int nb, nq;
-  int r;              // right-hand sides per work item for this term
-  float cost;
-  double w;           // WeightSG
-  unsigned char l[EVR_MAXD];
-};
+#include "sg4_items.cuh"
 
-struct Item {
-  int term;
-  int rhs0;
-};
+namespace evr {
 
-// a work item of a launch over several contexts (context index first)
-struct MItem {
-  int ctx, term, rhs0, pad;
-};
-
-// 1-D matrices of (mode, level), row-major [nout][nin] for the kernel.
-enum { M_BG = 0, M_GB = 1, M_D1 = 2, M_D2 = 3 };
-
-struct OpFields {
-  int type;
-  const double* V;     // [sum_nq] or NULL
-  const double* G;     // [sum_nq*D*D] (GGiq per term) or NULL = identity
-  const double* Jac;   // [sum_nq] or NULL
-  const double* sqRho; // [sum_nq] or NULL
-  double F2[EVR_MAXD * EVR_MAXD];
-  double F1[EVR_MAXD];
-};
-
-struct KParams {
-  int D, Lp1;
-  int nrhs_v;                // virtual right-hand sides (2*nrhs for complex)
-  int cshift;                // 1 for interleaved complex, else 0
-  const TermInfo* terms;
-  const Item* items;
-  int n_items;
-  int item_base;             // plain path: items [item_base, item_base+gridDim.x)
-  unsigned int* counter;     // batched path: global work counter
-  const int* map;
-  const double* mats;
-  const int* mat_off;        // [D*Lp1*8]: forward set, then transposed set
-  int transpose;             // 1: apply H^T (the adjoint of the real operator)
-  const int* nb_of_l;
-  const int* nq_of_l;
-  const double* psi;
-  long long ldpsi;           // in doubles, already scaled for complex
-  double* hpsi;
-  long long ldh;
-  double scale;              // 1/Esc
-  const double* V;
-  const double* G;
-  const double* Jac;
-  const double* sqRho;
-  const double* F2;          // device [D*D]
-  const double* F1;          // device [D]
-  int type;
-  int nbuf;                  // work arrays per item
-  int smem_doubles;
-  double* gscratch;
-  long long scratch_per_cta; // doubles
-  double* contrib;           // [sum_nb][nrhs_v] weighted term contributions
-  const double* cfac;        // [sum_nq] -1/2/(Jac sqRho) or NULL (= -1/2)
-  long long sum_nb;
-  long long fbase;           // grid point of the first field entry (term slices)
-  int nb0;                   // channels (electronic states): a vector is nb0 blocks of Nfun
-  long long Nfun;            // packed basis functions per channel
-  long long vstride;         // V[(a*nb0 + b)*vstride + point] for nb0 > 1
-};
-
-struct ItemShared {
-  int nb[EVR_MAXD], nq[EVR_MAXD];
-  int ord[EVR_MAXD];          // basis->grid mode order
-  int pos[EVR_MAXD];          // rank of each mode in that order (inverse of ord)
-  int st[EVR_MAXD];           // grid stride of each mode (product of the nq before it)
-  int mo[EVR_MAXD][4];
-  long long off_nb, off_nq;
-  int nb_t, nq_t, r, rhs0, term;
-  double w;
-  double* base;
-};
-
-__device__ __forceinline__ long long vaddr(const KParams& p, int v, int n, long long ld) {
-  // element n (0-based, packed index) of virtual right-hand side v: column
-  // v >> cshift is channel a of right-hand side j (RvecB((a-1)*Max_nDI + n))
-  const int col = v >> p.cshift;
-  const int j = col / p.nb0, a = col - j * p.nb0;
-  return (long long)j * ld + (((long long)a * p.Nfun + n) << p.cshift) + (v & p.cshift);
+// The kernels of launch geometry geo (0 wide, 1 narrow, 2 mid).
+static const GeoKernels& geo_kernels(int geo) {
+  return geo == 1 ? geo_kernels_narrow : (geo == 2 ? geo_kernels_mid : geo_kernels_wide);
 }
 
-// y(j,a) = sum_b V_ab x(j,b) at grid point q for nb0 > 1: the electronic
-// matrix of the operator (OpGrid(iterm)%Grid(:,a,b) of the reference) couples
-// the channels of one right-hand side; the item holds whole channel groups.
-__device__ __forceinline__ double vmat_apply(const KParams& p, const double* xs, int e, int nqt, long long oq,
-                                             int rhs0) {
-  const int q = e % nqt, jj = e / nqt;
-  const int a = ((rhs0 + jj) >> p.cshift) % p.nb0;
-  double y = 0.0;
-  for (int b = 0; b < p.nb0; ++b) {
-    const int jb = jj + ((b - a) << p.cshift);
-    const int ab = p.transpose ? b * p.nb0 + a : a * p.nb0 + b;
-    y = fma(__ldg(p.V + (long long)ab * p.vstride + oq + q), xs[jb * nqt + q], y);
-  }
-  return y;
-}
-
-// out[a + S*(k + nout*b)] (+)= scale * sum_m M[k*NIN+m] in[a + S*(m + NIN*b)]
-// One thread per fibre (a, b); the NIN inputs of the fibre stay in registers,
-// matrix loads are warp-uniform, and four outputs are formed at once as
-// independent FMA chains (GB300's FP64 pipe has a long latency, one chain per
-// warp cannot keep it busy).  MODE 0 stores, 1 adds, 2 adds scale times.
-template <int NIN, int MODE>
-__device__ __forceinline__ void mode_pass_t(const double* __restrict__ M, int nout, int S, int R,
-                                            const double* in, double* out, double scale) {
-  const int nf = S * R;
-  for (int f = threadIdx.x; f < nf; f += blockDim.x) {
-    const int b = f / S, a = f - b * S;
-    const double* fi = in + a + S * NIN * b;
-    double v[NIN];
-#pragma unroll
-    for (int m = 0; m < NIN; ++m) v[m] = fi[S * m];
-    double* fo = out + a + S * nout * b;
-    int k = 0;
-    for (; k + 4 <= nout; k += 4) {
-      const double* M0 = M + k * NIN;
-      double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
-#pragma unroll
-      for (int m = 0; m < NIN; ++m) {
-        s0 = fma(__ldg(M0 + m), v[m], s0);
-        s1 = fma(__ldg(M0 + NIN + m), v[m], s1);
-        s2 = fma(__ldg(M0 + 2 * NIN + m), v[m], s2);
-        s3 = fma(__ldg(M0 + 3 * NIN + m), v[m], s3);
-      }
-      if (MODE == 0) {
-        fo[S * k] = s0; fo[S * (k + 1)] = s1; fo[S * (k + 2)] = s2; fo[S * (k + 3)] = s3;
-      } else if (MODE == 1) {
-        fo[S * k] += s0; fo[S * (k + 1)] += s1; fo[S * (k + 2)] += s2; fo[S * (k + 3)] += s3;
-      } else {
-        fo[S * k] = fma(scale, s0, fo[S * k]);
-        fo[S * (k + 1)] = fma(scale, s1, fo[S * (k + 1)]);
-        fo[S * (k + 2)] = fma(scale, s2, fo[S * (k + 2)]);
-        fo[S * (k + 3)] = fma(scale, s3, fo[S * (k + 3)]);
-      }
-    }
-    for (; k < nout; ++k) {
-      const double* Mk = M + k * NIN;
-      double s0 = 0.0;
-#pragma unroll
-      for (int m = 0; m < NIN; ++m) s0 = fma(__ldg(Mk + m), v[m], s0);
-      if (MODE == 0) fo[S * k] = s0;
-      else if (MODE == 1) fo[S * k] += s0;
-      else fo[S * k] = fma(scale, s0, fo[S * k]);
-    }
-  }
-}
-
-// Few fibres (when one thread per fibre leaves a longer critical path than
-// one thread per output element): one thread per output element, so the
-// threads share the pass evenly.  Each output is one FMA chain over the
-// fibre's inputs in the same order as above, so the bits are the same.  The
-// typical basis<->grid pass of a small term has one or two fibres per
-// thread; splitting made the 6-D benchmark 4.8 % faster.
-template <int NIN, int MODE>
-__device__ __forceinline__ void mode_pass_split(const double* __restrict__ M, int nout, int S, int R,
-                                                const double* in, double* out, double scale) {
-  const int nf = S * R;
-  for (int u = threadIdx.x; u < nf * nout; u += blockDim.x) {
-    const int k = u / nf, f = u - k * nf;
-    const int b = f / S, a = f - b * S;
-    const double* fi = in + a + S * NIN * b;
-    const double* Mk = M + k * NIN;
-    double s0 = 0.0;
-#pragma unroll
-    for (int m = 0; m < NIN; ++m) s0 = fma(__ldg(Mk + m), fi[S * m], s0);
-    double* fo = out + a + S * (k + nout * b);
-    if (MODE == 0) *fo = s0;
-    else if (MODE == 1) *fo += s0;
-    else *fo = fma(scale, s0, *fo);
-  }
-}
-
-template <int MODE>
-__device__ __noinline__ void mode_pass_m(const double* M, int nin, int nout, int S, int R, const double* in, double* out,
-                            double scale) {
-  const int nf = S * R, T = blockDim.x;
-  if (nout > 1 && (nf * nout + T - 1) / T < ((nf + T - 1) / T) * nout) {
-    switch (nin) {
-#define EVR_CASE(n) \
-  case n:           \
-    mode_pass_split<n, MODE>(M, nout, S, R, in, out, scale); return;
-      EVR_CASE(1) EVR_CASE(2) EVR_CASE(3) EVR_CASE(4) EVR_CASE(5) EVR_CASE(6) EVR_CASE(7) EVR_CASE(8)
-      EVR_CASE(9) EVR_CASE(10) EVR_CASE(11) EVR_CASE(12) EVR_CASE(13) EVR_CASE(14) EVR_CASE(15) EVR_CASE(16)
-#undef EVR_CASE
-      default: return;
-    }
-  }
-  switch (nin) {
-#define EVR_CASE(n) \
-  case n:           \
-    mode_pass_t<n, MODE>(M, nout, S, R, in, out, scale); break;
-    EVR_CASE(1) EVR_CASE(2) EVR_CASE(3) EVR_CASE(4) EVR_CASE(5) EVR_CASE(6) EVR_CASE(7) EVR_CASE(8)
-    EVR_CASE(9) EVR_CASE(10) EVR_CASE(11) EVR_CASE(12) EVR_CASE(13) EVR_CASE(14) EVR_CASE(15) EVR_CASE(16)
-#undef EVR_CASE
-    default: break;
-  }
-}
-
-__device__ void mode_pass(const double* M, int nin, int nout, int S, int R, const double* in, double* out,
-                          bool acc, double scale) {
-  if (!acc) mode_pass_m<0>(M, nin, nout, S, R, in, out, 1.0);
-  else if (scale == 1.0) mode_pass_m<1>(M, nin, nout, S, R, in, out, 1.0);
-  else mode_pass_m<2>(M, nin, nout, S, R, in, out, scale);
-}
-
-// Derivative pass along mode i on the grid (DerivOp_TO_RDP_OF_SmolaykRep).
-__device__ void grid_deriv(const KParams& p, const ItemShared& it, int i, int which, const double* in,
-                           double* out, bool acc, double scale) {
-  int S = 1, R = it.r;
-  for (int j = 0; j < p.D; ++j) {
-    if (j < i) S *= it.nq[j];
-    else if (j > i) R *= it.nq[j];
-  }
-  mode_pass(p.mats + it.mo[i][which], it.nq[i], it.nq[i], S, R, in, out, acc, scale);
-}
-
-// basis->grid (to_grid, BDP_TO_GDP) or grid->basis (GDP_TO_BDP).  The
-// reference applies modes 1..D; the product of 1-D maps commutes, so the
-// modes are taken in the order that minimises multiply-adds: basis->grid in
-// ascending (nq-nb)/(nb*nq) (the modes that grow the array most go last),
-// grid->basis in the reverse order (they shrink it first).
-// The extents of the other modes at step k follow from their ranks in the
-// order (a mode already passed has its output size), read from the item's
-// shared block rather than kept in a per-thread array.
-__device__ double* transform(const KParams& p, const ItemShared& it, bool to_grid, double* a, double* b) {
-  for (int k = 0; k < p.D; ++k) {
-    const int i = it.ord[to_grid ? k : p.D - 1 - k];
-    const int nin = to_grid ? it.nb[i] : it.nq[i];
-    const int nout = to_grid ? it.nq[i] : it.nb[i];
-    int S = 1, R = it.r;
-    for (int j = 0; j < p.D; ++j) {
-      const bool done = to_grid ? it.pos[j] < k : it.pos[j] > p.D - 1 - k;
-      const int c = (done == to_grid) ? it.nq[j] : it.nb[j];
-      if (j < i) S *= c;
-      else if (j > i) R *= c;
-    }
-    mode_pass(p.mats + it.mo[i][to_grid ? M_BG : M_GB], nin, nout, S, R, a, b, false, 1.0);
-    __syncthreads();
-    double* t = a;
-    a = b;
-    b = t;
-  }
-  return a;
-}
-
-// Type-10 grid operator in two fused passes over the grid points of an item
-// (D <= 12):
-//   pass A, per point: phi_j = (d_j x)(point) for every mode j (D independent
-//     FMA chains over the mode fibres through the point), then
-//     U_i = Jac sum_j G_ji phi_j, stored;
-//   pass B, per point: O = c * sum_i (d_i U_i)(point) + O  (O holds V.x), or,
-//     without Jac and rho, O = V.x - 1/2 sum_i (d_i U_i)(point) written over x.
-// The reference applies d_j to the whole grid mode by mode
-// (DerivOp_TO_RDP_OF_SmolaykRep); the same products, with two barriers
-// instead of 2D+2 and no phi arrays.  For H^T the matrices are transposed
-// and c (= -1/2/(Jac s)) and s trade places (done by the caller).
-// Position of element e = j*nqt + q of an item (q's digits along the modes,
-// mode 1 fastest, and the right-hand side j), advanced by a fixed stride with
-// mixed-radix carries so the loops over the grid do no integer division.
-template <int DD>
-struct GridPos {
-  int dig[DD], sdig[DD];
-  int e, j, sj;
-  __device__ __forceinline__ void init(const int* nq, int nqt, int e0, int stride) {
-    e = e0;
-    j = e0 / nqt;
-    int q = e0 - j * nqt;
-    sj = stride / nqt;
-    int s = stride - sj * nqt;
-#pragma unroll
-    for (int i = 0; i < DD; ++i) {
-      dig[i] = q % nq[i];
-      q /= nq[i];
-      sdig[i] = s % nq[i];
-      s /= nq[i];
-    }
-  }
-  __device__ __forceinline__ void advance(const int* nq, int stride) {
-    e += stride;
-    int carry = 0;
-#pragma unroll
-    for (int i = 0; i < DD; ++i) {
-      const int d = dig[i] + sdig[i] + carry;  // <= 2 nq - 1
-      carry = d >= nq[i];
-      dig[i] = carry ? d - nq[i] : d;
-    }
-    j += sj + carry;
-  }
-};
-
-// The point's digits come from GridPos (INC, fewer instructions) or from
-// divisions of the element index (fewer registers: the narrow geometry's
-// 64-register budget spills less without the digit arrays).
-template <int DD, bool INC, class MS>
-__device__ __forceinline__ void point_digits(GridPos<DD>& gp, const MS& ms, int nqt, int e, int* idx, int& q) {
-  if constexpr (INC) {
-    q = e - gp.j * nqt;
-#pragma unroll
-    for (int i = 0; i < DD; ++i) idx[i] = gp.dig[i];
-  } else {
-    q = e % nqt;
-    int rem = q;
-#pragma unroll
-    for (int i = 0; i < DD; ++i) {
-      const int n = ms.nq(i);
-      idx[i] = rem % n;
-      rem /= n;
-    }
-  }
-}
-
-// Per-mode sizes, grid strides and derivative matrices: in registers for the
-// wide geometry, read from the item's shared block for the narrow one (its
-// 64-register budget cannot hold 4 D values beside the point's digits and
-// the D partial sums; spilled copies would live in local memory that the
-// full shared-memory carve-out leaves almost no L1 for).
-template <int DD, bool REG>
-struct ModeSizes;
-template <int DD>
-struct ModeSizes<DD, true> {
-  int nq_[DD], st_[DD];
-  const double* Md_[DD];
-  __device__ __forceinline__ ModeSizes(const KParams& p, const ItemShared& it) {
-#pragma unroll
-    for (int i = 0; i < DD; ++i) {
-      nq_[i] = it.nq[i];
-      st_[i] = it.st[i];
-      Md_[i] = p.mats + it.mo[i][M_D1];
-    }
-  }
-  __device__ __forceinline__ int nq(int i) const { return nq_[i]; }
-  __device__ __forceinline__ int st(int i) const { return st_[i]; }
-  __device__ __forceinline__ const double* Md(int i) const { return Md_[i]; }
-};
-template <int DD>
-struct ModeSizes<DD, false> {
-  const volatile ItemShared& it;
-  const double* mats;
-  __device__ __forceinline__ ModeSizes(const KParams& p, const ItemShared& s) : it(s), mats(p.mats) {}
-  __device__ __forceinline__ int nq(int i) const { return it.nq[i]; }
-  __device__ __forceinline__ int st(int i) const { return it.st[i]; }
-  __device__ __forceinline__ const double* Md(int i) const { return mats + it.mo[i][M_D1]; }
-};
-
-template <int DD, bool INC>
-__device__ void type10_fused(const KParams& p, const ItemShared& it, const double* x, double* O, double* U,
-                             int NQR, bool inplace) {
-  const int nqt = it.nq_t;
-  const long long oq = it.off_nq;
-  const ModeSizes<DD, INC> ms(p, it);
-  const long long GD = (long long)DD * DD;
-  const long long si = p.transpose ? nqt : (long long)nqt * DD;  // G offset step of the output index
-  const long long sj = p.transpose ? (long long)nqt * DD : nqt;  // ... and of the input index
-  GridPos<DD> gp;
-  if constexpr (INC) gp.init(ms.nq_, nqt, threadIdx.x, blockDim.x);
-  for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
-    int idx[DD], q;
-    point_digits<DD, INC>(gp, ms, nqt, e, idx, q);
-    if constexpr (INC) gp.advance(ms.nq_, blockDim.x);
-    const double* xr = x + (e - q);
-    double phi[DD];
-#pragma unroll
-    for (int j = 0; j < DD; ++j) {
-      const int n = ms.nq(j), sd = ms.st(j);
-      const double* fib = xr + (q - idx[j] * sd);
-      const double* row = ms.Md(j) + idx[j] * n;
-      double a = 0.0;
-      for (int m = 0; m < n; ++m) a = fma(__ldg(row + m), fib[m * sd], a);
-      phi[j] = a;
-    }
-    const double jac = p.Jac ? __ldg(p.Jac + oq + q) : 1.0;
-    const double* g = p.G ? p.G + oq * GD + q : nullptr;
-#pragma unroll
-    for (int i = 0; i < DD; ++i) {
-      double u;
-      if (g) {
-        u = 0.0;
-#pragma unroll
-        for (int j = 0; j < DD; ++j) u = fma(__ldg(g + si * i + sj * j), phi[j], u);
-      } else {
-        u = phi[i];
-      }
-      U[(long long)i * NQR + e] = p.Jac ? u * jac : u;
-    }
-  }
-  __syncthreads();
-  if constexpr (INC) gp.init(ms.nq_, nqt, threadIdx.x, blockDim.x);
-  for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
-    int idx[DD], q;
-    point_digits<DD, INC>(gp, ms, nqt, e, idx, q);
-    if constexpr (INC) gp.advance(ms.nq_, blockDim.x);
-    // one FMA chain over the fibres of every mode (no partial sums to add:
-    // the FP64 pipe, not latency, bounds the kernel)
-    double sum = 0.0;
-#pragma unroll
-    for (int i = 0; i < DD; ++i) {
-      const int n = ms.nq(i), sd = ms.st(i);
-      const double* fib = U + (long long)i * NQR + (e - idx[i] * sd);
-      const double* row = ms.Md(i) + idx[i] * n;
-      for (int m = 0; m < n; ++m) sum = fma(__ldg(row + m), fib[m * sd], sum);
-    }
-    if (inplace) {  // O is x: V.x + (-1/2) sum, both directions
-      const double vx = p.V ? __ldg(p.V + oq + q) * O[e] : 0.0;
-      O[e] = fma(-0.5, sum, vx);
-    } else {
-      const double cf = !p.transpose ? (p.cfac ? __ldg(p.cfac + oq + q) : -0.5)
-                                     : (p.sqRho ? __ldg(p.sqRho + oq + q) : 1.0);
-      O[e] = fma(cf, sum, O[e]);
-    }
-  }
-  __syncthreads();
-}
-
-template <int FMAX>
-__device__ void type10_fused_dispatch(const KParams& p, const ItemShared& it, const double* x, double* O, double* U,
-                                      int NQR, bool inplace) {
-  switch (p.D) {
-#define EVR_T10(n)                                                        \
-  case n:                                                                 \
-    if constexpr (n <= FMAX)                                              \
-      type10_fused<n, (FMAX > EVR_NARROW_FMAX) || EVR_NARROW_INC>(p, it, x, O, U, NQR, inplace); \
-    break;
-    EVR_T10(1) EVR_T10(2) EVR_T10(3) EVR_T10(4) EVR_T10(5) EVR_T10(6) EVR_T10(7) EVR_T10(8) EVR_T10(9)
-    EVR_T10(10) EVR_T10(11) EVR_T10(12)
-#undef EVR_T10
-    default: break;
-  }
-}
-
-// The weighted term result WeightSG(l) * y_b goes to contrib[off_nb + k][v]
-// (no atomics); the two reduce kernels add the contributions of each packed
-// function in Smolyak-term order, as tabR_AT_iG_TO_tabPackedBasis
-// accumulates them (sub_module_basis_BtoG_GtoB_SG4.f90:1255-1294).
-__device__ void store_contrib(const KParams& p, const ItemShared& it, const double* yb) {
-  const int nbt = it.nb_t;
-  const double wt = it.w;
-  const int* map = p.map + it.off_nb;
-  const int r = it.r;
-  for (int e = threadIdx.x; e < nbt * r; e += blockDim.x) {
-    const int k = e / r, j = e - k * r;
-    if (__ldg(map + k) > 0) p.contrib[(it.off_nb + k) * p.nrhs_v + it.rhs0 + j] = wt * yb[j * nbt + k];
-  }
-  __syncthreads();
-}
-
-template <int FMAX>
-__device__ void run_item(const KParams& p, ItemShared& it, double* smem, int term, int rhs0) {
-  if (threadIdx.x == 0) {
-    const TermInfo& T = p.terms[term];
-    it.term = term;
-    it.rhs0 = rhs0;
-    it.r = min(T.r, p.nrhs_v - rhs0);
-    it.off_nb = T.off_nb;
-    it.off_nq = T.off_nq - p.fbase;
-    it.nb_t = T.nb;
-    it.nq_t = T.nq;
-    it.w = T.w;
-    long long need = (long long)p.nbuf * T.nq * it.r;
-    it.base = (need <= p.smem_doubles) ? smem : p.gscratch + (long long)blockIdx.x * p.scratch_per_cta;
-  }
-  if (threadIdx.x < p.D) {
-    const int i = threadIdx.x;
-    const int l = p.terms[term].l[i];
-    const int k = i * p.Lp1 + l;
-    it.nb[i] = p.nb_of_l[k];
-    it.nq[i] = p.nq_of_l[k];
-    for (int q = 0; q < 4; ++q) it.mo[i][q] = p.mat_off[k * 8 + 4 * p.transpose + q];
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {  // insertion sort of the modes by (nq-nb)/(nb*nq), ties by index
-    for (int i = 0; i < p.D; ++i) {
-      int j = i;
-      const int ni = it.nq[i] - it.nb[i], di = it.nb[i] * it.nq[i];
-      while (j > 0) {
-        const int o = it.ord[j - 1];
-        // key(o) <= key(i)  <=>  (nq_o-nb_o) nb_i nq_i <= (nq_i-nb_i) nb_o nq_o  (integers)
-        if ((it.nq[o] - it.nb[o]) * di <= ni * (it.nb[o] * it.nq[o])) break;
-        it.ord[j] = o;
-        --j;
-      }
-      it.ord[j] = i;
-    }
-    int stride = 1;
-    for (int k = 0; k < p.D; ++k) {
-      it.pos[it.ord[k]] = k;
-      it.st[k] = stride;
-      stride *= it.nq[k];
-    }
-  }
-  __syncthreads();
-  const int D = p.D, r = it.r, nbt = it.nb_t, nqt = it.nq_t;
-  const int NQR = nqt * r;
-  double* buf = it.base;
-  double* X = buf;
-  double* T = buf + NQR;
-  const int* map = p.map + it.off_nb;
-
-  // gather (tabPackedBasis_TO_tabR_AT_iG) into the buffer from which the D
-  // ping-pong passes of basis->grid end in X
-  double* G0 = (D & 1) ? T : X;
-  for (int e = threadIdx.x; e < nbt * r; e += blockDim.x) {
-    const int j = e / nbt, k = e - j * nbt;
-    int n = __ldg(map + k);
-    G0[e] = n > 0 ? p.psi[vaddr(p, it.rhs0 + j, n - 1, p.ldpsi)] : 0.0;
-  }
-  __syncthreads();
-  double* x = transform(p, it, true, G0, G0 == X ? T : X);
-  double* y;
-  const long long oq = it.off_nq;
-
-  if (p.type == 0) {
-    // CASE 0: y = V.x
-    if (p.nb0 == 1) {
-      for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
-        const int q = e % nqt;
-        x[e] = (p.V ? __ldg(p.V + oq + q) : 0.0) * x[e];
-      }
-      y = x;
-    } else {  // channel coupling: into the other transform buffer
-      y = (x == X) ? T : X;
-      for (int e = threadIdx.x; e < NQR; e += blockDim.x) y[e] = p.V ? vmat_apply(p, x, e, nqt, oq, it.rhs0) : 0.0;
-    }
-    __syncthreads();
-  } else if (p.type == 1) {
-    // CASE 1: y = V.x + sum F2_ij d_i d_j x + sum F1_i d_i x
-    double* Y = buf + 2 * NQR;
-    double* C = buf + 3 * NQR;
-    for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
-      const int q = e % nqt;
-      Y[e] = !p.V ? 0.0 : (p.nb0 == 1 ? __ldg(p.V + oq + q) * x[e] : vmat_apply(p, x, e, nqt, oq, it.rhs0));
-    }
-    __syncthreads();
-    for (int i = 0; i < D; ++i)
-      for (int j = i; j < D; ++j) {
-        double f = p.F2[i * D + j];
-        if (f == 0.0) continue;
-        if (i == j) {
-          grid_deriv(p, it, i, M_D2, x, Y, true, f);
-        } else {
-          grid_deriv(p, it, i, M_D1, x, C, false, 1.0);
-          __syncthreads();
-          grid_deriv(p, it, j, M_D1, C, Y, true, f);
-        }
-        __syncthreads();
-      }
-    for (int i = 0; i < D; ++i) {
-      double f = p.F1[i];
-      if (f == 0.0) continue;
-      grid_deriv(p, it, i, M_D1, x, Y, true, f);
-      __syncthreads();
-    }
-    y = Y;
-  } else if (D <= FMAX) {
-    // CASE 10 through the fused grid passes; x is in X.  Without Jac and rho
-    // (D + 1 arrays) U_1..U_D follow X and pass B writes O = V.x + c.sum over
-    // x itself (each point is read and written by one thread; the -1/2 of
-    // H^T is applied there too: scaling by -1/2 is exact, so the result is
-    // the same bits as scaling x first).  Otherwise x is rescaled in place
-    // and O = V.x starts in T, with U_1..U_D after it (D + 2 arrays).
-    const bool inplace = p.nbuf == D + 1;
-    double* O = inplace ? x : T;
-    double* U = buf + (inplace ? 1 : 2) * NQR;
-    if (!inplace) {
-      for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
-        const int q = e % nqt;
-        const double xv = x[e];
-        O[e] = p.V ? __ldg(p.V + oq + q) * xv : 0.0;
-        if (!p.transpose) {
-          if (p.sqRho) x[e] = xv * __ldg(p.sqRho + oq + q);
-        } else {
-          x[e] = xv * (p.cfac ? __ldg(p.cfac + oq + q) : -0.5);
-        }
-      }
-      __syncthreads();
-    }
-    type10_fused_dispatch<FMAX>(p, it, x, O, U, NQR, inplace);
-    double* yb = transform(p, it, false, O, inplace ? buf + NQR : x);
-    store_contrib(p, it, yb);
-    return;
-  } else {
-    // CASE 10: -1/2 sum_i d_i(Jac sum_j G_ji d_j(s x)) / (Jac s) + V x
-    double* VX = buf + 2 * NQR;
-    double* O = buf + 3 * NQR;
-    double* Phi = buf + 4 * NQR;
-    // forward: s.x first and -1/2/(Jac s) last; H^T swaps the two scalings
-    for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
-      const int q = e % nqt;
-      double xv = x[e];
-      VX[e] = p.V ? __ldg(p.V + oq + q) * xv : 0.0;
-      if (!p.transpose) {
-        if (p.sqRho) x[e] = xv * __ldg(p.sqRho + oq + q);
-      } else {
-        x[e] = xv * (p.cfac ? __ldg(p.cfac + oq + q) : -0.5);
-      }
-    }
-    __syncthreads();
-    for (int j = 0; j < D; ++j) grid_deriv(p, it, j, M_D1, x, Phi + (long long)j * NQR, false, 1.0);
-    __syncthreads();
-    double* U = x;  // s.x is no longer needed
-    const long long GD = (long long)D * D;
-    for (int i = 0; i < D; ++i) {
-      for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
-        const int q = e % nqt;
-        double u = 0.0;
-        if (p.G) {
-          // output i, input j: G_ji = GGiq(q, j, i) forward, G_ij for H^T
-          const double* g = p.G + oq * GD + q;
-          const long long si = p.transpose ? nqt : (long long)nqt * D;
-          const long long sj = p.transpose ? (long long)nqt * D : nqt;
-          for (int j = 0; j < D; ++j)
-            u = fma(__ldg(g + si * i + sj * j), Phi[(long long)j * NQR + e], u);
-        } else {
-          u = Phi[(long long)i * NQR + e];
-        }
-        if (p.Jac) u *= __ldg(p.Jac + oq + q);
-        U[e] = u;
-      }
-      __syncthreads();
-      grid_deriv(p, it, i, M_D1, U, O, i > 0, 1.0);
-      __syncthreads();
-    }
-    // -1/2 O / (Jac s) + V x, with -1/2/(Jac s) formed once per operator
-    for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
-      const int q = e % nqt;
-      const double cf = !p.transpose ? (p.cfac ? __ldg(p.cfac + oq + q) : -0.5)
-                                     : (p.sqRho ? __ldg(p.sqRho + oq + q) : 1.0);
-      O[e] = fma(cf, O[e], VX[e]);
-    }
-    __syncthreads();
-    y = O;
-    // G->B ping-pongs between O and U
-    double* yb = transform(p, it, false, O, U);
-    store_contrib(p, it, yb);
-    return;
-  }
-  double* other = (y == X) ? T : X;
-  if (p.type == 1) other = (x == X) ? X : T;  // x is free after the operator
-  double* yb = transform(p, it, false, y, other);
-  store_contrib(p, it, yb);
-}
-
-template <int MINB, int FMAX>
-__global__ void __launch_bounds__(EVR_CTA_THREADS, MINB) hpsi_batched_kernel(KParams p) {
-  extern __shared__ double smem[];
-  __shared__ ItemShared it;
-  __shared__ int next;
-  for (;;) {
-    if (threadIdx.x == 0) next = (int)atomicAdd(p.counter, 1u);
-    __syncthreads();
-    int idx = next;
-    __syncthreads();
-    if (idx >= p.n_items) break;
-    const Item itm = p.items[idx];
-    run_item<FMAX>(p, it, smem, itm.term, itm.rhs0);
-  }
-}
-
-// Items of several contexts in one launch: each item names its context,
-// whose parameter block is copied to shared memory before the item runs.
-// With a counter the CTAs pull items until the list is empty; without one
-// (the per-term path) CTA b runs item item_base + b.
-template <int MINB, int FMAX>
-__global__ void __launch_bounds__(EVR_CTA_THREADS, MINB) hpsi_multi_kernel(const KParams* __restrict__ ps,
-                                                              const MItem* __restrict__ items, int n_items,
-                                                              int item_base, unsigned int* counter) {
-  extern __shared__ double smem[];
-  __shared__ ItemShared it;
-  __shared__ KParams sp;
-  __shared__ int next;
-  for (int round = 0;; ++round) {
-    if (threadIdx.x == 0) next = counter ? (int)atomicAdd(counter, 1u) : (round == 0 ? item_base + (int)blockIdx.x : n_items);
-    __syncthreads();
-    const int idx = next;
-    __syncthreads();
-    if (idx >= n_items) break;
-    const MItem m = items[idx];
-    {
-      const int* src = (const int*)(ps + m.ctx);
-      int* dst = (int*)&sp;
-      for (int w = threadIdx.x; w < (int)(sizeof(KParams) / sizeof(int)); w += blockDim.x) dst[w] = src[w];
-    }
-    __syncthreads();
-    run_item<FMAX>(sp, it, smem, m.term, m.rhs0);
-  }
-}
-
-// the two geometries' kernels (geo 1: narrow, D <= EVR_NARROW_FMAX)
 static void launch_batched(int geo, unsigned grid, size_t smem, cudaStream_t s, const KParams& p) {
-  if (geo) hpsi_batched_kernel<EVR_NARROW_CTAS, EVR_NARROW_FMAX><<<grid, EVR_CTA_THREADS, smem, s>>>(p);
-  else hpsi_batched_kernel<EVR_WIDE_CTAS, EVR_WIDE_FMAX><<<grid, EVR_CTA_THREADS, smem, s>>>(p);
+  geo_kernels(geo).batched(grid, smem, s, p);
 }
 
 static void launch_multi(int geo, unsigned grid, size_t smem, cudaStream_t s, const KParams* ps, const MItem* items,
                          int n_items, int item_base, unsigned int* counter) {
-  if (geo)
-    hpsi_multi_kernel<EVR_NARROW_CTAS, EVR_NARROW_FMAX><<<grid, EVR_CTA_THREADS, smem, s>>>(ps, items, n_items,
-                                                                                           item_base, counter);
-  else
-    hpsi_multi_kernel<EVR_WIDE_CTAS, EVR_WIDE_FMAX><<<grid, EVR_CTA_THREADS, smem, s>>>(ps, items, n_items, item_base,
-                                                                                       counter);
+  geo_kernels(geo).multi(grid, smem, s, ps, items, n_items, item_base, counter);
 }
 
-static int geo_ctas(int geo) { return geo ? EVR_NARROW_CTAS : EVR_WIDE_CTAS; }
+static int geo_ctas(int geo) { return geo_kernels(geo).ctas; }
+
 // Static shared memory plus the 1 KB the driver reserves per CTA, rounded up
-// to 256 bytes (queried once): for the wide geometry the larger of its two
-// item kernels (the field-driven propagation and multi-context plans run the
-// multi-context kernel there; sized for the single-context kernel alone, it
-// kept three CTAs per SM instead of four and the RK4 forward ran 7 % slower);
-// for the narrow one the single-context kernel, whose eight CTAs per SM
-// carry the large operators (a narrow multi-context launch, with its larger
-// parameter block, keeps seven).
-template <class K1, class K2>
-static int slack_of(K1 k1, K2 k2, bool both) {
-  cudaFuncAttributes a, b;
-  if (cudaFuncGetAttributes(&a, k1) != cudaSuccess || cudaFuncGetAttributes(&b, k2) != cudaSuccess) {
-    cudaGetLastError();
-    return 4096;
-  }
-  const size_t st = both ? std::max(a.sharedSizeBytes, b.sharedSizeBytes) : a.sharedSizeBytes;
-  return (int)((st + 1024 + 255) / 256 * 256);
-}
+// to 256 bytes (queried once): for the wide and mid geometries the larger of
+// their two item kernels (the field-driven propagation and multi-context
+// plans run the multi-context kernel there; sized for the single-context
+// kernel alone, it kept three wide CTAs per SM instead of four and the RK4
+// forward ran 8 % slower); for the narrow one the single-context kernel,
+// whose eight CTAs per SM carry the large operators (a narrow multi-context
+// launch, with its larger parameter block, keeps seven).
 static int smem_slack(int geo) {
-  static const int wide = slack_of(hpsi_batched_kernel<EVR_WIDE_CTAS, EVR_WIDE_FMAX>,
-                                   hpsi_multi_kernel<EVR_WIDE_CTAS, EVR_WIDE_FMAX>, true);
-  static const int narrow = slack_of(hpsi_batched_kernel<EVR_NARROW_CTAS, EVR_NARROW_FMAX>,
-                                     hpsi_multi_kernel<EVR_NARROW_CTAS, EVR_NARROW_FMAX>, false);
-  return geo ? narrow : wide;
+  static const std::vector<int> slack = [] {
+    std::vector<int> v(3, 4096);
+    for (int g = 0; g < 3; ++g) {
+      size_t b = 0, m = 0;
+      if (geo_kernels(g).static_smem(&b, &m) != cudaSuccess) {
+        cudaGetLastError();
+        continue;
+      }
+      const size_t st = g == 1 ? b : std::max(b, m);
+      v[g] = (int)((st + 1024 + 255) / 256 * 256);
+    }
+    return v;
+  }();
+  return slack[geo];
 }
 
 // dynamic shared memory per CTA: the SM's 228 KB split between the resident
-// CTAs, less the slack above, so all of them fit (54.75 KB wide, 26.5 KB narrow)
+// CTAs, less the slack above, so all of them fit (54.75 KB wide, 26.5 KB
+// narrow, 35.75 KB mid)
 static int geo_smem_bytes(int geo) { return (228 * 1024 / geo_ctas(geo) - smem_slack(geo)) / 256 * 256; }
 
 // dynamic shared memory of every geometry's kernels (set at context creation)
 static cudaError_t set_smem_attributes() {
   cudaError_t e = cudaSuccess;
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(hpsi_batched_kernel<EVR_WIDE_CTAS, EVR_WIDE_FMAX>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, geo_smem_bytes(0));
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(hpsi_multi_kernel<EVR_WIDE_CTAS, EVR_WIDE_FMAX>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, geo_smem_bytes(0));
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(hpsi_batched_kernel<EVR_NARROW_CTAS, EVR_NARROW_FMAX>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, geo_smem_bytes(1));
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(hpsi_multi_kernel<EVR_NARROW_CTAS, EVR_NARROW_FMAX>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, geo_smem_bytes(1));
+  for (int g = 0; g < 3 && e == cudaSuccess; ++g) e = geo_kernels(g).set_smem(geo_smem_bytes(g));
   return e;
 }
 
@@ -1204,12 +469,17 @@ extern "C" int evr_sg4_create(const evr_sg4_desc* d, evr_sg4_ctx** out) {
     TermInfo& T = c->terms[t];
     memset(&T, 0, sizeof(T));
     long long nb = 1, nq = 1;
+    int mnb[EVR_MAXD], mnq[EVR_MAXD], ord[EVR_MAXD];
     for (int i = 0; i < D; ++i) {
       int l = d->tab_l[t * D + i];
       T.l[i] = (unsigned char)l;
-      nb *= c->nb_of_l[i * Lp1 + l];
-      nq *= c->nq_of_l[i * Lp1 + l];
+      mnb[i] = c->nb_of_l[i * Lp1 + l];
+      mnq[i] = c->nq_of_l[i * Lp1 + l];
+      nb *= mnb[i];
+      nq *= mnq[i];
     }
+    mode_order(mnb, mnq, D, ord);
+    for (int i = 0; i < D; ++i) T.ord[i] = (unsigned char)ord[i];
     T.off_nb = onb;
     T.off_nq = onq;
     T.nb = (int)nb;
@@ -1467,9 +737,11 @@ static void plan_work(const evr_sg4_ctx* c, int nrhs_v, int smem_doubles, std::v
   }
 }
 
-// Geometry of a plan with n_wide items planned for the wide kernel.
+// Geometry of a plan with n_wide items planned for the wide kernel: plans of
+// at least EVR_BIG_WAVES waves go narrow (D <= 6) or mid (D > 6).
 static int choose_geo(int D, size_t n_wide, int num_sms) {
-  return D <= EVR_NARROW_FMAX && n_wide >= (size_t)EVR_NARROW_WAVES * geo_ctas(0) * num_sms ? 1 : 0;
+  if (n_wide < (size_t)EVR_BIG_WAVES * geo_ctas(0) * num_sms) return 0;
+  return D <= EVR_NARROW_FMAX ? 1 : 2;
 }
 
 // The same list sorted by decreasing cost (the persistent kernel then ends
@@ -1747,16 +1019,7 @@ extern "C" int evr_sg4_flops_per_rhs(const evr_sg4_ctx* c, double* flops) {
     // B->G and G->B in the mode order the kernel uses (ascending
     // (nq-nb)/(nb*nq), ties by index; G->B reversed): 2 nin nout flops per fibre
     int ord[EVR_MAXD];
-    for (int i = 0; i < D; ++i) {
-      int j = i;
-      while (j > 0) {
-        const int o = ord[j - 1];
-        if ((nq[o] - nb[o]) * (nb[i] * nq[i]) <= (nq[i] - nb[i]) * (nb[o] * nq[o])) break;
-        ord[j] = o;
-        --j;
-      }
-      ord[j] = i;
-    }
+    mode_order(nb, nq, D, ord);
     double f = 0.0;
     for (int dir = 0; dir < 2; ++dir) {
       int cur[EVR_MAXD];
@@ -1961,7 +1224,7 @@ extern "C" int evr_sg4_hpsi_noalloc(evr_sg4_ctx* c, int nrhs, const double* psi,
 // ------------------------------------------------------------------------
 struct evr_sg4_multi {
   int n = 0, cshift = 0, transpose = 0, grid = 0, smem_doubles = 0;
-  int geo = 1;                   // narrow only when every context is
+  int geo = 0;                   // launch geometry of the merged plan (choose_geo)
   std::vector<evr_sg4_ctx*> ctxs;
   std::vector<int> nrhs_v, type, nbuf;  // per context; type and work arrays per point fix the plan
   std::vector<TermInfo*> d_terms;
@@ -2023,8 +1286,8 @@ extern "C" int evr_sg4_multi_create(int n, evr_sg4_ctx* const* ctxs, const int* 
   std::vector<float> allcost;
   long long max_need = 0;
   auto fail = [&](int rc) { free_multi(m); return rc; };
-  // geometry: narrow only if every context has D <= 6 and the merged wide
-  // plan has enough waves of items
+  // geometry: wide unless the merged wide plan has enough waves of items;
+  // then narrow if every context has D <= 6, else mid
   size_t n_wide = 0;
   int dmax = 0;
   for (int k = 0; k < n; ++k) {
