@@ -469,17 +469,12 @@ extern "C" int evr_sg4_create(const evr_sg4_desc* d, evr_sg4_ctx** out) {
     TermInfo& T = c->terms[t];
     memset(&T, 0, sizeof(T));
     long long nb = 1, nq = 1;
-    int mnb[EVR_MAXD], mnq[EVR_MAXD], ord[EVR_MAXD];
     for (int i = 0; i < D; ++i) {
       int l = d->tab_l[t * D + i];
       T.l[i] = (unsigned char)l;
-      mnb[i] = c->nb_of_l[i * Lp1 + l];
-      mnq[i] = c->nq_of_l[i * Lp1 + l];
-      nb *= mnb[i];
-      nq *= mnq[i];
+      nb *= c->nb_of_l[i * Lp1 + l];
+      nq *= c->nq_of_l[i * Lp1 + l];
     }
-    mode_order(mnb, mnq, D, ord);
-    for (int i = 0; i < D; ++i) T.ord[i] = (unsigned char)ord[i];
     T.off_nb = onb;
     T.off_nq = onq;
     T.nb = (int)nb;
@@ -1068,6 +1063,13 @@ extern "C" int evr_sg4_ctx_sizes(const evr_sg4_ctx* c, long long* out) {
   out[5] = c->z.max_nq;
   out[6] = c->D;
   out[7] = c->L;
+  return EVR_OK;
+}
+
+extern "C" int evr_sg4_last_geometry(const evr_sg4_ctx* c, int* geo, int* ctas_per_sm) {
+  if (!c || !geo) return set_error(EVR_ERR_ARG, "last_geometry: NULL argument");
+  *geo = c->geo;
+  if (ctas_per_sm) *ctas_per_sm = geo_ctas(c->geo);
   return EVR_OK;
 }
 

@@ -57,12 +57,14 @@ struct TermInfo {
   float cost;
   double w;           // WeightSG
   unsigned char l[EVR_MAXD];
-  unsigned char ord[EVR_MAXD];  // basis->grid mode order (mode_order)
 };
 
 // Modes in ascending (nq-nb)/(nb*nq), ties by index (the basis->grid order
 // that minimises multiply-adds; grid->basis runs it backwards).  Integer
 // comparison: key(o) <= key(i) <=> (nq_o-nb_o) nb_i nq_i <= (nq_i-nb_i) nb_o nq_o.
+// The flop count uses it on the host; each work item sorts its modes the
+// same way on the device (one thread, D <= 12: cheaper there than reading a
+// stored order, measured).
 static inline void mode_order(const int* nb, const int* nq, int D, int* ord) {
   for (int i = 0; i < D; ++i) {
     int j = i;
@@ -539,23 +541,35 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ter
     long long need = (long long)p.nbuf * T.nq * it.r;
     it.base = (need <= p.smem_doubles) ? smem : p.gscratch + (long long)blockIdx.x * p.scratch_per_cta;
   }
-  if (threadIdx.x < p.D) {  // one thread per mode; the order comes with the term
+  if (threadIdx.x < p.D) {
     const int i = threadIdx.x;
-    const TermInfo& T = p.terms[term];
-    const int k = i * p.Lp1 + T.l[i];
+    const int l = p.terms[term].l[i];
+    const int k = i * p.Lp1 + l;
     it.nb[i] = p.nb_of_l[k];
     it.nq[i] = p.nq_of_l[k];
     for (int q = 0; q < 4; ++q) it.mo[i][q] = p.mat_off[k * 8 + 4 * p.transpose + q];
-    const int o = T.ord[i];
-    it.ord[i] = o;
-    it.pos[o] = i;
   }
   __syncthreads();
-  if (threadIdx.x < p.D) {  // grid strides (first read after the gather's barrier)
+  if (threadIdx.x == 0) {  // the modes in mode_order, and their grid strides
+    for (int i = 0; i < p.D; ++i) {
+      int j = i;
+      const int ni = it.nq[i] - it.nb[i], di = it.nb[i] * it.nq[i];
+      while (j > 0) {
+        const int o = it.ord[j - 1];
+        if ((it.nq[o] - it.nb[o]) * di <= ni * (it.nb[o] * it.nq[o])) break;
+        it.ord[j] = o;
+        --j;
+      }
+      it.ord[j] = i;
+    }
     int stride = 1;
-    for (int j = 0; j < (int)threadIdx.x; ++j) stride *= it.nq[j];
-    it.st[threadIdx.x] = stride;
+    for (int k = 0; k < p.D; ++k) {
+      it.pos[it.ord[k]] = k;
+      it.st[k] = stride;
+      stride *= it.nq[k];
+    }
   }
+  __syncthreads();
   const int D = p.D, r = it.r, nbt = it.nb_t, nqt = it.nq_t;
   const int NQR = nqt * r;
   double* buf = it.base;

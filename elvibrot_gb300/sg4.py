@@ -111,6 +111,7 @@ def _declare(L):
         "evr_sg4_apply": [vp, ctypes.c_int, ctypes.c_int, vp, ll, vp, ll, ctypes.c_double, ctypes.c_double, vp],
         "evr_sg4_flops_per_rhs": [vp, dp],
         "evr_sg4_last_launches": [vp, ctypes.POINTER(ll)],
+        "evr_sg4_last_geometry": [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)],
         "evr_probe_fp64_peak": [dp],
         "evr_sg4_ctx_sizes": [vp, ctypes.POINTER(ll)],
         "evr_sg4_rk4_field": [vp, vp, ctypes.POINTER(RK4Opts), dp, vp, vp],
@@ -336,6 +337,12 @@ class ParamOp:
         n = ctypes.c_longlong()
         check(lib().evr_sg4_last_launches(self._h, ctypes.byref(n)))
         return n.value
+
+    def last_geometry(self):
+        """(geometry, CTAs per SM) of the current work plan: 0 wide, 1 narrow, 2 mid."""
+        g, c = ctypes.c_int(), ctypes.c_int()
+        check(lib().evr_sg4_last_geometry(self._h, ctypes.byref(g), ctypes.byref(c)))
+        return g.value, c.value
 
     # -- device-pointer calls (torch CUDA tensors, column-major N x nrhs) --
     def hpsi_dev(self, psi, out, E0: float = 0.0, Esc: float = 1.0, stream: int = 0, plain: bool = False,

@@ -237,6 +237,14 @@ int evr_sg4_tune(evr_sg4_ctx* c, int nrhs, int flags, int* best_rmax, double* be
  * length of a vector, nb0 * N. */
 int evr_sg4_ctx_sizes(const evr_sg4_ctx* c, long long* out);
 
+/* Launch geometry of the context's current work plan (the last H.psi's RHS
+ * count): geo 0 = wide (4 CTAs per SM), 1 = narrow (8 per SM; D <= 6 and at
+ * least four waves of items), 2 = mid (6 per SM; D > 6 and at least four
+ * waves).  ctas_per_sm may be NULL.  Replaces no reference interface (the
+ * reference's OpenMP thread count, Tune_SG4threads_HPsi vib.f90:2013-2123,
+ * is the nearest analogue). */
+int evr_sg4_last_geometry(const evr_sg4_ctx* c, int* geo, int* ctas_per_sm);
+
 /* ------------------------------------------------------------------------
  * Callers of the path, on the device.
  * ---------------------------------------------------------------------- */

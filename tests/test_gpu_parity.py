@@ -74,6 +74,34 @@ def check_against_oracle(op, O, kw, psi, label):
     return got
 
 
+def test_launch_geometries_match_oracle_and_each_other():
+    """A 7-D type-10 operator: 24 right-hand sides make a plan of more than
+    four waves of items (the mid geometry, six CTAs per SM), 2 a small one
+    (wide, four per SM); a 6-D operator with 20 takes the narrow geometry.
+    Each geometry runs the same arithmetic, so the values agree bit for bit."""
+    need_cuda()
+    m = make_model(7, 5, 10, 4242)
+    O, kw = oracle_for(m)
+    op = m.operator()
+    psi = random_psi(O.N, 24, 7)
+    got = gpu_apply(op, psi)
+    assert op.last_geometry() == (2, 6)
+    e = rel_err(got, O.hpsi(psi, **kw))
+    print(f"7-D L=5 type 10, 24 RHS (mid geometry): gpu-vs-double {e:.2e}")
+    assert e <= TOL
+    got2 = gpu_apply(op, psi[:, :2])
+    assert op.last_geometry() == (0, 4)
+    assert np.array_equal(got2, got[:, :2])
+    m6 = make_model(6, 7, 10, 4243)
+    op6 = m6.operator()
+    psi6 = random_psi(op6.basis.N, 20, 8)
+    big = gpu_apply(op6, psi6)
+    assert op6.last_geometry() == (1, 8)
+    small = gpu_apply(op6, psi6[:, :1])
+    assert op6.last_geometry() == (0, 4)
+    assert np.array_equal(small, big[:, :1])
+
+
 @pytest.mark.parametrize("D,L,type_op,nrhs", [(3, 6, 1, 1), (3, 6, 1, 5), (4, 5, 10, 7), (6, 4, 10, 3),
                                               (5, 5, 1, 4), (2, 9, 10, 2)])
 def test_hpsi_matches_oracle(D, L, type_op, nrhs):
