@@ -362,14 +362,15 @@ struct evr_sg4_ctx {
 
 // Work arrays per item and grid point.  The fused type-10 passes need x and
 // U_1..U_D, plus a separate V.x array when x is rescaled in place (Jac or rho
-// given): without them pass B writes O over x (D + 1 arrays, so more items
-// keep their arrays in shared memory).
+// given) or when V couples channels (a point's value needs the other
+// channels' x): otherwise pass B writes O over x (D + 1 arrays, so more
+// items keep their arrays in shared memory).
 static int nbuf_for(const evr_sg4_ctx* c) {
   const int D = c->D;
   if (c->type == 0) return 2;
   if (c->type == 1) return 4;
   if (D > EVR_FUSED_MAXD) return D + 4;
-  return (c->d_Jac || c->d_sqRho) ? D + 2 : D + 1;
+  return (c->d_Jac || c->d_sqRho || c->nb0 > 1) ? D + 2 : D + 1;
 }
 
 static void free_ctx(evr_sg4_ctx* c) {
@@ -591,8 +592,7 @@ extern "C" int evr_sg4_set_operator(evr_sg4_ctx* c, const evr_sg4_op_desc* op) {
   c->type = op->type;
   c->items_nrhs = -1;  // work split depends on the operator's buffer count and the slices
   int rc;
-  if (c->nb0 > 1) {  // electronic matrices: V(:, a, b) given on the grid, operators 0 and 1
-    if (op->type == 10) return set_error(EVR_ERR_ARG, "nb0=%d: type_Op 10 needs nb0 = 1", c->nb0);
+  if (c->nb0 > 1) {  // electronic matrices: V(:, a, b) given on the grid
     if (op->V_nterms > 0 && !op->V_grid)
       return set_error(EVR_ERR_ARG, "nb0=%d: pass V as V_grid[nb0*nb0*sum_nq]", c->nb0);
   }
@@ -1031,10 +1031,12 @@ extern "C" int evr_sg4_flops_per_rhs(const evr_sg4_ctx* c, double* flops) {
     double sum_nqi = 0;
     for (int i = 0; i < D; ++i) sum_nqi += nq[i];
     const double q = T.nq;
+    // V.x: one product per point, or a row of the nb0 x nb0 electronic matrix
+    const double vq = c->d_V ? (c->nb0 > 1 ? 2.0 * c->nb0 * q : q) : 0.0;
     if (c->type == 0) {
-      f += q;
+      f += vq;
     } else if (c->type == 1) {
-      f += c->d_V ? q : 0.0;
+      f += vq;
       for (int i = 0; i < D; ++i)
         for (int j = i; j < D; ++j)
           if (c->F2[i * D + j] != 0.0) f += 2.0 * q * (i == j ? nq[i] : nq[i] + nq[j]) + 2.0 * q;
@@ -1044,7 +1046,7 @@ extern "C" int evr_sg4_flops_per_rhs(const evr_sg4_ctx* c, double* flops) {
       f += 4.0 * q * sum_nqi;                       // D derivative passes, twice
       f += c->d_G ? 2.0 * D * D * q : 0.0;           // G contraction
       f += (c->d_Jac ? 2.0 * D * q : 0.0) + (c->d_sqRho ? 2.0 * q : 0.0);
-      f += (c->d_V ? q : 0.0) + 4.0 * q;            // V.x and the final combination
+      f += vq + 2.0 * q;                            // V.x and the final multiply-add
     }
     f += 2.0 * T.nb;                                // weighted scatter
     F += f;
@@ -1224,21 +1226,28 @@ extern "C" int evr_sg4_hpsi_noalloc(evr_sg4_ctx* c, int nrhs, const double* psi,
 // shared by all contexts) and the merged cost-sorted item list; the contexts
 // lend their read-only tables and operator grids.
 // ------------------------------------------------------------------------
+// One persistent launch of a plan: the merged items of its contexts, in one
+// launch geometry.
+struct MGroup {
+  int geo = 0, grid = 0, smem_doubles = 0;
+  std::vector<MItem> sorted;     // its contexts' items, decreasing cost
+  MItem* d_items = nullptr;      // the full list
+  MItem* d_sub = nullptr;        // a filtered list (some contexts skipped)
+  unsigned int* d_counter = nullptr;
+  long long scratch_per_cta = 0;
+};
+
 struct evr_sg4_multi {
-  int n = 0, cshift = 0, transpose = 0, grid = 0, smem_doubles = 0;
-  int geo = 0;                   // launch geometry of the merged plan (choose_geo)
+  int n = 0, cshift = 0, transpose = 0;
   std::vector<evr_sg4_ctx*> ctxs;
   std::vector<int> nrhs_v, type, nbuf;  // per context; type and work arrays per point fix the plan
+  std::vector<int> group;        // per context: its launch group
+  std::vector<MGroup> groups;    // one, or two when D <= 6 contexts fill a narrow launch of their own
   std::vector<TermInfo*> d_terms;
   std::vector<double*> d_contrib;
   std::vector<double*> d_part;
-  double* d_scratch = nullptr;
-  long long scratch_per_cta = 0;
-  std::vector<MItem> sorted;     // all contexts, decreasing cost
-  MItem* d_items = nullptr;      // the full list
-  MItem* d_sub = nullptr;        // a filtered list (some contexts skipped)
+  double* d_scratch = nullptr;   // global-scratch slabs, shared by the groups (launched in turn)
   KParams* d_params = nullptr;
-  unsigned int* d_counter = nullptr;
   long long last_launches = 0;
 };
 
@@ -1255,7 +1264,11 @@ static void free_multi(evr_sg4_multi* m) {
   for (TermInfo* p : m->d_terms) if (p) cudaFree(p);
   for (double* p : m->d_contrib) if (p) cudaFree(p);
   for (double* p : m->d_part) if (p) cudaFree(p);
-  void* ptrs[] = {m->d_scratch, m->d_items, m->d_sub, m->d_params, m->d_counter};
+  for (MGroup& g : m->groups) {
+    void* gp[] = {g.d_items, g.d_sub, g.d_counter};
+    for (void* q : gp) if (q) cudaFree(q);
+  }
+  void* ptrs[] = {m->d_scratch, m->d_params};
   for (void* q : ptrs) if (q) cudaFree(q);
   delete m;
 }
@@ -1284,14 +1297,13 @@ extern "C" int evr_sg4_multi_create(int n, evr_sg4_ctx* const* ctxs, const int* 
   m->d_terms.assign(n, nullptr);
   m->d_contrib.assign(n, nullptr);
   m->d_part.assign(n, nullptr);
-  std::vector<MItem> all;
-  std::vector<float> allcost;
-  long long max_need = 0;
   auto fail = [&](int rc) { free_multi(m); return rc; };
-  // geometry: wide unless the merged wide plan has enough waves of items;
-  // then narrow if every context has D <= 6, else mid
-  size_t n_wide = 0;
-  int dmax = 0;
+  // Launch groups.  The contexts with D <= 6 run narrow in a launch of their
+  // own when their items fill enough waves and other contexts exist;
+  // otherwise one launch takes every context, in the geometry of the merged
+  // wide plan (wide; narrow if every D <= 6, else mid, once it has enough
+  // waves of items).
+  std::vector<size_t> n_wide(n);
   for (int k = 0; k < n; ++k) {
     evr_sg4_ctx* c = ctxs[k];
     std::vector<TermInfo> terms;
@@ -1299,14 +1311,46 @@ extern "C" int evr_sg4_multi_create(int n, evr_sg4_ctx* const* ctxs, const int* 
     std::vector<float> cost;
     long long need = 0;
     plan_work(c, (nrhs[k] * c->nb0) << m->cshift, geo_smem_bytes(0) / 8, terms, items, cost, need);
-    n_wide += items.size();
-    dmax = std::max(dmax, c->D);
+    n_wide[k] = items.size();
   }
-  m->geo = choose_geo(dmax, n_wide, ctxs[0]->num_sms);
-  m->smem_doubles = geo_smem_bytes(m->geo) / 8;
-  m->grid = geo_ctas(m->geo) * ctxs[0]->num_sms;
+  const int sms = ctxs[0]->num_sms;
+  size_t small_items = 0, all_items = 0;
+  int dmax = 0, n_small = 0;
+  for (int k = 0; k < n; ++k) {
+    all_items += n_wide[k];
+    dmax = std::max(dmax, ctxs[k]->D);
+    if (ctxs[k]->D <= EVR_NARROW_FMAX) {
+      small_items += n_wide[k];
+      ++n_small;
+    }
+  }
+  m->group.assign(n, 0);
+  if (n_small > 0 && n_small < n && choose_geo(EVR_NARROW_FMAX, small_items, sms) == 1) {
+    int dbig = 0;
+    for (int k = 0; k < n; ++k)
+      if (ctxs[k]->D > EVR_NARROW_FMAX) {
+        m->group[k] = 1;
+        dbig = std::max(dbig, ctxs[k]->D);
+      }
+    m->groups.resize(2);
+    m->groups[0].geo = 1;
+    m->groups[1].geo = choose_geo(dbig, all_items - small_items, sms);
+  } else {
+    m->groups.resize(1);
+    m->groups[0].geo = choose_geo(dmax, all_items, sms);
+  }
+  const int ng = (int)m->groups.size();
+  std::vector<std::vector<MItem>> all(ng);
+  std::vector<std::vector<float>> allcost(ng);
+  long long scratch_doubles = 0;
+  for (MGroup& g : m->groups) {
+    g.smem_doubles = geo_smem_bytes(g.geo) / 8;
+    g.grid = geo_ctas(g.geo) * sms;
+  }
   for (int k = 0; k < n; ++k) {
     evr_sg4_ctx* c = ctxs[k];
+    const int gk = m->group[k];
+    MGroup& g = m->groups[gk];
     const int nv = (nrhs[k] * c->nb0) << m->cshift;
     m->nrhs_v[k] = nv;
     m->type[k] = c->type;
@@ -1315,11 +1359,11 @@ extern "C" int evr_sg4_multi_create(int n, evr_sg4_ctx* const* ctxs, const int* 
     std::vector<Item> items;
     std::vector<float> cost;
     long long need = 0;
-    plan_work(c, nv, m->smem_doubles, terms, items, cost, need);
-    if (need > m->smem_doubles) max_need = std::max(max_need, need);
+    plan_work(c, nv, g.smem_doubles, terms, items, cost, need);
+    if (need > g.smem_doubles) g.scratch_per_cta = std::max(g.scratch_per_cta, need);
     for (size_t q = 0; q < items.size(); ++q) {
-      all.push_back(MItem{k, items[q].term, items[q].rhs0, 0});
-      allcost.push_back(cost[q]);
+      all[gk].push_back(MItem{k, items[q].term, items[q].rhs0, 0});
+      allcost[gk].push_back(cost[q]);
     }
     if (cudaMalloc(&m->d_terms[k], terms.size() * sizeof(TermInfo)) != cudaSuccess ||
         cudaMemcpy(m->d_terms[k], terms.data(), terms.size() * sizeof(TermInfo), cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -1329,19 +1373,26 @@ extern "C" int evr_sg4_multi_create(int n, evr_sg4_ctx* const* ctxs, const int* 
       return fail(set_error(EVR_ERR_CUDA, "multi_create: device allocation for context %d failed", k));
     }
   }
-  std::vector<int> order(all.size());
-  std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return allcost[a] > allcost[b]; });
-  m->sorted.resize(all.size());
-  for (size_t q = 0; q < order.size(); ++q) m->sorted[q] = all[order[q]];
-  m->scratch_per_cta = max_need;
-  const size_t ni = m->sorted.size();
-  if ((max_need && cudaMalloc(&m->d_scratch, (size_t)max_need * m->grid * 8) != cudaSuccess) ||
-      cudaMalloc(&m->d_items, ni * sizeof(MItem)) != cudaSuccess ||
-      cudaMalloc(&m->d_sub, ni * sizeof(MItem)) != cudaSuccess ||
-      cudaMalloc(&m->d_params, (size_t)n * sizeof(KParams)) != cudaSuccess ||
-      cudaMalloc(&m->d_counter, sizeof(unsigned int)) != cudaSuccess ||
-      cudaMemcpy(m->d_items, m->sorted.data(), ni * sizeof(MItem), cudaMemcpyHostToDevice) != cudaSuccess) {
+  for (int gi = 0; gi < ng; ++gi) {
+    MGroup& g = m->groups[gi];
+    std::vector<int> order(all[gi].size());
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return allcost[gi][a] > allcost[gi][b]; });
+    g.sorted.resize(all[gi].size());
+    for (size_t q = 0; q < order.size(); ++q) g.sorted[q] = all[gi][order[q]];
+    scratch_doubles = std::max(scratch_doubles, g.scratch_per_cta * g.grid);
+    const size_t ni = std::max<size_t>(1, g.sorted.size());
+    if (cudaMalloc(&g.d_items, ni * sizeof(MItem)) != cudaSuccess ||
+        cudaMalloc(&g.d_sub, ni * sizeof(MItem)) != cudaSuccess ||
+        cudaMalloc(&g.d_counter, sizeof(unsigned int)) != cudaSuccess ||
+        cudaMemcpy(g.d_items, g.sorted.data(), g.sorted.size() * sizeof(MItem), cudaMemcpyHostToDevice) !=
+            cudaSuccess) {
+      cudaGetLastError();
+      return fail(set_error(EVR_ERR_CUDA, "multi_create: device allocation failed"));
+    }
+  }
+  if ((scratch_doubles && cudaMalloc(&m->d_scratch, (size_t)scratch_doubles * 8) != cudaSuccess) ||
+      cudaMalloc(&m->d_params, (size_t)n * sizeof(KParams)) != cudaSuccess) {
     cudaGetLastError();
     return fail(set_error(EVR_ERR_CUDA, "multi_create: device allocation failed"));
   }
@@ -1375,33 +1426,40 @@ extern "C" int evr_sg4_multi_hpsi(evr_sg4_multi* m, const double* const* psi, co
       return set_error(EVR_ERR_ARG, "multi_hpsi: Esc of context %d must be finite and non-zero", k);
     KParams& p = params[k];
     p = make_params(c, m->nrhs_v[k], m->cshift, psi[k], ldpsi[k] << m->cshift, hpsi[k], ldh[k] << m->cshift, 1.0);
+    const MGroup& g = m->groups[m->group[k]];
     p.transpose = m->transpose;
-    p.smem_doubles = m->smem_doubles;  // the plan's geometry, not the context's own last plan
+    p.smem_doubles = g.smem_doubles;  // the plan's geometry, not the context's own last plan
     p.terms = m->d_terms[k];
     p.contrib = m->d_contrib[k];
     p.gscratch = m->d_scratch;
-    p.scratch_per_cta = m->scratch_per_cta;
+    p.scratch_per_cta = g.scratch_per_cta;
     p.counter = nullptr;
     p.items = nullptr;
     ++active;
   }
   if (active == 0) return set_error(EVR_ERR_ARG, "multi_hpsi: every context is skipped");
-  const MItem* items = m->d_items;
-  int n_items = (int)m->sorted.size();
-  if (active < m->n) {  // the sorted list without the skipped contexts
-    std::vector<MItem> sub;
-    sub.reserve(m->sorted.size());
-    for (const MItem& q : m->sorted)
-      if (psi[q.ctx]) sub.push_back(q);
-    CUDA_TRY(cudaMemcpyAsync(m->d_sub, sub.data(), sub.size() * sizeof(MItem), cudaMemcpyHostToDevice, s));
-    CUDA_TRY(cudaStreamSynchronize(s));  // `sub` leaves scope
-    items = m->d_sub;
-    n_items = (int)sub.size();
-  }
   CUDA_TRY(cudaMemcpyAsync(m->d_params, params.data(), (size_t)m->n * sizeof(KParams), cudaMemcpyHostToDevice, s));
-  CUDA_TRY(cudaMemsetAsync(m->d_counter, 0, sizeof(unsigned int), s));
-  launch_multi(m->geo, m->grid, (size_t)m->smem_doubles * 8, s, m->d_params, items, n_items, 0, m->d_counter);
-  CUDA_TRY(cudaGetLastError());
+  int launched = 0;
+  for (MGroup& g : m->groups) {  // one after the other: they share the scratch slabs
+    const MItem* items = g.d_items;
+    int n_items = (int)g.sorted.size();
+    if (active < m->n) {  // the sorted list without the skipped contexts
+      std::vector<MItem> sub;
+      sub.reserve(g.sorted.size());
+      for (const MItem& q : g.sorted)
+        if (psi[q.ctx]) sub.push_back(q);
+      if (!sub.empty())
+        CUDA_TRY(cudaMemcpyAsync(g.d_sub, sub.data(), sub.size() * sizeof(MItem), cudaMemcpyHostToDevice, s));
+      CUDA_TRY(cudaStreamSynchronize(s));  // `sub` leaves scope
+      items = g.d_sub;
+      n_items = (int)sub.size();
+    }
+    if (n_items == 0) continue;
+    CUDA_TRY(cudaMemsetAsync(g.d_counter, 0, sizeof(unsigned int), s));
+    launch_multi(g.geo, g.grid, (size_t)g.smem_doubles * 8, s, m->d_params, items, n_items, 0, g.d_counter);
+    CUDA_TRY(cudaGetLastError());
+    ++launched;
+  }
   for (int k = 0; k < m->n; ++k) {
     if (!psi[k]) continue;
     int rc = launch_reduce(m->ctxs[k], m->d_contrib[k], (double2*)m->d_part[k], m->nrhs_v[k], m->cshift, psi[k],
@@ -1410,7 +1468,7 @@ extern "C" int evr_sg4_multi_hpsi(evr_sg4_multi* m, const double* const* psi, co
     if (rc) return rc;
   }
   // `params` is pageable: the copy above is staged before cudaMemcpyAsync returns
-  m->last_launches = 1 + 2LL * active;
+  m->last_launches = launched + 2LL * active;
   return EVR_OK;
 }
 
@@ -1494,26 +1552,27 @@ int evr::field_pair_create(evr_sg4_ctx* a, evr_sg4_ctx* b, int transpose, FieldP
     return set_error(EVR_ERR_CUDA, "field pair: device allocation failed");
   }
   evr_sg4_multi* m = f->m;
+  const MGroup& g = m->groups[0];  // one basis, one launch group
   KParams ps[2];
   for (int k = 0; k < 2; ++k) {
     ps[k] = make_params(cs[k], 2, 1, f->x, 2 * a->N, nullptr, 2 * a->N, 1.0);
     ps[k].transpose = m->transpose;
-    ps[k].smem_doubles = m->smem_doubles;
+    ps[k].smem_doubles = g.smem_doubles;
     ps[k].terms = m->d_terms[k];
     ps[k].contrib = m->d_contrib[k];
     ps[k].gscratch = m->d_scratch;
-    ps[k].scratch_per_cta = m->scratch_per_cta;
+    ps[k].scratch_per_cta = g.scratch_per_cta;
     ps[k].counter = nullptr;
     ps[k].items = nullptr;
   }
   if (cudaMemcpy(m->d_params, ps, sizeof(ps), cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemset(m->d_counter, 0, sizeof(unsigned int)) != cudaSuccess) {
+      cudaMemset(g.d_counter, 0, sizeof(unsigned int)) != cudaSuccess) {
     cudaGetLastError();
     field_pair_destroy(f);
     return set_error(EVR_ERR_CUDA, "field pair: parameter upload failed");
   }
   // enough CTAs for every item, so small operators leave SMs to other streams
-  f->grid = (int)std::min<size_t>((size_t)m->grid, std::max<size_t>(1, m->sorted.size()));
+  f->grid = (int)std::min<size_t>((size_t)g.grid, std::max<size_t>(1, g.sorted.size()));
   *out = f;
   return EVR_OK;
 }
@@ -1530,12 +1589,13 @@ int evr::field_pair_apply(FieldPair* f, void* stream) {
   cudaStream_t s = (cudaStream_t)stream;
   evr_sg4_multi* m = f->m;
   evr_sg4_ctx* c = m->ctxs[0];
-  launch_multi(m->geo, f->grid, (size_t)m->smem_doubles * 8, s, m->d_params, m->d_items, (int)m->sorted.size(), 0,
-               m->d_counter);
+  const MGroup& g = m->groups[0];
+  launch_multi(g.geo, f->grid, (size_t)g.smem_doubles * 8, s, m->d_params, g.d_items, (int)g.sorted.size(), 0,
+               g.d_counter);
   const long long t1 = c->n_chunks * 4;
   const long long b1 = std::max<long long>(1, std::min<long long>((t1 + 255) / 256, 16LL * c->num_sms));
   pair_chunks_kernel<<<(unsigned)b1, 256, 0, s>>>(m->d_contrib[0], m->d_contrib[1], c->d_chunk_q, c->n_chunks,
-                                                 c->d_inv_idx, f->part, m->d_counter);
+                                                 c->d_inv_idx, f->part, g.d_counter);
   CUDA_TRY(cudaGetLastError());
   return EVR_OK;
 }

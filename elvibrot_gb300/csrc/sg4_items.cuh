@@ -638,15 +638,22 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ter
     // x itself (each point is read and written by one thread; the -1/2 of
     // H^T is applied there too: scaling by -1/2 is exact, so the result is
     // the same bits as scaling x first).  Otherwise x is rescaled in place
-    // and O = V.x starts in T, with U_1..U_D after it (D + 2 arrays).
+    // and O = V.x starts in T, with U_1..U_D after it (D + 2 arrays); with
+    // several channels V couples them (VPsi(:,ib0) of the reference, formed
+    // before the rescaling, so in a pass of its own).
     const bool inplace = p.nbuf == D + 1;
     double* O = inplace ? x : T;
     double* U = buf + (inplace ? 1 : 2) * NQR;
     if (!inplace) {
+      if (p.nb0 > 1) {
+        for (int e = threadIdx.x; e < NQR; e += blockDim.x)
+          O[e] = p.V ? vmat_apply(p, x, e, nqt, oq, it.rhs0) : 0.0;
+        __syncthreads();
+      }
       for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
         const int q = e % nqt;
         const double xv = x[e];
-        O[e] = p.V ? __ldg(p.V + oq + q) * xv : 0.0;
+        if (p.nb0 == 1) O[e] = p.V ? __ldg(p.V + oq + q) * xv : 0.0;
         if (!p.transpose) {
           if (p.sqRho) x[e] = xv * __ldg(p.sqRho + oq + q);
         } else {
@@ -664,11 +671,16 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ter
     double* VX = buf + 2 * NQR;
     double* O = buf + 3 * NQR;
     double* Phi = buf + 4 * NQR;
-    // forward: s.x first and -1/2/(Jac s) last; H^T swaps the two scalings
+    // forward: s.x first and -1/2/(Jac s) last; H^T swaps the two scalings;
+    // coupled channels' V.x before the rescaling, in a pass of its own
+    if (p.nb0 > 1) {
+      for (int e = threadIdx.x; e < NQR; e += blockDim.x) VX[e] = p.V ? vmat_apply(p, x, e, nqt, oq, it.rhs0) : 0.0;
+      __syncthreads();
+    }
     for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
       const int q = e % nqt;
       double xv = x[e];
-      VX[e] = p.V ? __ldg(p.V + oq + q) * xv : 0.0;
+      if (p.nb0 == 1) VX[e] = p.V ? __ldg(p.V + oq + q) * xv : 0.0;
       if (!p.transpose) {
         if (p.sqRho) x[e] = xv * __ldg(p.sqRho + oq + q);
       } else {

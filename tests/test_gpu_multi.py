@@ -73,6 +73,35 @@ def test_multi_matches_one_launch_per_context(cplx, transpose):
         assert torch.equal(a, c) and torch.equal(b, c)
 
 
+def test_multi_two_launch_groups():
+    """Contexts with D <= 6 whose items fill a narrow launch run in a launch
+    of their own (eight CTAs per SM), the others in a second one; every
+    context's values are the bits of its own single launch."""
+    need_cuda()
+    ops = [make_model(6, 7, 10, 51).operator(), make_model(7, 4, 1, 52).operator(),
+           make_model(3, 5, 1, 53).operator()]
+    nrhs = [20, 3, 2]
+    psis = [_rand(op, r, False, 60 + k) for k, (op, r) in enumerate(zip(ops, nrhs))]
+    ref = []
+    for op, P in zip(ops, psis):
+        O = torch.empty_like(P)
+        op.hpsi_dev(P, O)
+        ref.append(O)
+    plan = MultiOp(ops, nrhs)
+    outs = [torch.full_like(P, float("nan")) for P in psis]
+    plan.hpsi(psis, outs)
+    torch.cuda.synchronize()
+    assert plan.last_launches() == 2 + 2 * 3
+    for k in range(3):
+        assert torch.equal(outs[k], ref[k]), f"context {k}"
+    # with the 7-D context skipped only the narrow launch runs
+    outs2 = [torch.full_like(P, 7.0) for P in psis]
+    plan.hpsi([psis[0], None, psis[2]], outs2)
+    torch.cuda.synchronize()
+    assert plan.last_launches() == 1 + 2 * 2
+    assert torch.equal(outs2[0], ref[0]) and torch.equal(outs2[2], ref[2]) and torch.all(outs2[1] == 7.0)
+
+
 def test_multi_skips_null_contexts_and_leaves_contexts_usable():
     need_cuda()
     ops = _uneven_ops()[:4]

@@ -131,12 +131,46 @@ def test_three_channels_random_coupling():
         assert np.max(np.abs(out.cpu().numpy().T - want)) / np.max(np.abs(want)) <= 1e-12
 
 
-def test_channels_reject_type10_and_polynomial_v():
+def test_channels_type10_matches_oracle_blocks():
+    """Type 10 with two and three channels: V couples them (the reference's
+    VPsi(:,ib0) = sum_jb0 V(:,ib0,jb0) psi_jb0, formed before the rho
+    rescaling), the G-dependent kinetic operator acts on each channel; with
+    and without Jac/rho (the in-place and separate-V.x layouts)."""
+    need_cuda()
+    from elvibrot_gb300.configs import make_model
+    for D, L, nb0, with_rho in ((3, 4, 2, False), (4, 3, 3, True)):
+        m = make_model(D, L, 10, 4300 + D)
+        basis = SG4Basis(D, L, L, 1, 1, 2, 1, nb0=nb0)
+        O = OracleSG4(D, L, L, 1, 1, 2, 1)
+        Q = O.grid_points()
+        nq = np.prod(O.tables()[0] + 2, axis=1)
+        G = m.G_grid(Q, nq)
+        rng = np.random.default_rng(44 + D)
+        Vm = np.empty((nb0, nb0, len(Q)))
+        for a in range(nb0):
+            for b in range(nb0):
+                c = rng.normal(size=D + 1) * 0.1
+                Vm[a, b] = c[0] + Q @ c[1:] + (0.5 * (Q * Q).sum(axis=1) if a == b else 0.0)
+        extra = {}
+        if with_rho:
+            extra = dict(Jac=1.0 + 0.1 * np.cos(Q.sum(axis=1)), sqRho=1.0 + 0.05 * np.sin(Q[:, 0]))
+        I = np.eye(O.N)
+        Href = np.block([[O.hpsi(I, type_op=10, V=Vm[a, a], G=G, **extra) if a == b else O.hpsi(I, type_op=0, V=Vm[a, b])
+                          for b in range(nb0)] for a in range(nb0)])
+        op = ParamOp(basis, 10, V=Vm.reshape(nb0 * nb0, -1), G=G, **extra)
+        scale = np.max(np.abs(Href))
+        for cplx, tr in ((False, False), (True, False), (False, True)):
+            H = gpu_dense(op, basis.nvec, cplx, tr)
+            ref = Href.T if tr else Href
+            err = np.max(np.abs(H - ref)) / scale
+            print(f"type 10, {D}-D L={L}, nb0={nb0}, rho={with_rho}, cplx={cplx}, transpose={tr}: {err:.2e}")
+            assert err <= 1e-12
+
+
+def test_channels_reject_polynomial_v():
     need_cuda()
     from elvibrot_gb300 import Polynomial
     basis = SG4Basis(3, 3, 3, 1, 1, 2, 1, nb0=2)
-    with pytest.raises(EVRError):
-        ParamOp(basis, 10, V=np.zeros(4 * basis.sum_nq))
     with pytest.raises(EVRError):
         ParamOp(basis, 1, V_poly=Polynomial(np.array([1.0]), np.zeros((1, 3), dtype=np.int32)),
                 F2=-0.5 * np.eye(3))
