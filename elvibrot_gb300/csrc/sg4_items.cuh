@@ -178,6 +178,41 @@ __device__ __forceinline__ double vmat_apply(const KParams& p, const double* xs,
   return y;
 }
 
+// Type-10 prologue with coupled channels: VX = V.x (the electronic matrix
+// of each point applied to the channels of a right-hand side, VPsi(:,ib0)
+// of the reference), then x rescaled in place (by sqRho forward, by the
+// -1/2/(Jac sqRho) factor for H^T), each over the NQR elements of an item.
+// Out of line and separate from the one-channel loop: inlined, it shifted
+// the register allocation of the one-channel kernels (0.6-0.8 % on the 6-D
+// benchmark).
+static __device__ __noinline__ void channels_prologue(const KParams& p, long long oq, int nqt, int rhs0, double* x,
+                                                      double* VX, int NQR) {
+  for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
+    if (!p.V) {
+      VX[e] = 0.0;
+      continue;
+    }
+    const int q = e % nqt, jj = e / nqt;
+    const int a = ((rhs0 + jj) >> p.cshift) % p.nb0;
+    double y = 0.0;
+    for (int b = 0; b < p.nb0; ++b) {
+      const int jb = jj + ((b - a) << p.cshift);
+      const int ab = p.transpose ? b * p.nb0 + a : a * p.nb0 + b;
+      y = fma(__ldg(p.V + (long long)ab * p.vstride + oq + q), x[jb * nqt + q], y);
+    }
+    VX[e] = y;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
+    const int q = e % nqt;
+    if (!p.transpose) {
+      if (p.sqRho) x[e] *= __ldg(p.sqRho + oq + q);
+    } else {
+      x[e] *= p.cfac ? __ldg(p.cfac + oq + q) : -0.5;
+    }
+  }
+}
+
 // out[a + S*(k + nout*b)] (+)= scale * sum_m M[k*NIN+m] in[a + S*(m + NIN*b)]
 // One thread per fibre (a, b); the NIN inputs of the fibre stay in registers,
 // matrix loads are warp-uniform, and four outputs are formed at once as
@@ -646,18 +681,17 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ter
     double* U = buf + (inplace ? 1 : 2) * NQR;
     if (!inplace) {
       if (p.nb0 > 1) {
-        for (int e = threadIdx.x; e < NQR; e += blockDim.x)
-          O[e] = p.V ? vmat_apply(p, x, e, nqt, oq, it.rhs0) : 0.0;
-        __syncthreads();
-      }
-      for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
-        const int q = e % nqt;
-        const double xv = x[e];
-        if (p.nb0 == 1) O[e] = p.V ? __ldg(p.V + oq + q) * xv : 0.0;
-        if (!p.transpose) {
-          if (p.sqRho) x[e] = xv * __ldg(p.sqRho + oq + q);
-        } else {
-          x[e] = xv * (p.cfac ? __ldg(p.cfac + oq + q) : -0.5);
+        channels_prologue(p, oq, nqt, it.rhs0, x, O, NQR);
+      } else {
+        for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
+          const int q = e % nqt;
+          const double xv = x[e];
+          O[e] = p.V ? __ldg(p.V + oq + q) * xv : 0.0;
+          if (!p.transpose) {
+            if (p.sqRho) x[e] = xv * __ldg(p.sqRho + oq + q);
+          } else {
+            x[e] = xv * (p.cfac ? __ldg(p.cfac + oq + q) : -0.5);
+          }
         }
       }
       __syncthreads();
@@ -674,17 +708,17 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ter
     // forward: s.x first and -1/2/(Jac s) last; H^T swaps the two scalings;
     // coupled channels' V.x before the rescaling, in a pass of its own
     if (p.nb0 > 1) {
-      for (int e = threadIdx.x; e < NQR; e += blockDim.x) VX[e] = p.V ? vmat_apply(p, x, e, nqt, oq, it.rhs0) : 0.0;
-      __syncthreads();
-    }
-    for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
-      const int q = e % nqt;
-      double xv = x[e];
-      if (p.nb0 == 1) VX[e] = p.V ? __ldg(p.V + oq + q) * xv : 0.0;
-      if (!p.transpose) {
-        if (p.sqRho) x[e] = xv * __ldg(p.sqRho + oq + q);
-      } else {
-        x[e] = xv * (p.cfac ? __ldg(p.cfac + oq + q) : -0.5);
+      channels_prologue(p, oq, nqt, it.rhs0, x, VX, NQR);
+    } else {
+      for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
+        const int q = e % nqt;
+        double xv = x[e];
+        VX[e] = p.V ? __ldg(p.V + oq + q) * xv : 0.0;
+        if (!p.transpose) {
+          if (p.sqRho) x[e] = xv * __ldg(p.sqRho + oq + q);
+        } else {
+          x[e] = xv * (p.cfac ? __ldg(p.cfac + oq + q) : -0.5);
+        }
       }
     }
     __syncthreads();
@@ -759,7 +793,6 @@ __global__ void __launch_bounds__(EVR_CTA_THREADS, MINB) hpsi_multi_kernel(const
                                                               int item_base, unsigned int* counter) {
   extern __shared__ double smem[];
   __shared__ ItemShared it;
-  __shared__ KParams sp;
   __shared__ int next;
   for (int round = 0;; ++round) {
     if (threadIdx.x == 0) next = counter ? (int)atomicAdd(counter, 1u) : (round == 0 ? item_base + (int)blockIdx.x : n_items);
@@ -768,13 +801,12 @@ __global__ void __launch_bounds__(EVR_CTA_THREADS, MINB) hpsi_multi_kernel(const
     __syncthreads();
     if (idx >= n_items) break;
     const MItem m = items[idx];
-    {
-      const int* src = (const int*)(ps + m.ctx);
-      int* dst = (int*)&sp;
-      for (int w = threadIdx.x; w < (int)(sizeof(KParams) / sizeof(int)); w += blockDim.x) dst[w] = src[w];
-    }
-    __syncthreads();
-    run_item<FMAX>(sp, it, smem, m.term, m.rhs0);
+    // a private copy of the context's parameters: the compiler keeps the
+    // fields it needs in registers, which no store to the shared work arrays
+    // can alias (a copy in shared memory was reloaded in the inner loops:
+    // 1 % slower RK4, 1.5 % slower 64-instance draw)
+    const KParams p = ps[m.ctx];
+    run_item<FMAX>(p, it, smem, m.term, m.rhs0);
   }
 }
 
