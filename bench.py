@@ -44,6 +44,15 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(t, device):
+    """The largest of the ranks' values (the job's time is its slowest rank's)."""
+    import torch
+    import torch.distributed as dist
+    x = torch.tensor([float(t)], dtype=torch.float64, device=device)
+    dist.all_reduce(x, op=dist.ReduceOp.MAX)
+    return float(x.item())
+
+
 def build_oracle_inputs(model):
     from oracle.oracle import OracleSG4
     O = OracleSG4(model.D, model.L, model.L, 1, 1, 2, 1, scaleQ=model.scaleQ)
@@ -449,9 +458,7 @@ def run_ours(args, ws, rank, local):
     ms = [a.elapsed_time(b) for a, b in ev]
     t_tot = sum(ms) / 1e3
     if ws > 1:
-        t = torch.tensor([t_tot], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_tot = float(t.item())
+        t_tot = max_over_ranks(t_tot, "cuda")
         dist.barrier()
     ms_step = 1e3 * t_tot / args.steps
     value = ws * args.steps * nrhs / t_tot
