@@ -60,7 +60,7 @@ typedef struct {
   int LB;                   /* basis level (L_SparseBasis) */
   int nb0;                  /* channels (electronic states, nb_be), 1..8: a vector is nb0
                                blocks of N (RvecB((ie-1)*Max_nDI + iB)); nb0 > 1 takes
-                               operator types 0 and 1 with V as a grid */
+                               operator types 0, 1 and 10 with V as a grid */
   const int* nb_of_l;       /* [D*(L+1)] */
   const int* nq_of_l;       /* [D*(L+1)] */
   const double* x;          /* sum over (i,l) of nq */
