@@ -365,10 +365,25 @@ struct evr_sg4_ctx {
 // given) or when V couples channels (a point's value needs the other
 // channels' x): otherwise pass B writes O over x (D + 1 arrays, so more
 // items keep their arrays in shared memory).
+// Type 1 with an off-diagonal F2 or an F1 term (the fused passes then stage
+// U_1..U_{D-1}).
+static bool t1_mixed(const evr_sg4_ctx* c) {
+  const int D = c->D;
+  for (int i = 0; i < D; ++i) {
+    if (c->F1[i] != 0.0) return true;
+    for (int j = i + 1; j < D; ++j)
+      if (c->F2[i * D + j] != 0.0) return true;
+  }
+  return false;
+}
+
 static int nbuf_for(const evr_sg4_ctx* c) {
   const int D = c->D;
   if (c->type == 0) return 2;
-  if (c->type == 1) return 4;
+  // type 1: the fused passes of the wide and mid kernels take x, O and, with
+  // mixed terms, U_1..U_{D-1}; the narrow kernel's term-by-term passes X, T,
+  // Y, C (a plan's geometry is chosen after its split, so room for both)
+  if (c->type == 1) return std::max(4, 2 + (t1_mixed(c) ? D - 1 : 0));
   if (D > EVR_FUSED_MAXD) return D + 4;
   return (c->d_Jac || c->d_sqRho || c->nb0 > 1) ? D + 2 : D + 1;
 }
@@ -869,6 +884,7 @@ static KParams make_params(evr_sg4_ctx* c, int nrhs_v, int cshift, const double*
   p.sqRho = c->d_sqRho;
   p.F2 = c->d_F2;
   p.F1 = c->d_F1;
+  p.t1_mixed = c->type == 1 && t1_mixed(c) ? 1 : 0;
   p.type = c->type;
   p.nbuf = nbuf_for(c);
   p.smem_doubles = c->smem_doubles;
@@ -1035,13 +1051,18 @@ extern "C" int evr_sg4_flops_per_rhs(const evr_sg4_ctx* c, double* flops) {
     const double vq = c->d_V ? (c->nb0 > 1 ? 2.0 * c->nb0 * q : q) : 0.0;
     if (c->type == 0) {
       f += vq;
-    } else if (c->type == 1) {
+    } else if (c->type == 1) {  // the fused passes (type1_fused; the same for a diagonal F2 term by term)
       f += vq;
       for (int i = 0; i < D; ++i)
-        for (int j = i; j < D; ++j)
-          if (c->F2[i * D + j] != 0.0) f += 2.0 * q * (i == j ? nq[i] : nq[i] + nq[j]) + 2.0 * q;
-      for (int i = 0; i < D; ++i)
-        if (c->F1[i] != 0.0) f += 2.0 * q * nq[i] + 2.0 * q;
+        if (c->F2[i * D + i] != 0.0) f += 2.0 * q * nq[i] + 2.0 * q;  // F2_ii d2_i x
+      if (t1_mixed(c)) {
+        for (int i = 0; i < D; ++i) {
+          f += 2.0 * q * nq[i];                                       // d_i x
+          if (c->F1[i] != 0.0) f += 2.0 * q;                          // F1_i d_i x
+        }
+        f += 2.0 * q * (D * (D - 1) / 2);                             // U_i = sum_{j>i} F2_ij d_j x
+        for (int i = 0; i + 1 < D; ++i) f += 2.0 * q * nq[i];         // d_i U_i
+      }
     } else {
       f += 4.0 * q * sum_nqi;                       // D derivative passes, twice
       f += c->d_G ? 2.0 * D * D * q : 0.0;           // G contraction

@@ -140,6 +140,7 @@ struct KParams {
   int nb0;                   // channels (electronic states): a vector is nb0 blocks of Nfun
   long long Nfun;            // packed basis functions per channel
   long long vstride;         // V[(a*nb0 + b)*vstride + point] for nb0 > 1
+  int t1_mixed;              // type 1: some F2_ij (i < j) or F1_i is non-zero
 };
 
 struct ItemShared {
@@ -529,6 +530,99 @@ __device__ void type10_fused(const KParams& p, const ItemShared& it, const doubl
   __syncthreads();
 }
 
+// Type-1 grid operator (CASE 1 of sub_TabOpPsi_OF_ONEDP_FOR_SGtype4,
+// y = V.x + sum_{i<=j} F2_ij d_i d_j x + sum_i F1_i d_i x; the reference
+// applies each term as a derivative pass of its own) in fused passes over
+// the grid points of an item:
+//   pass A, per point: V.x + sum_i F2_ii (d2_i x)(point), and with mixed
+//     terms also + sum_i F1_i (d_i x)(point) and U_i = sum_{j>i} F2_ij
+//     (d_j x)(point), stored (the derivatives along different modes commute);
+//   pass B (mixed terms only): O += sum_i (d_i U_i)(point), one FMA chain.
+// One or two barriers instead of one or two per term.  For H^T the matrices
+// are the transposed set (chosen with the item's matrix offsets).
+template <int DD, bool INC>
+__device__ void type1_fused(const KParams& p, const ItemShared& it, const double* x, double* O, double* U,
+                            int NQR) {
+  const int nqt = it.nq_t;
+  const long long oq = it.off_nq;
+  const ModeSizes<DD, INC> ms(p, it);
+  const bool mixed = p.t1_mixed != 0;
+  GridPos<DD> gp;
+  if constexpr (INC) gp.init(ms.nq_, nqt, threadIdx.x, blockDim.x);
+  for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
+    int idx[DD], q;
+    point_digits<DD, INC>(gp, ms, nqt, e, idx, q);
+    if constexpr (INC) gp.advance(ms.nq_, blockDim.x);
+    const double* xr = x + (e - q);
+    double acc = !p.V ? 0.0 : (p.nb0 == 1 ? __ldg(p.V + oq + q) * x[e] : vmat_apply(p, x, e, nqt, oq, it.rhs0));
+    double phi[DD];
+#pragma unroll
+    for (int i = 0; i < DD; ++i) {
+      const int n = ms.nq(i), sd = ms.st(i);
+      const double* fib = xr + (q - idx[i] * sd);
+      const double f2 = __ldg(p.F2 + i * DD + i);
+      if (f2 != 0.0) {
+        const double* row2 = p.mats + it.mo[i][M_D2] + idx[i] * n;
+        double d = 0.0;
+        for (int m = 0; m < n; ++m) d = fma(__ldg(row2 + m), fib[m * sd], d);
+        acc = fma(f2, d, acc);
+      }
+      phi[i] = 0.0;
+      if (mixed) {
+        const double* row = ms.Md(i) + idx[i] * n;
+        double a = 0.0;
+        for (int m = 0; m < n; ++m) a = fma(__ldg(row + m), fib[m * sd], a);
+        phi[i] = a;
+        const double f1 = __ldg(p.F1 + i);
+        if (f1 != 0.0) acc = fma(f1, a, acc);
+      }
+    }
+    if (mixed) {
+#pragma unroll
+      for (int i = 0; i + 1 < DD; ++i) {
+        double u = 0.0;
+#pragma unroll
+        for (int j = i + 1; j < DD; ++j) u = fma(__ldg(p.F2 + i * DD + j), phi[j], u);
+        U[(long long)i * NQR + e] = u;
+      }
+    }
+    O[e] = acc;
+  }
+  __syncthreads();
+  if (!mixed) return;
+  if constexpr (INC) gp.init(ms.nq_, nqt, threadIdx.x, blockDim.x);
+  for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
+    int idx[DD], q;
+    point_digits<DD, INC>(gp, ms, nqt, e, idx, q);
+    if constexpr (INC) gp.advance(ms.nq_, blockDim.x);
+    double sum = O[e];
+#pragma unroll
+    for (int i = 0; i + 1 < DD; ++i) {
+      const int n = ms.nq(i), sd = ms.st(i);
+      const double* fib = U + (long long)i * NQR + (e - idx[i] * sd);
+      const double* row = ms.Md(i) + idx[i] * n;
+      for (int m = 0; m < n; ++m) sum = fma(__ldg(row + m), fib[m * sd], sum);
+    }
+    O[e] = sum;
+  }
+  __syncthreads();
+}
+
+template <int FMAX>
+__device__ void type1_fused_dispatch(const KParams& p, const ItemShared& it, const double* x, double* O, double* U,
+                                     int NQR) {
+  switch (p.D) {
+#define EVR_T1(n)                                                                                          \
+  case n:                                                                                                  \
+    if constexpr (n <= FMAX) type1_fused<n, (FMAX > EVR_NARROW_FMAX) || EVR_NARROW_INC>(p, it, x, O, U, NQR); \
+    break;
+    EVR_T1(1) EVR_T1(2) EVR_T1(3) EVR_T1(4) EVR_T1(5) EVR_T1(6) EVR_T1(7) EVR_T1(8) EVR_T1(9)
+    EVR_T1(10) EVR_T1(11) EVR_T1(12)
+#undef EVR_T1
+    default: break;
+  }
+}
+
 template <int FMAX>
 __device__ void type10_fused_dispatch(const KParams& p, const ItemShared& it, const double* x, double* O, double* U,
                                       int NQR, bool inplace) {
@@ -639,34 +733,44 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ter
     }
     __syncthreads();
   } else if (p.type == 1) {
-    // CASE 1: y = V.x + sum F2_ij d_i d_j x + sum F1_i d_i x
-    double* Y = buf + 2 * NQR;
-    double* C = buf + 3 * NQR;
-    for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
-      const int q = e % nqt;
-      Y[e] = !p.V ? 0.0 : (p.nb0 == 1 ? __ldg(p.V + oq + q) * x[e] : vmat_apply(p, x, e, nqt, oq, it.rhs0));
-    }
-    __syncthreads();
-    for (int i = 0; i < D; ++i)
-      for (int j = i; j < D; ++j) {
-        double f = p.F2[i * D + j];
-        if (f == 0.0) continue;
-        if (i == j) {
-          grid_deriv(p, it, i, M_D2, x, Y, true, f);
-        } else {
-          grid_deriv(p, it, i, M_D1, x, C, false, 1.0);
+    // CASE 1 through the fused grid passes in the wide and mid kernels (x in
+    // X, O in T, then U_1..U_{D-1}); the narrow kernel keeps the term-by-term
+    // passes: compiled into it, the fused code shifted its register
+    // allocation and cost the type-10 benchmark 1.2 %
+    if constexpr (FMAX > EVR_NARROW_FMAX) {
+      double* O = T;
+      type1_fused_dispatch<FMAX>(p, it, x, O, buf + 2 * NQR, NQR);
+      y = O;
+    } else {
+      // CASE 1: y = V.x + sum F2_ij d_i d_j x + sum F1_i d_i x, term by term
+      double* Y = buf + 2 * NQR;
+      double* C = buf + 3 * NQR;
+      for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
+        const int q = e % nqt;
+        Y[e] = !p.V ? 0.0 : (p.nb0 == 1 ? __ldg(p.V + oq + q) * x[e] : vmat_apply(p, x, e, nqt, oq, it.rhs0));
+      }
+      __syncthreads();
+      for (int i = 0; i < D; ++i)
+        for (int j = i; j < D; ++j) {
+          double f = p.F2[i * D + j];
+          if (f == 0.0) continue;
+          if (i == j) {
+            grid_deriv(p, it, i, M_D2, x, Y, true, f);
+          } else {
+            grid_deriv(p, it, i, M_D1, x, C, false, 1.0);
+            __syncthreads();
+            grid_deriv(p, it, j, M_D1, C, Y, true, f);
+          }
           __syncthreads();
-          grid_deriv(p, it, j, M_D1, C, Y, true, f);
         }
+      for (int i = 0; i < D; ++i) {
+        double f = p.F1[i];
+        if (f == 0.0) continue;
+        grid_deriv(p, it, i, M_D1, x, Y, true, f);
         __syncthreads();
       }
-    for (int i = 0; i < D; ++i) {
-      double f = p.F1[i];
-      if (f == 0.0) continue;
-      grid_deriv(p, it, i, M_D1, x, Y, true, f);
-      __syncthreads();
+      y = Y;
     }
-    y = Y;
   } else if (D <= FMAX) {
     // CASE 10 through the fused grid passes; x is in X.  Without Jac and rho
     // (D + 1 arrays) U_1..U_D follow X and pass B writes O = V.x + c.sum over
