@@ -260,6 +260,10 @@ def test_transposed_operator_matches_dense_transpose(type_op):
     op.hpsi_dev(P, out, transpose=True)
     torch.cuda.synchronize()
     assert rel_err(out.cpu().numpy().T, H.T @ psi) <= TOL
+    # and H itself (for type 1 the fused passes with every mixed and first-derivative term)
+    op.hpsi_dev(P, out)
+    torch.cuda.synchronize()
+    assert rel_err(out.cpu().numpy().T, H @ psi) <= TOL
     # complex psi through the transposed operator
     pc = random_psi(O.N, 2, 3, complex_=True)
     Pc = torch.from_numpy(np.ascontiguousarray(pc.T)).cuda()
