@@ -531,7 +531,7 @@ def run_ours(args, ws, rank, local):
         result = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded PCG64, configs[1] shapes)",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded PCG64; 6-D L=8 SG4 shapes, 20 RHS)",
             "config": {"workload": WORKLOAD, "D": D, "L": model.L, "nrhs": nrhs, "N": N, "nb_SG": b.nb_SG,
                        "sum_nq": b.sum_nq, "type_op": 10, "l2": "flushed (256 MB write) before every timed step",
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
@@ -576,7 +576,7 @@ def run_reference(args, ws, rank):
     v = args.steps * nrhs / dt
     return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic (seeded PCG64, configs[1] shapes)", "impl": "reference",
+            "dtype": "f64", "data": "synthetic (seeded PCG64; 6-D L=8 SG4 shapes, 20 RHS)", "impl": "reference",
             "config": {"workload": WORKLOAD, "D": model.D, "L": model.L, "nrhs": nrhs, "N": O.N},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": f"{args.steps} full 20-RHS H.psi steps (the reference is Fortran with no "
