@@ -755,21 +755,30 @@ static int choose_geo(int D, size_t n_wide, int num_sms) {
 }
 
 // The same list sorted by decreasing cost (the persistent kernel then ends
-// balanced), with each term's block size written into c->terms; chooses the
-// launch geometry (c->geo, c->smem_doubles, c->grid) for this plan.
-static void plan_items(evr_sg4_ctx* c, int nrhs_v, std::vector<Item>& items, std::vector<Item>& sorted,
-                       long long& max_need) {
+// balanced), with each term's block size written into `terms`, and the
+// launch geometry chosen for this plan (the context is not modified).
+static void plan_sorted(const evr_sg4_ctx* c, int nrhs_v, std::vector<TermInfo>& terms, std::vector<Item>& items,
+                        std::vector<Item>& sorted, long long& max_need, int& geo) {
   std::vector<float> cost;
-  plan_work(c, nrhs_v, geo_smem_bytes(0) / 8, c->terms, items, cost, max_need);
-  c->geo = choose_geo(c->D, items.size(), c->num_sms);
-  c->smem_doubles = geo_smem_bytes(c->geo) / 8;
-  c->grid = geo_ctas(c->geo) * c->num_sms;
-  if (c->geo) plan_work(c, nrhs_v, c->smem_doubles, c->terms, items, cost, max_need);
+  plan_work(c, nrhs_v, geo_smem_bytes(0) / 8, terms, items, cost, max_need);
+  geo = choose_geo(c->D, items.size(), c->num_sms);
+  if (geo) plan_work(c, nrhs_v, geo_smem_bytes(geo) / 8, terms, items, cost, max_need);
   std::vector<int> order(items.size());
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
   sorted.resize(items.size());
   for (size_t k = 0; k < order.size(); ++k) sorted[k] = items[order[k]];
+}
+
+// plan_sorted into the context's own term table and launch geometry
+// (c->terms, c->geo, c->smem_doubles, c->grid).
+static void plan_items(evr_sg4_ctx* c, int nrhs_v, std::vector<Item>& items, std::vector<Item>& sorted,
+                       long long& max_need) {
+  int geo = 0;
+  plan_sorted(c, nrhs_v, c->terms, items, sorted, max_need, geo);
+  c->geo = geo;
+  c->smem_doubles = geo_smem_bytes(geo) / 8;
+  c->grid = geo_ctas(geo) * c->num_sms;
 }
 
 static int build_items(evr_sg4_ctx* c, int nrhs_v) {
@@ -1137,11 +1146,12 @@ extern "C" int evr_probe_fp64_peak(double* tflops) {
 // H.psi without device allocation.
 //
 // Some callers cannot call cudaMalloc: code running inside a caller-owned
-// memory budget (a host program whose allocator owns every device byte), a
-// real-time loop that must not hit the driver's allocator, or a host thread
-// that is not allowed to change the device heap between two CUDA-graph
-// launches.  evr_sg4_hpsi_noalloc gives them the batched kernel with all of
-// its scratch -- the work counter, the work list, the per-term contributions
+// memory budget (a host program whose allocator owns every device byte and
+// forbids allocations behind its back), or a real-time loop that must stay
+// out of the driver's allocator, whose calls can synchronise the device.
+// evr_sg4_hpsi_noalloc gives them the batched kernel with all of its scratch
+// -- the work counter, the term table of this call's plan, the work list,
+// the per-term contributions, the chunk partials of the ordered accumulation
 // and the per-CTA slabs for terms larger than shared memory -- carved from
 // one fixed, file-scope device array instead of device allocations.
 //
@@ -1151,7 +1161,9 @@ extern "C" int evr_probe_fp64_peak(double* tflops) {
 // cleared at the start of each call and every other byte a call reads is
 // written by that call first.  Two calls whose kernels overlap on the GPU
 // (different streams, or different host threads) race on the array: keep
-// calls on one stream, or serialise them.
+// calls on one stream, or serialise them.  The call plans into local copies
+// (term table, geometry), so the context's own cached plan for evr_sg4_hpsi
+// is left as it was.
 // ------------------------------------------------------------------------
 static __device__ __align__(256) unsigned char g_noalloc_scratch[EVR_SG4_NOALLOC_SCRATCH_BYTES];
 
@@ -1196,21 +1208,25 @@ extern "C" int evr_sg4_hpsi_noalloc(evr_sg4_ctx* c, int nrhs, const double* psi,
     return set_error(EVR_ERR_ARG, "hpsi_noalloc: psi and hpsi must be device pointers");
   }
   const int nrhs_v = nrhs * c->nb0;
+  // this call's plan, in local copies: the context's cached plan stays as it is
+  std::vector<TermInfo> terms;
   std::vector<Item> items, sorted;
   long long max_need = 0;
-  plan_items(c, nrhs_v, items, sorted, max_need);
-  c->items_nrhs = -1;  // the allocating path rebuilds its own list next time
-  // carve: [counter | items | contributions | chunk partials | large-term slabs], 256-byte aligned
+  int geo = 0;
+  plan_sorted(c, nrhs_v, terms, items, sorted, max_need, geo);
+  const int smem_doubles = geo_smem_bytes(geo) / 8;
+  // carve: [counter | terms | items | contributions | chunk partials | large-term slabs], 256-byte aligned
   auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
-  const size_t off_items = 256;
+  const size_t off_terms = 256;
+  const size_t off_items = off_terms + up(terms.size() * sizeof(TermInfo));
   const size_t off_contrib = off_items + up(sorted.size() * sizeof(Item));
   const size_t off_part = off_contrib + up((size_t)c->z.sum_nb * nrhs_v * 8);
   const size_t off_slabs = off_part + up((size_t)c->n_chunks * nrhs_v * 16);
-  const long long per_cta = max_need > c->smem_doubles ? max_need : 0;
+  const long long per_cta = max_need > smem_doubles ? max_need : 0;
   // with large-term slabs, launch only as many CTAs as the array has slabs for
-  int grid = c->grid;
+  int grid = geo_ctas(geo) * c->num_sms;
   if (per_cta > 0 && off_slabs < (size_t)EVR_SG4_NOALLOC_SCRATCH_BYTES)
-    grid = (int)std::min<long long>(c->grid, ((size_t)EVR_SG4_NOALLOC_SCRATCH_BYTES - off_slabs) / ((size_t)per_cta * 8));
+    grid = (int)std::min<long long>(grid, ((size_t)EVR_SG4_NOALLOC_SCRATCH_BYTES - off_slabs) / ((size_t)per_cta * 8));
   const size_t total = off_slabs + (size_t)per_cta * std::max(grid, 1) * 8;
   if (grid < 1 || total > (size_t)EVR_SG4_NOALLOC_SCRATCH_BYTES)
     return set_error(EVR_ERR_ARG,
@@ -1218,24 +1234,26 @@ extern "C" int evr_sg4_hpsi_noalloc(evr_sg4_ctx* c, int nrhs, const double* psi,
                      "%u-byte array; use evr_sg4_hpsi or fewer right-hand sides",
                      nrhs, total, (unsigned)EVR_SG4_NOALLOC_SCRATCH_BYTES);
   cudaStream_t s = (cudaStream_t)stream;
-  CUDA_TRY(cudaMemcpyAsync(c->d_terms, c->terms.data(), c->terms.size() * sizeof(TermInfo),
-                           cudaMemcpyHostToDevice, s));
+  // both host lists are pageable: cudaMemcpyAsync stages them before it
+  // returns, so they may go out of scope when this call does
+  CUDA_TRY(cudaMemcpyAsync(base + off_terms, terms.data(), terms.size() * sizeof(TermInfo), cudaMemcpyHostToDevice,
+                           s));
   CUDA_TRY(cudaMemcpyAsync(base + off_items, sorted.data(), sorted.size() * sizeof(Item), cudaMemcpyHostToDevice, s));
   CUDA_TRY(cudaMemsetAsync(base, 0, sizeof(unsigned int), s));
   KParams p = make_params(c, nrhs_v, 0, psi, ldpsi, hpsi, ldh, 1.0);
+  p.terms = (const TermInfo*)(base + off_terms);
   p.items = (const Item*)(base + off_items);
   p.n_items = (int)sorted.size();
   p.counter = (unsigned int*)base;
+  p.smem_doubles = smem_doubles;
   p.contrib = (double*)(base + off_contrib);
   p.gscratch = per_cta ? (double*)(base + off_slabs) : nullptr;
   p.scratch_per_cta = per_cta;
-  launch_batched(c->geo, grid, (size_t)c->smem_doubles * 8, s, p);
+  launch_batched(geo, grid, (size_t)smem_doubles * 8, s, p);
   CUDA_TRY(cudaGetLastError());
   int rc = launch_reduce(c, p.contrib, (double2*)(base + off_part), nrhs_v, 0, psi, ldpsi, hpsi, ldh, E0, Esc, s);
   if (rc) return rc;
   CUDA_TRY(cudaGetLastError());
-  // (both host lists were copied from pageable memory, which cudaMemcpyAsync
-  // stages before it returns, so they may go out of scope now)
   c->last_launches = 3;
   return EVR_OK;
 }

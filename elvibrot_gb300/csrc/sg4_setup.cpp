@@ -36,8 +36,12 @@ typedef long double ld;
 
 // ---------------------------------------------------------------- quadrature
 // Nodes: eigenvalues of the symmetric tridiagonal Jacobi matrix of the
-// Hermite weight exp(-x^2) (zero diagonal, off-diagonal sqrt(k/2)), by the
-// implicit QL method, then Newton steps on the orthonormal recurrence.
+// Hermite weight exp(-x^2) (zero diagonal, off-diagonal sqrt(k/2)) -- the
+// Golub-Welsch construction (G. H. Golub and J. H. Welsch, "Calculation of
+// Gauss quadrature rules", Math. Comp. 23 (1969) 221-230) -- by the implicit
+// QL method with Wilkinson shifts (eigenvalues only; the EISPACK tql1 scheme
+// of Bowdler, Martin, Reinsch and Wilkinson, Numer. Math. 11 (1968) 293-306),
+// then Newton steps on the orthonormal recurrence.
 static void jacobi_ql(int n, std::vector<ld>& d, std::vector<ld>& e) {
   for (int l = 0; l < n; ++l) {
     int iter = 0, m;

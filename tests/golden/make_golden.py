@@ -1,8 +1,8 @@
 """Regenerates the golden fixtures in this folder from the ElVibRot source tree.
 
-Run once in a checkout that has the reference mounted (default path below, or
-pass it as argv[1]); the fixtures are committed so the tests never need the
-reference at run time.
+Run once with the path of an ElVibRot checkout as the only argument
+(python make_golden.py <ElVibRot source tree>); the fixtures are committed so
+the tests never need the reference at run time.
 
   hermquadra.json : Internal_data/HermQuadra/herm{1..40}.txt -- Gauss-Hermite
                     nodes (column 2), weights (column 3) and weights*exp(x^2)
@@ -26,7 +26,9 @@ import os
 import re
 import sys
 
-ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2 or not os.path.isdir(sys.argv[1]):
+    sys.exit("usage: python make_golden.py <path of the ElVibRot source tree>")
+ref = sys.argv[1]
 here = os.path.dirname(os.path.abspath(__file__))
 
 herm = {}
