@@ -66,7 +66,9 @@ class _OrcOp(ctypes.Structure):
     _fields_ = [("type", ctypes.c_int), ("V", ctypes.POINTER(ctypes.c_double)),
                 ("G", ctypes.POINTER(ctypes.c_double)), ("Jac", ctypes.POINTER(ctypes.c_double)),
                 ("sqRho", ctypes.POINTER(ctypes.c_double)), ("F2", ctypes.POINTER(ctypes.c_double)),
-                ("F1", ctypes.POINTER(ctypes.c_double))]
+                ("F1", ctypes.POINTER(ctypes.c_double)), ("V_nterms", ctypes.c_int),
+                ("V_coef", ctypes.POINTER(ctypes.c_double)), ("V_expo", ctypes.POINTER(ctypes.c_int)),
+                ("G0", ctypes.POINTER(ctypes.c_double)), ("G1", ctypes.POINTER(ctypes.c_double))]
 
 
 def gauss_hermite(nq: int):
@@ -131,11 +133,13 @@ class OracleSG4:
         return Q.reshape(self.sum_nq, self.D)
 
     def hpsi(self, psi, type_op=10, V=None, G=None, Jac=None, sqRho=None, F2=None, F1=None, nthreads=0,
-             extended=False):
+             extended=False, V_poly=None, G0=None, G1=None):
         """psi: (N,) or (N, nrhs) float64, column-major per RHS.
 
-        extended=True runs the same algorithm with long-double intermediates
-        (the accuracy yardstick); the result is rounded to double."""
+        V / G are grids; alternatively V_poly = (coef[nt], expo[nt, D]) and the
+        affine G0[D, D], G1[D, D, D] are evaluated term by term at the grid
+        points.  extended=True runs the same algorithm with long-double
+        intermediates (the accuracy yardstick); the result is rounded to double."""
         psi = np.asarray(psi, dtype=np.float64)
         one = psi.ndim == 1
         P = psi.reshape(self.N, -1)
@@ -143,7 +147,14 @@ class OracleSG4:
         Pc = np.ascontiguousarray(P.T)  # rhs-major = column-major N x nrhs
         H = np.zeros_like(Pc)
         keep = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (V, G, Jac, sqRho, F2, F1)]
-        op = _OrcOp(type_op, *[_dp(a) for a in keep])
+        coef = expo = None
+        if V_poly is not None:
+            coef = np.ascontiguousarray(V_poly[0], dtype=np.float64)
+            expo = np.ascontiguousarray(V_poly[1], dtype=np.int32).reshape(len(coef), self.D)
+        g0 = None if G0 is None else np.ascontiguousarray(G0, dtype=np.float64)
+        g1 = None if G1 is None else np.ascontiguousarray(G1, dtype=np.float64)
+        op = _OrcOp(type_op, *[_dp(a) for a in keep], 0 if coef is None else len(coef), _dp(coef), _ip(expo),
+                    _dp(g0), _dp(g1))
         fn = lib().orc_hpsi_ld if extended else lib().orc_hpsi
         rc = fn(self.h, ctypes.byref(op), nrhs, _dp(Pc), _dp(H), int(nthreads))
         if rc != 0:

@@ -61,7 +61,15 @@ void orc_grid_points(const orc_sg4* s, double* Q);
  *  type 10: y = -1/2 sum_i d_i (Jac sum_j G_ji d_j (s x)) / (Jac s) + V x,
  *           s = sqRhoOVERJac.  G[sum_nq*D*D] per term laid out (iq, j, i) with
  *           iq fastest (GGiq), NULL = identity; Jac, sqRho NULL = 1.
- *  V[sum_nq] concatenated per term (OpGrid%Grid layout), NULL = 0. */
+ *  V[sum_nq] concatenated per term (OpGrid%Grid layout), NULL = 0.
+ *  Fields given in analytic form instead of grids are evaluated term by
+ *  term, once per call, at the term's grid points, as the reference's type-10
+ *  path evaluates its fields per term inside the term loop
+ *  (get_OpGrid_type10_OF_ONEDP_FOR_SG4, sub_OpPsi_SG4.f90:2536, called at
+ *  :1553; V per point through get_d0MatOp_AT_Qact):
+ *    V (when V is NULL and V_nterms > 0) = sum_t V_coef[t] prod_i Q_i^V_expo[t*D+i];
+ *    G (type 10, when G is NULL and G0 or G1 is given)
+ *      G_ij(Q) = G0[i*D+j] (identity if NULL) + sum_k G1[(i*D+j)*D+k] Q_k. */
 typedef struct {
   int type;
   const double* V;
@@ -70,6 +78,11 @@ typedef struct {
   const double* sqRho;
   const double* F2;
   const double* F1;
+  int V_nterms;
+  const double* V_coef;
+  const int* V_expo;
+  const double* G0;
+  const double* G1;
 } orc_op;
 
 /* hpsi[N*nrhs] = H psi[N*nrhs] (column-major, ld = N).  nthreads <= 0 = all. */

@@ -147,3 +147,25 @@ def test_pyrazine_autocorrelation_golden():
     err = max(np.max(np.abs(got.real - ac["re"])), np.max(np.abs(got.imag - ac["im"])))
     print(f"pyrazine 12-D L=1 autocorrelation: max error {err:.2e} over {len(t)} times")
     assert err <= g["criterion"]
+
+
+def test_oracle_analytic_fields_match_grid_fields():
+    """The oracle's term-by-term evaluation of a polynomial V and an affine G
+    (no stored grids: what the large 12-D checks need) gives the operator of
+    the same fields passed as grids."""
+    from elvibrot_gb300.configs import make_model
+    m = make_model(4, 4, 10, 99)
+    O = OracleSG4(m.D, m.L, m.L, 1, 1, 2, 1, scaleQ=m.scaleQ)
+    Q = O.grid_points()
+    nq = np.prod(O.tables()[0] + 2, axis=1)
+    psi = np.random.default_rng(4).normal(size=(O.N, 3))
+    ref = O.hpsi(psi, type_op=10, V=m.V(Q), G=m.G_grid(Q, nq))
+    got = O.hpsi(psi, type_op=10, V_poly=(m.V.coef, m.V.expo), G0=m.G0, G1=m.G1)
+    assert np.max(np.abs(got - ref)) <= 1e-13 * np.max(np.abs(ref))
+    # type 1 with the polynomial V
+    m1 = make_model(3, 5, 1, 98)
+    O1 = OracleSG4(m1.D, m1.L, m1.L, 1, 1, 2, 1, scaleQ=m1.scaleQ)
+    psi1 = np.random.default_rng(5).normal(size=(O1.N, 2))
+    r1 = O1.hpsi(psi1, type_op=1, V=m1.V(O1.grid_points()), F2=m1.F2.ravel())
+    g1 = O1.hpsi(psi1, type_op=1, V_poly=(m1.V.coef, m1.V.expo), F2=m1.F2.ravel())
+    assert np.max(np.abs(g1 - r1)) <= 1e-13 * np.max(np.abs(r1))
