@@ -37,6 +37,12 @@ CONFIG_INDEX = 1
 WORKLOAD = "6-D SG4 (HO modes, L=LB=8, nb=l+1, nq=l+2), type-10 KEO with Q-dependent G, 20 real RHS"
 
 
+def workload_config(model, nrhs, N, nb_SG, sum_nq):
+    """The workload's description, identical in both arms (no device or run keys)."""
+    return {"workload": WORKLOAD, "D": model.D, "L": model.L, "nrhs": nrhs, "N": int(N), "nb_SG": int(nb_SG),
+            "sum_nq": int(sum_nq), "type_op": int(model.type_op)}
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -66,12 +72,13 @@ def build_oracle_inputs(model):
     return O, kw
 
 
-def time_oracle(model, nrhs, min_seconds, min_steps, max_steps, seed):
-    """Times the CPU restatement on all host threads; returns (Hpsi/s, steps, seconds, threads)."""
+def time_oracle(model, nrhs, min_seconds, min_steps, max_steps, seed, threads=None):
+    """Times the CPU restatement on `threads` host threads (all by default);
+    returns (Hpsi/s, steps, seconds, threads)."""
     from elvibrot_gb300.configs import random_psi
     O, kw = build_oracle_inputs(model)
     psi = random_psi(O.N, nrhs, seed)
-    threads = os.cpu_count() or 1
+    threads = threads or os.cpu_count() or 1
     O.hpsi(psi[:, :1], nthreads=threads, **kw)  # warm
     t0 = time.perf_counter()
     steps = 0
@@ -148,7 +155,9 @@ def profile_traffic():
 
 
 def bench_davidson(op):
-    """Lowest 20 levels of the benchmark operator (restart 60, residual 1e-8)."""
+    """Lowest 20 levels of the benchmark operator (restart 60, residual 1e-8):
+    every iteration as two recorded CUDA graphs (the default) and as the same
+    steps launched one by one."""
     import torch
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -158,13 +167,20 @@ def bench_davidson(op):
     # one untimed solve first: its cuBLAS calls load the library's kernels
     # (seconds on a cold page cache), which is not the solver's cost
     op.davidson(20, max_subspace=60, conv_resi=1e-8, symmetrize=True, diag=d, max_it=1000)
-    torch.cuda.synchronize()
-    t1w = time.perf_counter()
-    ev, vec, rs, its = op.davidson(20, max_subspace=60, conv_resi=1e-8, symmetrize=True, diag=d, max_it=1000)
-    torch.cuda.synchronize()
-    t2 = time.perf_counter()
-    return {"levels": 20, "max_subspace": 60, "conv_resi": 1e-8, "iterations": its, "davidson_s": t2 - t1w,
-            "diagonal_s": t1 - t0, "max_residual": float(np.max(rs)), "E0_hartree": float(ev[0])}
+    res = {"levels": 20, "max_subspace": 60, "conv_resi": 1e-8, "diagonal_s": t1 - t0}
+    runs = {}
+    for graph in (False, True):
+        torch.cuda.synchronize()
+        ta = time.perf_counter()
+        runs[graph] = op.davidson(20, max_subspace=60, conv_resi=1e-8, symmetrize=True, diag=d, max_it=1000,
+                                  graph=graph)
+        torch.cuda.synchronize()
+        res["davidson_s" if graph else "davidson_eager_s"] = time.perf_counter() - ta
+    ev, vec, rs, its = runs[True]
+    res.update({"iterations": its, "eager_over_graph": res["davidson_eager_s"] / res["davidson_s"],
+                "bit_identical_to_eager": bool(np.array_equal(ev, runs[False][0])),
+                "max_residual": float(np.max(rs)), "E0_hartree": float(ev[0])})
+    return res
 
 
 def bench_oc_gradient():
@@ -190,21 +206,34 @@ def bench_oc_gradient():
         Hmax = float((v * hv).sum().item())
         v, hv = hv, v
     E0 = 0.5 * (float(ev[0]) + Hmax)                     # RK4 on H0 - E0 (fcn_field's para_H%E0)
-    P = psi0.clone()
     nsub = 10                                            # RK4 steps of 0.5 a.u. per 5-a.u. field sample
-    H0.rk4_field(mu, E[:10], P, 5.0, E0=E0, nsub=nsub)  # warm
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    P = psi0.clone()
-    H0.rk4_field(mu, E, P, 5.0, E0=E0, nsub=nsub)
-    torch.cuda.synchronize()
-    t1 = time.perf_counter()
-    J, g = H0.oc_gradient(mu, E, psi0, target, 5.0, checkpoint=45, E0=E0, nsub=nsub)
-    torch.cuda.synchronize()
-    t2 = time.perf_counter()
-    return {"workload": "4-D SG4 L=7 type 1, 2000 field samples of 5 a.u. (10 RK4 steps each), checkpoint every 45",
-            "s_per_iter": t2 - t1, "forward_s": t1 - t0, "ratio_to_forward": (t2 - t1) / (t1 - t0),
-            "J": J, "E0": E0, "Hmax_estimate": Hmax, "norm_after_forward": float(torch.linalg.vector_norm(P).item())}
+    res = {"workload": "4-D SG4 L=7 type 1, 2000 field samples of 5 a.u. (10 RK4 steps each), checkpoint every 45",
+           "E0": E0, "Hmax_estimate": Hmax}
+    out = {}
+    for graph in (True, False):
+        P = psi0.clone()
+        H0.rk4_field(mu, E[:10], P, 5.0, E0=E0, nsub=nsub, graph=graph)  # warm
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        P = psi0.clone()
+        H0.rk4_field(mu, E, P, 5.0, E0=E0, nsub=nsub, graph=graph)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        J, g = H0.oc_gradient(mu, E, psi0, target, 5.0, checkpoint=45, E0=E0, nsub=nsub, graph=graph)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        out[graph] = (P.cpu(), J, g)
+        sfx = "" if graph else "_eager"
+        res.update({"s_per_iter" + sfx: t2 - t1, "forward_s" + sfx: t1 - t0})
+        if graph:
+            res.update({"ratio_to_forward": (t2 - t1) / (t1 - t0), "J": J,
+                        "norm_after_forward": float(torch.linalg.vector_norm(P).item()),
+                        "us_per_rk4_stage": 1e6 * (t1 - t0) / (len(E) * nsub * 4)})
+    res["graph_bit_identical_to_eager"] = bool(torch.equal(out[True][0], out[False][0]) and out[True][1] == out[False][1]
+                                               and np.array_equal(out[True][2], out[False][2]))
+    res["forward_eager_over_graph"] = res["forward_s_eager"] / res["forward_s"]
+    res["gradient_eager_over_graph"] = res["s_per_iter_eager"] / res["s_per_iter"]
+    return res
 
 
 def coherent_packets(D, L, scaleQ, nrhs, shift=1.0):
@@ -360,8 +389,10 @@ def _terms_array(D, L):
 
 
 def type10_flops_per_rhs(D, L):
-    """evr_sg4_flops_per_rhs for a type-10 operator with V and G (nb = l+1, nq = l+2): the
-    basis<->grid passes in the kernel's mode order (larger l first, ties by index) plus the grid work."""
+    """evr_sg4_flops_per_rhs for a type-10 operator with V and G (nb = l+1, nq = l+2), without
+    building the basis: the basis<->grid passes in the kernel's mode order (larger l first, ties by
+    index), the derivative passes (4 q sum nq_i), the G contraction (2 D^2 q), V.x (q), the single
+    multiply-add closing pass B (2 q) and the weighted scatter (2 nb)."""
     l, q = _terms_array(D, L)
     nb, nq = (l + 1).astype(np.float64), (l + 2).astype(np.float64)
     order = np.argsort(-l, axis=1, kind="stable")
@@ -375,7 +406,7 @@ def type10_flops_per_rhs(D, L):
             rest = np.prod(cur, axis=1) / cur[rows, i]
             f += 2.0 * nb[rows, i] * nq[rows, i] * rest
             cur[rows, i] = (nq if direction == 0 else nb)[rows, i]
-    f += 4.0 * q * nq.sum(axis=1) + 2.0 * D * D * q + q + 4.0 * q + 2.0 * np.prod(nb, axis=1)
+    f += 4.0 * q * nq.sum(axis=1) + 2.0 * D * D * q + q + 2.0 * q + 2.0 * np.prod(nb, axis=1)
     return float(f.sum())
 
 
@@ -416,6 +447,42 @@ def bench_streamed_12d(L=6, nrhs=32, budget_gib=64):
             "field_eval_flops": field_flops, "tflops_hpsi_only": flops / t / 1e12,
             "tflops_with_fields": (flops + field_flops) / t / 1e12,
             "L10_hpsi_s_estimate": t * f10 / fL, "L10_sum_nq": float(_terms_array(D, 10)[1].sum())}
+
+
+def bench_streamed_12d_l10(nrhs=1, budget_gib=64):
+    """The 12-D workload at its stated level, L=10 (646,646 Smolyak terms,
+    6.8e10 grid points; V and G would take 79 TB), on nrhs real vectors: one
+    H.psi with the fields evaluated slice by slice inside it.  Minutes of GPU
+    time, so only on request (--extras stream12_L10)."""
+    import torch
+    from elvibrot_gb300.configs import SEED0, make_model
+    m = make_model(12, 10, 10, SEED0 + 4)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    op = m.operator(field_budget=budget_gib << 30)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    N, snq = op.basis.N, op.basis.sum_nq
+    g = torch.Generator(device="cpu").manual_seed(10)
+    P = torch.randn((nrhs, N), generator=g, dtype=torch.float64).cuda()
+    P /= torch.linalg.vector_norm(P, dim=1, keepdim=True)
+    O = torch.empty_like(P)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    op.hpsi_dev(P, O)
+    b.record()
+    torch.cuda.synchronize()
+    t = a.elapsed_time(b) / 1e3
+    D = 12
+    flops = op.flops_per_rhs * nrhs
+    vmul = sum(int(np.sum(e)) for e in m.V.expo)
+    field_flops = snq * (2.0 * D ** 3 + vmul + len(m.V.coef))
+    return {"workload": f"12-D SG4 L=10 type 10, Q-dependent G, {nrhs} real vector(s), fields streamed",
+            "N": N, "nb_SG": op.basis.nb_SG, "sum_nq": snq, "field_bytes_resident": snq * 8 * (1 + D * D),
+            "field_budget": budget_gib << 30, "slices": op.field_slices, "setup_s": setup_s, "hpsi_s": t,
+            "hpsi_flops": flops, "field_eval_flops": field_flops, "tflops_with_fields": (flops + field_flops) / t / 1e12,
+            "flops_per_rhs_library": op.flops_per_rhs, "flops_per_rhs_formula": type10_flops_per_rhs(D, 10),
+            "finite": bool(torch.isfinite(O).all().item())}
 
 
 def run_ours(args, ws, rank, local):
@@ -497,6 +564,24 @@ def run_ours(args, ws, rank, local):
         pt += a.elapsed_time(b) / 1e3
     plain_value = plain_steps * nrhs / pt
 
+    # the autotuner's plan for this workload (same bits; the headline keeps the automatic plan)
+    tuned = None
+    if not args.no_tune:
+        tr = op.tune_plan(nrhs)
+        tt = 0.0
+        for k in range(plain_steps):
+            flush.fill_(float(k))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            op.hpsi_dev(psi, out, stream=sh)
+            b.record(stream)
+            torch.cuda.synchronize()
+            tt += a.elapsed_time(b) / 1e3
+        tuned = {"value": ws * plain_steps * nrhs / tt, "unit": UNIT, "ms_per_step": 1e3 * tt / plain_steps,
+                 "plan": {"geo": tr["geo"], "rmax": tr["rmax"], "split": tr["split"]},
+                 "tuner_best_ms": tr["ms"], "tuner_automatic_ms": tr["default_ms"]}
+        op.set_plan(-1, 32, 0)
+
     # callers of the path: Davidson on the same operator, OC gradient on the 4-D L=7 system
     extras = {}
     if not args.no_extras:
@@ -511,6 +596,8 @@ def run_ours(args, ws, rank, local):
             extras["cheby_graph"] = bench_cheby_graph()
         if "stream12" in want:
             extras["streamed_12d"] = bench_streamed_12d()
+        if "stream12_L10" in want:
+            extras["streamed_12d_L10"] = bench_streamed_12d_l10()
 
     flops = op.flops_per_rhs * nrhs
     achieved = flops / (ms_step / 1e3) / 1e12
@@ -527,14 +614,16 @@ def run_ours(args, ws, rank, local):
     if rank == 0:
         cpu_v, cpu_steps, cpu_dt, cpu_threads = time_oracle(model, nrhs, min_seconds=1.5, min_steps=1,
                                                             max_steps=50, seed=cfg["seed"])
+        cpu1_v, cpu1_steps, cpu1_dt, _ = time_oracle(model, nrhs, min_seconds=0.0, min_steps=1, max_steps=1,
+                                                     seed=cfg["seed"], threads=1)
         clocks = clk.summary()
         result = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded PCG64; 6-D L=8 SG4 shapes, 20 RHS)",
-            "config": {"workload": WORKLOAD, "D": D, "L": model.L, "nrhs": nrhs, "N": N, "nb_SG": b.nb_SG,
-                       "sum_nq": b.sum_nq, "type_op": 10, "l2": "flushed (256 MB write) before every timed step",
-                       "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+            "config": workload_config(model, nrhs, N, b.nb_SG, b.sum_nq),
+            "l2": "flushed (256 MB write) before every timed step",
+            "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * N * nrhs,
                     "d2h_bytes_per_step": 8 * N * nrhs},
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
@@ -549,9 +638,14 @@ def run_ours(args, ws, rank, local):
             "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cpu_threads, "kind": "port",
                              "sample": f"{cpu_steps} full 20-RHS H.psi of the same workload in {cpu_dt:.2f} s "
                                        f"(C/OpenMP restatement, OpenMP static over Smolyak terms)"},
+            "cpu_baseline_1thread": {"value": cpu1_v, "unit": UNIT, "cores": 1, "kind": "port",
+                                     "sample": f"{cpu1_steps} full 20-RHS H.psi in {cpu1_dt:.2f} s, one thread "
+                                               f"(the reference's serial per-term loop)"},
             "clocks": {"sm_mhz": clocks["sm_mhz"], "sm_max_mhz": clocks["sm_max_mhz"], "reasons": clocks["reasons"]},
             "gpu_launches": launches,
         }
+        if tuned:
+            result["tuned"] = tuned
         result.update(extras)
     return result
 
@@ -577,7 +671,9 @@ def run_reference(args, ws, rank):
     return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (seeded PCG64; 6-D L=8 SG4 shapes, 20 RHS)", "impl": "reference",
-            "config": {"workload": WORKLOAD, "D": model.D, "L": model.L, "nrhs": nrhs, "N": O.N},
+            "config": workload_config(model, nrhs, O.N, len(O.tables()[0]),
+                                      int(np.prod(O.tables()[0] + 2, axis=1).sum())),
+            "parallelism": f"{threads} host threads",
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": f"{args.steps} full 20-RHS H.psi steps (the reference is Fortran with no "
                                        f"compiler on this image; timed: its C/OpenMP restatement)"},
@@ -591,9 +687,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-extras", action="store_true", help="skip the timings of the callers")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner's plan")
     ap.add_argument("--extras", default="davidson,oc,uneven,graph,stream12",
                     help="callers to time: davidson, oc (optimal-control gradient), uneven (64-instance batching), "
-                         "graph (Chebyshev steps replayed from a CUDA graph), stream12 (12-D type 10, streamed fields)")
+                         "graph (Chebyshev steps replayed from a CUDA graph), stream12 (12-D type 10, streamed fields); "
+                         "also on request: stream12_L10 (the 12-D workload at L=10, minutes)")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if ws > 1:

@@ -154,6 +154,26 @@ __device__ __forceinline__ void neumaier_add(double& s, double& c, double x) {
   s = t;
 }
 
+// Neumaier sum of contrib[inv_idx[q] * nrhs_v + v] over q in [q0, q1), in
+// order, with the indices and values loaded eight at a time ahead of the
+// additions (each value sits behind an index load: a short list is
+// latency-bound); the additions are those of the plain loop, in its order.
+__device__ __forceinline__ void chunk_sum(const double* __restrict__ contrib, const long long* __restrict__ inv_idx,
+                                          long long q0, long long q1, int nrhs_v, int v, double& s, double& c) {
+  long long q = q0;
+  for (; q + 8 <= q1; q += 8) {
+    long long id[8];
+    double x[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) id[k] = inv_idx[q + k];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = contrib[id[k] * nrhs_v + v];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) neumaier_add(s, c, x[k]);
+  }
+  for (; q < q1; ++q) neumaier_add(s, c, contrib[inv_idx[q] * nrhs_v + v]);
+}
+
 __device__ __forceinline__ void out_value(double* hpsi, const double* psi, long long n, int v, int cshift,
                                           long long ldpsi, long long ldh, double sum, double E0, double Esc,
                                           int nb0, long long Nfun) {
@@ -191,7 +211,7 @@ __global__ void __launch_bounds__(256) hpsi_reduce_chunks_kernel(
     const long long ch = t / nrhs_v;
     const int v = (int)(t - ch * nrhs_v);
     double s = 0.0, c = 0.0;
-    for (long long q = chunk_q[ch]; q < chunk_q[ch + 1]; ++q) neumaier_add(s, c, contrib[inv_idx[q] * nrhs_v + v]);
+    chunk_sum(contrib, inv_idx, chunk_q[ch], chunk_q[ch + 1], nrhs_v, v, s, c);
     part[t] = make_double2(s, c);
   }
 }
@@ -283,6 +303,37 @@ __global__ void dfma_peak_kernel(double* out, int iters, double a, double b) {
   out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
 }
 
+// FP64 tensor-core probe: mma.sync m8n8k4 f64 (DMMA; 512 flops per warp
+// instruction) on four independent accumulator tiles per warp, in registers
+// only.  With `dfma` > 0 each step also runs that many DFMA chains per thread
+// beside the MMAs (the mixed probe: do DMMA and DFMA add up, or share a pipe).
+__device__ __forceinline__ void dmma_m8n8k4(double& d0, double& d1, double a, double b) {
+  asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};\n"
+               : "+d"(d0), "+d"(d1)
+               : "d"(a), "d"(b));
+}
+
+__global__ void dmma_peak_kernel(double* out, int iters, int dfma, double a, double b) {
+  double c[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) c[k] = threadIdx.x + k;
+  double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+  const double av = a * (1 + (threadIdx.x & 3)), bv = b * (1 + (threadIdx.x >> 3));
+  for (int i = 0; i < iters; ++i) {
+    dmma_m8n8k4(c[0], c[1], av, bv);
+    dmma_m8n8k4(c[2], c[3], av, bv);
+    dmma_m8n8k4(c[4], c[5], av, bv);
+    dmma_m8n8k4(c[6], c[7], av, bv);
+    if (dfma) {
+      x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    }
+  }
+  double t = x0 + x1 + x2 + x3;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) t += c[k];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = t;
+}
+
 }  // namespace evr
 
 using namespace evr;
@@ -329,7 +380,9 @@ struct evr_sg4_ctx {
   int grid = 0;
   int smem_doubles = 0;
   int geo = 0;                       // launch geometry (1: narrow, D <= EVR_NARROW_FMAX)
-  int rmax = 32;                     // most right-hand sides per work item (evr_sg4_tune)
+  int rmax = 32;                     // most right-hand sides per work item (plan knob)
+  int geo_override = -1;             // launch geometry (plan knob; -1 automatic)
+  int split = 0;                     // mode-pass thread mapping (plan knob)
   // operator
   bool have_op = false;
   int type = -1;
@@ -761,7 +814,7 @@ static void plan_sorted(const evr_sg4_ctx* c, int nrhs_v, std::vector<TermInfo>&
                         std::vector<Item>& sorted, long long& max_need, int& geo) {
   std::vector<float> cost;
   plan_work(c, nrhs_v, geo_smem_bytes(0) / 8, terms, items, cost, max_need);
-  geo = choose_geo(c->D, items.size(), c->num_sms);
+  geo = c->geo_override >= 0 ? c->geo_override : choose_geo(c->D, items.size(), c->num_sms);
   if (geo) plan_work(c, nrhs_v, geo_smem_bytes(geo) / 8, terms, items, cost, max_need);
   std::vector<int> order(items.size());
   std::iota(order.begin(), order.end(), 0);
@@ -855,13 +908,16 @@ static int build_items(evr_sg4_ctx* c, int nrhs_v) {
 static int launch_reduce(evr_sg4_ctx* c, const double* contrib, double2* part, int nrhs_v, int cshift,
                          const double* psi, long long ldpsi, double* hpsi, long long ldh, double E0, double Esc,
                          cudaStream_t s) {
+  // 64-thread blocks, up to 64 per SM: every thread runs a serial chain of
+  // FP64 additions, and GB300's FP64 pipe (about two operations per clock
+  // per SM) wants small reductions spread over all SMs
   const long long t1 = c->n_chunks * nrhs_v, t2 = c->N * nrhs_v;
-  const long long b1 = std::max<long long>(1, std::min<long long>((t1 + 255) / 256, 16LL * c->num_sms));
-  const long long b2 = std::max<long long>(1, std::min<long long>((t2 + 255) / 256, 16LL * c->num_sms));
-  hpsi_reduce_chunks_kernel<<<(unsigned)b1, 256, 0, s>>>(contrib, c->d_chunk_q, c->n_chunks, c->d_inv_idx, nrhs_v,
-                                                        part);
-  hpsi_reduce_join_kernel<<<(unsigned)b2, 256, 0, s>>>(part, c->d_fun_chunk, c->N, nrhs_v, cshift, psi, ldpsi, hpsi,
-                                                      ldh, E0, Esc, c->nb0);
+  const long long b1 = std::max<long long>(1, std::min<long long>((t1 + 63) / 64, 64LL * c->num_sms));
+  const long long b2 = std::max<long long>(1, std::min<long long>((t2 + 63) / 64, 64LL * c->num_sms));
+  hpsi_reduce_chunks_kernel<<<(unsigned)b1, 64, 0, s>>>(contrib, c->d_chunk_q, c->n_chunks, c->d_inv_idx, nrhs_v,
+                                                       part);
+  hpsi_reduce_join_kernel<<<(unsigned)b2, 64, 0, s>>>(part, c->d_fun_chunk, c->N, nrhs_v, cshift, psi, ldpsi, hpsi,
+                                                     ldh, E0, Esc, c->nb0);
   CUDA_TRY(cudaGetLastError());
   return EVR_OK;
 }
@@ -894,6 +950,7 @@ static KParams make_params(evr_sg4_ctx* c, int nrhs_v, int cshift, const double*
   p.F2 = c->d_F2;
   p.F1 = c->d_F1;
   p.t1_mixed = c->type == 1 && t1_mixed(c) ? 1 : 0;
+  p.split = c->split;
   p.type = c->type;
   p.nbuf = nbuf_for(c);
   p.smem_doubles = c->smem_doubles;
@@ -1139,6 +1196,45 @@ extern "C" int evr_probe_fp64_peak(double* tflops) {
   cudaFree(d);
   if (e != cudaSuccess) return set_error(EVR_ERR_CUDA, "probe: %s", cudaGetErrorString(e));
   *tflops = 2.0 * 8 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
+  return EVR_OK;
+}
+
+extern "C" int evr_probe_fp64_pipes(double* dfma_tflops, double* dmma_tflops, double* mixed_tflops) {
+  if (!dfma_tflops || !dmma_tflops || !mixed_tflops) return set_error(EVR_ERR_ARG, "probe: NULL argument");
+  int rc = evr_probe_fp64_peak(dfma_tflops);
+  if (rc) return rc;
+  int dev = 0, sms = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int blocks = 4 * sms, threads = 256, iters = 4096;
+  double* d = nullptr;
+  CUDA_TRY(cudaMalloc(&d, sizeof(double) * blocks * threads));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best[2] = {1e30f, 1e30f};
+  for (int mixed = 0; mixed < 2; ++mixed) {
+    dmma_peak_kernel<<<blocks, threads>>>(d, 64, mixed, 1.0000001, 1e-9);
+    for (int rep = 0; rep < 3; ++rep) {
+      cudaEventRecord(e0);
+      dmma_peak_kernel<<<blocks, threads>>>(d, iters, mixed, 1.0000001, 1e-9);
+      cudaEventRecord(e1);
+      cudaEventSynchronize(e1);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      best[mixed] = std::min(best[mixed], ms);
+    }
+  }
+  cudaError_t e = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(d);
+  if (e != cudaSuccess) return set_error(EVR_ERR_CUDA, "probe: %s", cudaGetErrorString(e));
+  const double warps = (double)blocks * threads / 32.0;
+  const double mma_flops = 4.0 * 512.0 * iters * warps;           // four m8n8k4 per step per warp
+  const double fma_flops = 2.0 * 4.0 * iters * blocks * threads;  // four DFMA per step per thread
+  *dmma_tflops = mma_flops / (best[0] * 1e-3) / 1e12;
+  *mixed_tflops = (mma_flops + fma_flops) / (best[1] * 1e-3) / 1e12;
   return EVR_OK;
 }
 
@@ -1533,6 +1629,72 @@ extern "C" int evr_sg4_hpsi_multi(int n, evr_sg4_ctx* const* ctxs, const int* nr
 }
 
 // ------------------------------------------------------------------------
+// A fixed H.psi: one context applied to fixed device buffers (nrhs real
+// columns, psi -> hpsi, ld = nb0*N, E0 = 0, Esc = 1), with a plan, work list
+// and scratch of its own and its parameter block uploaded once, so a launch
+// is kernels only and can be recorded in a CUDA graph (the context's own
+// cached plan, which other calls re-plan, is not involved).  Same items and
+// arithmetic as evr_sg4_apply, so the same bits.
+// ------------------------------------------------------------------------
+struct evr::BoundApply {
+  evr_sg4_multi* m = nullptr;
+  const double* psi = nullptr;
+  double* hpsi = nullptr;
+  long long ld = 0;
+};
+
+int evr::bound_apply_create(evr_sg4_ctx* c, int nrhs, int transpose, const double* psi, double* hpsi,
+                            BoundApply** out) {
+  *out = nullptr;
+  if (!c || nrhs < 1 || !psi || !hpsi) return set_error(EVR_ERR_ARG, "bound apply: bad arguments");
+  BoundApply* b = new BoundApply();
+  int rc = evr_sg4_multi_create(1, &c, &nrhs, transpose ? EVR_APPLY_TRANSPOSE : 0, &b->m);
+  if (rc) {
+    delete b;
+    return rc;
+  }
+  b->psi = psi;
+  b->hpsi = hpsi;
+  b->ld = c->nvec;
+  evr_sg4_multi* m = b->m;
+  const MGroup& g = m->groups[0];
+  KParams p = make_params(c, m->nrhs_v[0], 0, psi, b->ld, hpsi, b->ld, 1.0);
+  p.transpose = m->transpose;
+  p.smem_doubles = g.smem_doubles;
+  p.terms = m->d_terms[0];
+  p.contrib = m->d_contrib[0];
+  p.gscratch = m->d_scratch;
+  p.scratch_per_cta = g.scratch_per_cta;
+  p.counter = nullptr;
+  p.items = nullptr;
+  if (cudaMemcpy(m->d_params, &p, sizeof(p), cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaGetLastError();
+    bound_apply_destroy(b);
+    return set_error(EVR_ERR_CUDA, "bound apply: parameter upload failed");
+  }
+  *out = b;
+  return EVR_OK;
+}
+
+void evr::bound_apply_destroy(BoundApply* b) {
+  if (!b) return;
+  if (b->m) free_multi(b->m);
+  delete b;
+}
+
+int evr::bound_apply_launch(BoundApply* b, void* stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  evr_sg4_multi* m = b->m;
+  MGroup& g = m->groups[0];
+  CUDA_TRY(cudaMemsetAsync(g.d_counter, 0, sizeof(unsigned int), s));
+  launch_multi(g.geo, g.grid, (size_t)g.smem_doubles * 8, s, m->d_params, g.d_items, (int)g.sorted.size(), 0,
+               g.d_counter);
+  CUDA_TRY(cudaGetLastError());
+  return launch_reduce(m->ctxs[0], m->d_contrib[0], (double2*)m->d_part[0], m->nrhs_v[0], 0, b->psi, b->ld, b->hpsi,
+                       b->ld, 0.0, 1.0, s);
+}
+
+// ------------------------------------------------------------------------
 // Two operators of one basis (H0 and mu of a field-driven propagation)
 // applied to one complex vector in one persistent launch, up to the chunk
 // partials of their ordered accumulations; the caller joins them (and fuses
@@ -1543,49 +1705,54 @@ extern "C" int evr_sg4_hpsi_multi(int n, evr_sg4_ctx* const* ctxs, const int* nr
 // ------------------------------------------------------------------------
 struct evr::FieldPair {
   evr_sg4_multi* m = nullptr;
-  double* x = nullptr;         // [N] complex input
-  double2* part = nullptr;     // [2][n_chunks][2]
+  double* x = nullptr;         // [nrhs][N] complex input
+  double2* part = nullptr;     // [2][n_chunks][2 nrhs]
   int grid = 0;
+  int nrhs = 1;
   long long N = 0;
 };
 
+// Chunk sums of both operators: thread t = (op, chunk, virtual column v),
+// op-major, then chunk, then column (nrhs_v = 2 nrhs: re/im of each packet).
 __global__ void __launch_bounds__(256) pair_chunks_kernel(const double* __restrict__ contrib0,
                                                           const double* __restrict__ contrib1,
                                                           const long long* __restrict__ chunk_q, long long n_chunks,
-                                                          const long long* __restrict__ inv_idx,
+                                                          const long long* __restrict__ inv_idx, int nrhs_v,
                                                           double2* __restrict__ part, unsigned int* counter) {
   if (blockIdx.x == 0 && threadIdx.x == 0) *counter = 0u;  // the item kernel before this one has finished
-  const long long per = n_chunks * 2, total = 2 * per;
+  const long long per = n_chunks * nrhs_v, total = 2 * per;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
        t += (long long)gridDim.x * blockDim.x) {
     const int op = t >= per ? 1 : 0;
     const long long r = t - op * per;
-    const long long ch = r >> 1;
-    const int v = (int)(r & 1);
+    const long long ch = r / nrhs_v;
+    const int v = (int)(r - ch * nrhs_v);
     const double* contrib = op ? contrib1 : contrib0;
     double s = 0.0, c = 0.0;
-    for (long long q = chunk_q[ch]; q < chunk_q[ch + 1]; ++q) neumaier_add(s, c, contrib[inv_idx[q] * 2 + v]);
+    chunk_sum(contrib, inv_idx, chunk_q[ch], chunk_q[ch + 1], nrhs_v, v, s, c);
     part[t] = make_double2(s, c);
   }
 }
 
-int evr::field_pair_create(evr_sg4_ctx* a, evr_sg4_ctx* b, int transpose, FieldPair** out) {
+int evr::field_pair_create(evr_sg4_ctx* a, evr_sg4_ctx* b, int transpose, int nrhs, FieldPair** out) {
   *out = nullptr;
   if (!a || !b) return set_error(EVR_ERR_ARG, "field pair: NULL context");
+  if (nrhs < 1) return set_error(EVR_ERR_ARG, "field pair: nrhs < 1");
   if (a->N != b->N || a->nb_SG != b->nb_SG || a->z.sum_nb != b->z.sum_nb || a->n_chunks != b->n_chunks)
     return set_error(EVR_ERR_ARG, "field pair: the two operators are on different bases");
   if (a->nb0 != 1 || b->nb0 != 1) return set_error(EVR_ERR_ARG, "field pair: one channel (nb0 = 1) only");
   evr_sg4_ctx* cs[2] = {a, b};
-  const int nrhs[2] = {1, 1};
+  const int nr[2] = {nrhs, nrhs};
   FieldPair* f = new FieldPair();
-  int rc = evr_sg4_multi_create(2, cs, nrhs, EVR_APPLY_COMPLEX | (transpose ? EVR_APPLY_TRANSPOSE : 0), &f->m);
+  int rc = evr_sg4_multi_create(2, cs, nr, EVR_APPLY_COMPLEX | (transpose ? EVR_APPLY_TRANSPOSE : 0), &f->m);
   if (rc) {
     delete f;
     return rc;
   }
   f->N = a->N;
-  if (cudaMalloc(&f->x, (size_t)a->N * 16) != cudaSuccess ||
-      cudaMalloc(&f->part, (size_t)a->n_chunks * 4 * sizeof(double2)) != cudaSuccess) {
+  f->nrhs = nrhs;
+  if (cudaMalloc(&f->x, (size_t)a->N * nrhs * 16) != cudaSuccess ||
+      cudaMalloc(&f->part, (size_t)a->n_chunks * 4 * nrhs * sizeof(double2)) != cudaSuccess) {
     cudaGetLastError();
     field_pair_destroy(f);
     return set_error(EVR_ERR_CUDA, "field pair: device allocation failed");
@@ -1594,7 +1761,7 @@ int evr::field_pair_create(evr_sg4_ctx* a, evr_sg4_ctx* b, int transpose, FieldP
   const MGroup& g = m->groups[0];  // one basis, one launch group
   KParams ps[2];
   for (int k = 0; k < 2; ++k) {
-    ps[k] = make_params(cs[k], 2, 1, f->x, 2 * a->N, nullptr, 2 * a->N, 1.0);
+    ps[k] = make_params(cs[k], 2 * nrhs, 1, f->x, 2 * a->N, nullptr, 2 * a->N, 1.0);
     ps[k].transpose = m->transpose;
     ps[k].smem_doubles = g.smem_doubles;
     ps[k].terms = m->d_terms[k];
@@ -1631,10 +1798,13 @@ int evr::field_pair_apply(FieldPair* f, void* stream) {
   const MGroup& g = m->groups[0];
   launch_multi(g.geo, f->grid, (size_t)g.smem_doubles * 8, s, m->d_params, g.d_items, (int)g.sorted.size(), 0,
                g.d_counter);
-  const long long t1 = c->n_chunks * 4;
-  const long long b1 = std::max<long long>(1, std::min<long long>((t1 + 255) / 256, 16LL * c->num_sms));
-  pair_chunks_kernel<<<(unsigned)b1, 256, 0, s>>>(m->d_contrib[0], m->d_contrib[1], c->d_chunk_q, c->n_chunks,
-                                                 c->d_inv_idx, f->part, g.d_counter);
+  // 64-thread blocks: the Neumaier sums are FP64 chains, and GB300's FP64
+  // pipe (about two operations per clock per SM) wants them on many SMs
+  const int nrhs_v = 2 * f->nrhs;
+  const long long t1 = c->n_chunks * 2 * nrhs_v;
+  const long long b1 = std::max<long long>(1, std::min<long long>((t1 + 63) / 64, 64LL * c->num_sms));
+  pair_chunks_kernel<<<(unsigned)b1, 64, 0, s>>>(m->d_contrib[0], m->d_contrib[1], c->d_chunk_q, c->n_chunks,
+                                                 c->d_inv_idx, nrhs_v, f->part, g.d_counter);
   CUDA_TRY(cudaGetLastError());
   return EVR_OK;
 }
@@ -1644,26 +1814,121 @@ evr::FieldPairView evr::field_pair_view(const FieldPair* f) {
   const evr_sg4_ctx* c = f->m->ctxs[0];
   v.N = f->N;
   v.n_chunks = c->n_chunks;
+  v.nrhs = f->nrhs;
   v.fun_chunk = c->d_fun_chunk;
   v.part = f->part;
   v.x = f->x;
   return v;
 }
 
+
 // ------------------------------------------------------------------------
-// Autotuner: the most right-hand sides one work item carries trades reuse of
-// the 1-D matrices and operator fields (large blocks) against the number and
-// balance of items (small blocks).  Times H.psi on nrhs vectors for each
-// candidate and keeps the fastest, as Tune_SG4threads_HPsi
-// (SRC/sub_main/vib.f90:2013-2123) times H.psi for each OpenMP thread count.
+// Plan knobs and the autotuner (the counterpart of Tune_SG4threads_HPsi,
+// SRC/sub_main/vib.f90:2013-2123, which times H.psi for each OpenMP thread
+// count and keeps the fastest).  The knobs of a work plan are the launch
+// geometry (wide, narrow, mid: CTAs per SM against shared memory and
+// registers per item), the most right-hand sides one work item carries
+// (reuse of the 1-D matrices and operator fields against the number and
+// balance of items) and the thread mapping of the mode passes (one thread
+// per fibre, per output element, or chosen per pass).  None of them changes
+// the arithmetic of a term and right-hand side, so results are the same bits
+// for every setting.  The tuner times H.psi for each candidate on the
+// caller's block size and keeps the fastest, and records it in a JSON file
+// keyed by the shape of the workload, so later runs apply it without timing.
 // ------------------------------------------------------------------------
-extern "C" int evr_sg4_tune(evr_sg4_ctx* c, int nrhs, int flags, int* best_rmax, double* best_ms) {
+extern "C" int evr_sg4_set_plan(evr_sg4_ctx* c, int geo, int rmax, int split) {
+  if (!c) return set_error(EVR_ERR_ARG, "set_plan: NULL context");
+  if (geo < -1 || geo > 2) return set_error(EVR_ERR_ARG, "set_plan: geometry %d not in {-1, 0, 1, 2}", geo);
+  if (geo == 1 && c->D > EVR_NARROW_FMAX)
+    return set_error(EVR_ERR_ARG, "set_plan: the narrow geometry takes D <= %d (D = %d)", EVR_NARROW_FMAX, c->D);
+  if (rmax < 1 || rmax > 32) return set_error(EVR_ERR_ARG, "set_plan: rmax %d not in [1, 32]", rmax);
+  if (split < 0 || split > 2) return set_error(EVR_ERR_ARG, "set_plan: split %d not in {0, 1, 2}", split);
+  c->geo_override = geo;
+  c->rmax = rmax;
+  c->split = split;
+  c->items_nrhs = -1;
+  return EVR_OK;
+}
+
+extern "C" int evr_sg4_get_plan(const evr_sg4_ctx* c, int* geo, int* rmax, int* split) {
+  if (!c || !geo || !rmax || !split) return set_error(EVR_ERR_ARG, "get_plan: NULL argument");
+  *geo = c->geo_override;
+  *rmax = c->rmax;
+  *split = c->split;
+  return EVR_OK;
+}
+
+namespace evr {
+
+// cache key of a workload shape
+static std::string tune_key(const evr_sg4_ctx* c, int nrhs, int flags) {
+  char k[160];
+  snprintf(k, sizeof(k), "D%d_L%d_LB%d_T%d_NB0%d_N%lld_R%d_C%d_G%d", c->D, c->L, c->LB, c->type, c->nb0, c->N, nrhs,
+           (flags & EVR_APPLY_COMPLEX) ? 1 : 0, c->d_G ? 1 : 0);
+  return k;
+}
+
+struct TuneEntry {
+  int geo = -1, rmax = 32, split = 0;
+  double ms = 0.0, default_ms = 0.0;
+};
+
+// The cache: one JSON object, one entry per line,
+//   "key": {"geo": g, "rmax": r, "split": s, "ms": t, "default_ms": t0},
+static void tune_cache_read(const char* path, std::vector<std::pair<std::string, TuneEntry>>& out) {
+  out.clear();
+  FILE* f = fopen(path, "r");
+  if (!f) return;
+  char line[512];
+  while (fgets(line, sizeof(line), f)) {
+    char key[200];
+    TuneEntry e;
+    if (sscanf(line, " \"%199[^\"]\": {\"geo\": %d, \"rmax\": %d, \"split\": %d, \"ms\": %lf, \"default_ms\": %lf", key,
+               &e.geo, &e.rmax, &e.split, &e.ms, &e.default_ms) == 6)
+      out.emplace_back(key, e);
+  }
+  fclose(f);
+}
+
+static int tune_cache_write(const char* path, const std::vector<std::pair<std::string, TuneEntry>>& in) {
+  const std::string tmp = std::string(path) + ".tmp";
+  FILE* f = fopen(tmp.c_str(), "w");
+  if (!f) return set_error(EVR_ERR_ARG, "tune: cannot write the cache %s", path);
+  fprintf(f, "{\n");
+  for (size_t k = 0; k < in.size(); ++k) {
+    const TuneEntry& e = in[k].second;
+    fprintf(f, "  \"%s\": {\"geo\": %d, \"rmax\": %d, \"split\": %d, \"ms\": %.6f, \"default_ms\": %.6f}%s\n",
+            in[k].first.c_str(), e.geo, e.rmax, e.split, e.ms, e.default_ms, k + 1 < in.size() ? "," : "");
+  }
+  fprintf(f, "}\n");
+  fclose(f);
+  if (rename(tmp.c_str(), path) != 0) return set_error(EVR_ERR_ARG, "tune: cannot replace the cache %s", path);
+  return EVR_OK;
+}
+
+}  // namespace evr
+
+extern "C" int evr_sg4_tune_plan(evr_sg4_ctx* c, int nrhs, int flags, const char* cache_path, evr_tune_result* res) {
   if (!c || nrhs < 1) return set_error(EVR_ERR_ARG, "tune: NULL context or nrhs < 1");
   if (!c->have_op) return set_error(EVR_ERR_STATE, "tune: set_operator was not called");
   if (flags & ~EVR_APPLY_COMPLEX) return set_error(EVR_ERR_ARG, "tune: flags may only hold EVR_APPLY_COMPLEX");
+  const std::string key = tune_key(c, nrhs, flags);
+  std::vector<std::pair<std::string, TuneEntry>> cache;
+  if (cache_path) {
+    tune_cache_read(cache_path, cache);
+    for (const auto& kv : cache)
+      if (kv.first == key) {
+        int rc = evr_sg4_set_plan(c, kv.second.geo, kv.second.rmax, kv.second.split);
+        if (rc) return rc;
+        if (res) *res = evr_tune_result{kv.second.geo, kv.second.rmax, kv.second.split, kv.second.ms,
+                                        kv.second.default_ms, 1};
+        return EVR_OK;
+      }
+  }
   const size_t n = (size_t)c->nvec * nrhs * ((flags & EVR_APPLY_COMPLEX) ? 2 : 1);
   double *psi = nullptr, *out = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
+  const int keep_geo = c->geo_override, keep_rmax = c->rmax, keep_split = c->split;
   auto cleanup = [&]() {
     if (psi) cudaFree(psi);
     if (out) cudaFree(out);
@@ -1688,37 +1953,69 @@ extern "C" int evr_sg4_tune(evr_sg4_ctx* c, int nrhs, int flags, int* best_rmax,
       return set_error(EVR_ERR_CUDA, "tune: upload failed");
     }
   }
-  const int keep = c->rmax;
-  int best = keep;
-  double best_t = 1e300;
-  for (int rmax : {1, 2, 4, 8, 16, 32}) {
-    c->rmax = rmax;
-    c->items_nrhs = -1;
-    int rc = evr_sg4_apply(c, flags, nrhs, psi, c->nvec, out, c->nvec, 0.0, 1.0, nullptr);  // plan + warm
-    float ms = 0.f, tot = 0.f;
+  // time one plan: one untimed H.psi (plans the items), then the best of three
+  auto time_plan = [&](int geo, int rmax, int split, double* ms_out) -> int {
+    int rc = evr_sg4_set_plan(c, geo, rmax, split);
+    if (!rc) rc = evr_sg4_apply(c, flags, nrhs, psi, c->nvec, out, c->nvec, 0.0, 1.0, nullptr);
+    double best = 1e300;
     for (int rep = 0; rep < 3 && !rc; ++rep) {
+      float ms = 0.f;
       cudaEventRecord(e0, 0);
       rc = evr_sg4_apply(c, flags, nrhs, psi, c->nvec, out, c->nvec, 0.0, 1.0, nullptr);
       cudaEventRecord(e1, 0);
-      if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+      if (!rc && (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
         rc = set_error(EVR_ERR_CUDA, "tune: timing failed");
-      tot += ms;
+      best = std::min(best, (double)ms);
     }
-    if (rc) {
-      c->rmax = keep;
-      c->items_nrhs = -1;
-      cleanup();
-      return rc;
+    *ms_out = best;
+    return rc;
+  };
+  TuneEntry best;
+  int rc = time_plan(-1, 32, 0, &best.default_ms);  // the automatic plan first
+  if (!rc) {
+    best.ms = best.default_ms;
+    int auto_geo = 0;
+    {
+      std::vector<TermInfo> terms;
+      std::vector<Item> items, sorted;
+      long long need = 0;
+      plan_sorted(c, ((nrhs * c->nb0) << ((flags & EVR_APPLY_COMPLEX) ? 1 : 0)), terms, items, sorted, need, auto_geo);
     }
-    if (tot / 3.0 < best_t) {
-      best_t = tot / 3.0;
-      best = rmax;
-    }
+    best.geo = auto_geo;
+    std::vector<int> geos = {0, 2};
+    if (c->D <= EVR_NARROW_FMAX) geos.push_back(1);
+    for (int geo : geos)
+      for (int rmax : {4, 8, 16, 32})
+        for (int split : {0, 1, 2}) {
+          double ms = 0.0;
+          if ((rc = time_plan(geo, rmax, split, &ms))) break;
+          if (ms < best.ms) {
+            best.ms = ms;
+            best.geo = geo;
+            best.rmax = rmax;
+            best.split = split;
+          }
+        }
   }
-  c->rmax = best;
-  c->items_nrhs = -1;
   cleanup();
-  if (best_rmax) *best_rmax = best;
-  if (best_ms) *best_ms = best_t;
+  if (rc) {
+    evr_sg4_set_plan(c, keep_geo, keep_rmax, keep_split);
+    return rc;
+  }
+  if ((rc = evr_sg4_set_plan(c, best.geo, best.rmax, best.split))) return rc;
+  if (cache_path) {
+    cache.emplace_back(key, best);
+    if ((rc = tune_cache_write(cache_path, cache))) return rc;
+  }
+  if (res) *res = evr_tune_result{best.geo, best.rmax, best.split, best.ms, best.default_ms, 0};
+  return EVR_OK;
+}
+
+extern "C" int evr_sg4_tune(evr_sg4_ctx* c, int nrhs, int flags, int* best_rmax, double* best_ms) {
+  evr_tune_result r;
+  int rc = evr_sg4_tune_plan(c, nrhs, flags, nullptr, &r);
+  if (rc) return rc;
+  if (best_rmax) *best_rmax = r.rmax;
+  if (best_ms) *best_ms = r.ms;
   return EVR_OK;
 }

@@ -28,21 +28,30 @@ struct DescSizes {
 int set_error(int code, const char* fmt, ...);
 int desc_sizes(const evr_sg4_desc* d, DescSizes* z);
 
-// Two operators on one basis applied to one complex vector in one launch,
+// Two operators on one basis applied to nrhs complex vectors in one launch,
 // up to the chunk partials of both ordered accumulations (part: [2][n_chunks]
-// [re, im] (s, c) pairs, operator 0 first); `x` is the device input vector
-// (N complex) of every apply.  `transpose` applies both transposed.
+// [2 nrhs] (s, c) pairs: operator 0 first, then chunk, then re/im of each
+// vector); `x` is the device input block (N x nrhs complex, ld N) of every
+// apply.  `transpose` applies both transposed.
 struct FieldPair;
 struct FieldPairView {
   long long N = 0, n_chunks = 0;
+  int nrhs = 1;
   const long long* fun_chunk = nullptr;  // [N+1] first chunk of each packed function
   const void* part = nullptr;            // double2 partials
   double* x = nullptr;
 };
-int field_pair_create(evr_sg4_ctx* a, evr_sg4_ctx* b, int transpose, FieldPair** out);
+int field_pair_create(evr_sg4_ctx* a, evr_sg4_ctx* b, int transpose, int nrhs, FieldPair** out);
 void field_pair_destroy(FieldPair* f);
 int field_pair_apply(FieldPair* f, void* stream);
 FieldPairView field_pair_view(const FieldPair* f);
+// One context applied to fixed device buffers (nrhs real columns, ld nb0*N,
+// E0 = 0, Esc = 1) with a plan and scratch of its own and parameters uploaded
+// once: a launch enqueues kernels and a memset only (graph-recordable).
+struct BoundApply;
+int bound_apply_create(evr_sg4_ctx* c, int nrhs, int transpose, const double* psi, double* hpsi, BoundApply** out);
+int bound_apply_launch(BoundApply* b, void* stream);
+void bound_apply_destroy(BoundApply* b);
 // Contexts, right-hand sides per context, complex shift and transpose flag
 // of a multi-context plan.
 void multi_shape(const evr_sg4_multi* m, std::vector<evr_sg4_ctx*>* ctxs, std::vector<int>* nrhs, int* cshift,

@@ -141,6 +141,7 @@ struct KParams {
   long long Nfun;            // packed basis functions per channel
   long long vstride;         // V[(a*nb0 + b)*vstride + point] for nb0 > 1
   int t1_mixed;              // type 1: some F2_ij (i < j) or F1_i is non-zero
+  int split;                 // mode passes: 0 per-pass choice, 1 one thread per fibre, 2 per output
 };
 
 struct ItemShared {
@@ -289,11 +290,15 @@ __device__ __forceinline__ void mode_pass_split(const double* __restrict__ M, in
   }
 }
 
+// split: 0 picks per pass (one thread per output element when that gives a
+// shorter critical path), 1 keeps one thread per fibre, 2 splits whenever a
+// fibre has more than one output (a plan knob of the autotuner; the FMA
+// chain of every output is the same either way).
 template <int MODE>
 __device__ __noinline__ void mode_pass_m(const double* M, int nin, int nout, int S, int R, const double* in, double* out,
-                            double scale) {
+                            double scale, int split) {
   const int nf = S * R, T = blockDim.x;
-  if (nout > 1 && (nf * nout + T - 1) / T < ((nf + T - 1) / T) * nout) {
+  if (nout > 1 && split != 1 && (split == 2 || (nf * nout + T - 1) / T < ((nf + T - 1) / T) * nout)) {
     switch (nin) {
 #define EVR_CASE(n) \
   case n:           \
@@ -316,10 +321,10 @@ __device__ __noinline__ void mode_pass_m(const double* M, int nin, int nout, int
 }
 
 static __device__ void mode_pass(const double* M, int nin, int nout, int S, int R, const double* in, double* out,
-                          bool acc, double scale) {
-  if (!acc) mode_pass_m<0>(M, nin, nout, S, R, in, out, 1.0);
-  else if (scale == 1.0) mode_pass_m<1>(M, nin, nout, S, R, in, out, 1.0);
-  else mode_pass_m<2>(M, nin, nout, S, R, in, out, scale);
+                          bool acc, double scale, int split) {
+  if (!acc) mode_pass_m<0>(M, nin, nout, S, R, in, out, 1.0, split);
+  else if (scale == 1.0) mode_pass_m<1>(M, nin, nout, S, R, in, out, 1.0, split);
+  else mode_pass_m<2>(M, nin, nout, S, R, in, out, scale, split);
 }
 
 // Derivative pass along mode i on the grid (DerivOp_TO_RDP_OF_SmolaykRep).
@@ -330,7 +335,7 @@ static __device__ void grid_deriv(const KParams& p, const ItemShared& it, int i,
     if (j < i) S *= it.nq[j];
     else if (j > i) R *= it.nq[j];
   }
-  mode_pass(p.mats + it.mo[i][which], it.nq[i], it.nq[i], S, R, in, out, acc, scale);
+  mode_pass(p.mats + it.mo[i][which], it.nq[i], it.nq[i], S, R, in, out, acc, scale, p.split);
 }
 
 // basis->grid (to_grid, BDP_TO_GDP) or grid->basis (GDP_TO_BDP).  The
@@ -353,7 +358,7 @@ static __device__ double* transform(const KParams& p, const ItemShared& it, bool
       if (j < i) S *= c;
       else if (j > i) R *= c;
     }
-    mode_pass(p.mats + it.mo[i][to_grid ? M_BG : M_GB], nin, nout, S, R, a, b, false, 1.0);
+    mode_pass(p.mats + it.mo[i][to_grid ? M_BG : M_GB], nin, nout, S, R, a, b, false, 1.0, p.split);
     __syncthreads();
     double* t = a;
     a = b;

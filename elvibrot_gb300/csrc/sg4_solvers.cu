@@ -180,6 +180,184 @@ extern "C" int evr_sg4_diagonal(evr_sg4_ctx* c, double* diag, void* stream) {
   return EVR_OK;
 }
 
+// w *= 1/nrm when nrm > tol (the new direction survives), else w = 0 (it is
+// dropped; the Davidson basis keeps a zero column in that slot)
+__global__ void dav_scale_or_drop_kernel(double* w, long long N, const double* nrm, double tol, int* alive) {
+  const double r = *nrm;
+  const bool keep = r > tol;
+  const double f = keep ? 1.0 / r : 0.0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *alive = keep ? 1 : 0;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < N; e += (long long)gridDim.x * blockDim.x)
+    w[e] *= f;
+}
+
+// dst(:, m + j) = src(:, j), j < ncols, with m read from the device
+__global__ void dav_place_kernel(const double* src, double* dst, long long N, int ncols, const int* m_dev) {
+  const long long off = (long long)(*m_dev) * N;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < N * ncols;
+       e += (long long)gridDim.x * blockDim.x)
+    dst[off + e] = src[e];
+}
+
+namespace evr {
+
+// Parameters of one Davidson phase, written by the host into pinned memory
+// before the phase runs and copied to the device as the phase's first step
+// (a node of its graph): the Ritz coefficients Y (mmax x nev, zero rows for
+// unused slots), the Ritz values, the slot where new directions go and the
+// residual columns to expand.
+struct DavParams {
+  int m;
+  int ncols;
+  int pad[2];
+  // followed by: int cols[blk] (padded to 8 bytes), double theta[nev], double Y[mmax*nev]
+};
+
+struct DavState {
+  evr_sg4_ctx* c = nullptr;
+  cublasHandle_t h = nullptr;
+  cudaStream_t s = nullptr;
+  long long N = 0;
+  int nev = 0, blk = 0, mmax = 0;
+  bool sym = false;
+  const double* diag = nullptr;
+  double *V = nullptr, *HV = nullptr, *X = nullptr, *R = nullptr, *W = nullptr, *HW = nullptr, *tmp = nullptr;
+  double *Tt = nullptr, *T = nullptr, *cv = nullptr, *nrm = nullptr;
+  unsigned char* dparams = nullptr;  // device copy of the parameter block
+  unsigned char* hparams = nullptr;  // pinned
+  size_t params_bytes = 0;
+  double* h_T = nullptr;             // pinned: mmax x mmax
+  double* h_nrm = nullptr;           // pinned: nev residual norms, then blk norms of new directions
+  int* d_alive = nullptr;
+  int* h_alive = nullptr;            // pinned: blk
+  int* dm() const { return (int*)dparams; }
+  int* dcols() const { return (int*)(dparams + sizeof(DavParams)); }
+  size_t cols_bytes() const { return ((size_t)blk * sizeof(int) + 7) / 8 * 8; }
+  double* dtheta() const { return (double*)(dparams + sizeof(DavParams) + cols_bytes()); }
+  double* dY() const { return dtheta() + nev; }
+  int* hcols() const { return (int*)(hparams + sizeof(DavParams)); }
+  double* htheta() const { return (double*)(hparams + sizeof(DavParams) + cols_bytes()); }
+  double* hY() const { return htheta() + nev; }
+};
+
+static int ew_blocks(long long n) { return (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 1024)); }
+
+// Ritz vectors X = V Y, R = HV Y - X theta and the residual norms (into pinned
+// memory).  Fixed sizes (all mmax slots; unused slots are zero columns with
+// zero rows of Y), so one recorded graph serves every iteration.
+static int dav_phase_ritz(DavState& d, cudaStream_t s) {
+  const double one = 1.0, zero = 0.0;
+  const int N = (int)d.N;
+  CUBLAS_TRY(cublasSetStream(d.h, s));
+  CUDA_TRY_S(cudaMemcpyAsync(d.dparams, d.hparams, d.params_bytes, cudaMemcpyHostToDevice, s));
+  CUBLAS_TRY(cublasDgemm(d.h, CUBLAS_OP_N, CUBLAS_OP_N, N, d.nev, d.mmax, &one, d.V, N, d.dY(), d.mmax, &zero, d.X, N));
+  CUBLAS_TRY(cublasDgemm(d.h, CUBLAS_OP_N, CUBLAS_OP_N, N, d.nev, d.mmax, &one, d.HV, N, d.dY(), d.mmax, &zero, d.R, N));
+  residual_kernel<<<256, 256, 0, s>>>(d.R, d.X, d.dtheta(), d.N, d.nev);
+  CUDA_TRY_S(cudaGetLastError());
+  CUBLAS_TRY(cublasSetPointerMode(d.h, CUBLAS_POINTER_MODE_DEVICE));
+  for (int j = 0; j < d.nev; ++j) {
+    cublasStatus_t st = cublasDnrm2(d.h, N, d.R + (size_t)j * N, 1, d.nrm + j);
+    if (st != CUBLAS_STATUS_SUCCESS) {
+      cublasSetPointerMode(d.h, CUBLAS_POINTER_MODE_HOST);
+      return set_error(EVR_ERR_CUDA, "davidson: cublasDnrm2 status %d", (int)st);
+    }
+  }
+  CUBLAS_TRY(cublasSetPointerMode(d.h, CUBLAS_POINTER_MODE_HOST));
+  CUDA_TRY_S(cudaMemcpyAsync(d.h_nrm, d.nrm, (size_t)d.nev * 8, cudaMemcpyDeviceToHost, s));
+  return EVR_OK;
+}
+
+// Expansion by nw new directions W: the Davidson correction of the residual
+// columns `cols` (precond) or the caller's block as given, orthonormalised
+// against V (classical Gram-Schmidt, twice) and among themselves (modified
+// Gram-Schmidt, two passes per column; a direction whose norm falls below
+// 1e-10 is dropped, left as a zero column), placed in slots m..m+nw-1, H_s
+// applied, and the projected matrix T = V^T HV (all mmax slots) copied to
+// pinned memory with the survivor flags.  Every size is fixed for a given nw.
+template <class A>
+static int dav_phase_expand(DavState& d, int nw, bool precond, cudaStream_t s, A&& apply) {
+  const double one = 1.0, zero = 0.0, mone = -1.0;
+  const int N = (int)d.N;
+  CUBLAS_TRY(cublasSetStream(d.h, s));
+  CUDA_TRY_S(cudaMemcpyAsync(d.dparams, d.hparams, d.params_bytes, cudaMemcpyHostToDevice, s));
+  if (precond) {
+    precond_kernel<<<256, 256, 0, s>>>(d.W, d.R, d.diag, d.dtheta(), d.dcols(), d.N, nw);
+    CUDA_TRY_S(cudaGetLastError());
+  }
+  for (int pass = 0; pass < 2; ++pass) {  // against V (unused slots are zero)
+    CUBLAS_TRY(cublasDgemm(d.h, CUBLAS_OP_T, CUBLAS_OP_N, d.mmax, nw, N, &one, d.V, N, d.W, N, &zero, d.Tt, d.mmax));
+    CUBLAS_TRY(cublasDgemm(d.h, CUBLAS_OP_N, CUBLAS_OP_N, N, nw, d.mmax, &mone, d.V, N, d.Tt, d.mmax, &one, d.W, N));
+  }
+  for (int j = 0; j < nw; ++j) {
+    double* wj = d.W + (size_t)j * N;
+    for (int pass = 0; pass < 2 && j > 0; ++pass) {
+      CUBLAS_TRY(cublasDgemv(d.h, CUBLAS_OP_T, N, j, &one, d.W, N, wj, 1, &zero, d.cv, 1));
+      CUBLAS_TRY(cublasDgemv(d.h, CUBLAS_OP_N, N, j, &mone, d.W, N, d.cv, 1, &one, wj, 1));
+    }
+    CUBLAS_TRY(cublasSetPointerMode(d.h, CUBLAS_POINTER_MODE_DEVICE));
+    cublasStatus_t st = cublasDnrm2(d.h, N, wj, 1, d.nrm + d.nev + j);
+    CUBLAS_TRY(cublasSetPointerMode(d.h, CUBLAS_POINTER_MODE_HOST));
+    if (st != CUBLAS_STATUS_SUCCESS) return set_error(EVR_ERR_CUDA, "davidson: cublasDnrm2 status %d", (int)st);
+    dav_scale_or_drop_kernel<<<ew_blocks(d.N), 256, 0, s>>>(wj, d.N, d.nrm + d.nev + j, 1e-10, d.d_alive + j);
+  }
+  dav_place_kernel<<<ew_blocks(d.N * nw), 256, 0, s>>>(d.W, d.V, d.N, nw, d.dm());
+  CUDA_TRY_S(cudaGetLastError());
+  int rc = apply(nw, s);
+  if (rc) return rc;
+  dav_place_kernel<<<ew_blocks(d.N * nw), 256, 0, s>>>(d.HW, d.HV, d.N, nw, d.dm());
+  CUDA_TRY_S(cudaGetLastError());
+  CUBLAS_TRY(cublasDgemm(d.h, CUBLAS_OP_T, CUBLAS_OP_N, d.mmax, d.mmax, N, &one, d.V, N, d.HV, N, &zero, d.T, d.mmax));
+  CUDA_TRY_S(cudaMemcpyAsync(d.h_T, d.T, (size_t)d.mmax * d.mmax * 8, cudaMemcpyDeviceToHost, s));
+  CUDA_TRY_S(cudaMemcpyAsync(d.h_alive, d.d_alive, (size_t)nw * sizeof(int), cudaMemcpyDeviceToHost, s));
+  return EVR_OK;
+}
+
+// A phase run eagerly, or recorded once as a CUDA graph (keyed by its shape)
+// and replayed.  The first run of each shape is eager: it also sizes the
+// H.psi plan for that block, which allocates, and allocation cannot be
+// recorded.
+struct DavGraphs {
+  std::vector<cudaGraphExec_t> exec;  // [0]: Ritz phase; [1 + nw]: expansion by nw
+  std::vector<char> seen;
+  cudaStream_t cs = nullptr;
+  ~DavGraphs() {
+    for (cudaGraphExec_t e : exec)
+      if (e) cudaGraphExecDestroy(e);
+    if (cs) cudaStreamDestroy(cs);
+  }
+};
+
+template <class F>
+static int dav_run(DavGraphs& g, int key, bool graph, cudaStream_t s, F&& enqueue) {
+  if (!graph || !g.seen[key]) {
+    g.seen[key] = 1;
+    return enqueue(s);
+  }
+  if (!g.exec[key]) {
+    if (!g.cs) CUDA_TRY_S(cudaStreamCreateWithFlags(&g.cs, cudaStreamNonBlocking));
+    CUDA_TRY_S(cudaStreamSynchronize(s));
+    cudaGraph_t gr = nullptr;
+    CUDA_TRY_S(cudaStreamBeginCapture(g.cs, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue(g.cs);
+    cudaError_t ec = cudaStreamEndCapture(g.cs, &gr);
+    if (rc) {
+      if (gr) cudaGraphDestroy(gr);
+      return rc;
+    }
+    if (ec != cudaSuccess) return set_error(EVR_ERR_CUDA, "davidson: graph capture: %s", cudaGetErrorString(ec));
+    ec = cudaGraphInstantiate(&g.exec[key], gr, 0);
+    cudaGraphDestroy(gr);
+    if (ec != cudaSuccess) {
+      g.exec[key] = nullptr;
+      return set_error(EVR_ERR_CUDA, "davidson: graph instantiate: %s", cudaGetErrorString(ec));
+    }
+  }
+  CUDA_TRY_S(cudaGraphLaunch(g.exec[key], s));
+  return EVR_OK;
+}
+
+}  // namespace evr
+
 extern "C" int evr_sg4_davidson(evr_sg4_ctx* c, const evr_davidson_opts* o, const double* guess, int nguess,
                                 const double* diag, double* evals, double* evecs, double* resid, int* iterations,
                                 void* stream) {
@@ -193,130 +371,193 @@ extern "C" int evr_sg4_davidson(evr_sg4_ctx* c, const evr_davidson_opts* o, cons
   const int mmax = o->max_subspace > 0 ? o->max_subspace : std::max(3 * nev, nev + 2 * blk);
   if (nev < 1 || nev > N || blk < 1 || mmax < nev + blk || mmax > N || o->max_it < 1 || !(o->conv_resi > 0))
     return set_error(EVR_ERR_ARG, "davidson: need 1 <= nev, block >= 1, nev+block <= max_subspace <= N, conv_resi > 0");
-  const bool sym = o->symmetrize != 0;
+  if (N > 2147483647LL) return set_error(EVR_ERR_ARG, "davidson: N exceeds the int range of cuBLAS");
   cudaStream_t s = (cudaStream_t)stream;
-  cublasHandle_t h = nullptr;
-  CUBLAS_TRY(cublasCreate(&h));
-  struct HGuard {
-    cublasHandle_t h;
-    ~HGuard() { cublasDestroy(h); }
-  } hg{h};
-  CUBLAS_TRY(cublasSetStream(h, s));
-  DevBuf V, HV, X, R, T, W, tmp, Y, th, colsb;
-  CUDA_TRY_S(cudaMalloc(&V.p, (size_t)N * mmax * 8));
-  CUDA_TRY_S(cudaMalloc(&HV.p, (size_t)N * mmax * 8));
-  CUDA_TRY_S(cudaMalloc(&X.p, (size_t)N * nev * 8));
-  CUDA_TRY_S(cudaMalloc(&R.p, (size_t)N * nev * 8));
-  CUDA_TRY_S(cudaMalloc(&W.p, (size_t)N * std::max(nev, blk) * 8));
-  CUDA_TRY_S(cudaMalloc(&tmp.p, (size_t)N * mmax * 8));
-  CUDA_TRY_S(cudaMalloc(&T.p, (size_t)mmax * mmax * 8));
-  CUDA_TRY_S(cudaMalloc(&Y.p, (size_t)mmax * nev * 8));
-  CUDA_TRY_S(cudaMalloc(&th.p, (size_t)nev * 8));
-  CUDA_TRY_S(cudaMalloc(&colsb.p, (size_t)blk * 8));
-  int* cols = (int*)colsb.p;
-  const double one = 1.0, zero = 0.0, mone = -1.0;
-
-  // orthonormalise the nw columns of W against V(:, :m) and among themselves
-  // (classical Gram-Schmidt twice, then modified Gram-Schmidt in the block);
-  // appends the surviving columns to V and returns how many survived.
-  auto add_block = [&](int m, int nw, int& added) -> int {
-    added = 0;
-    for (int pass = 0; pass < 2 && m > 0; ++pass) {
-      CUBLAS_TRY(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, m, nw, (int)N, &one, V.p, (int)N, W.p, (int)N, &zero,
-                             T.p, mmax));
-      CUBLAS_TRY(cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)N, nw, m, &mone, V.p, (int)N, T.p, mmax, &one,
-                             W.p, (int)N));
+  DavState d;
+  d.c = c;
+  d.s = s;
+  d.N = N;
+  d.nev = nev;
+  d.blk = blk;
+  d.mmax = mmax;
+  d.sym = o->symmetrize != 0;
+  d.diag = diag;
+  CUBLAS_TRY(cublasCreate(&d.h));
+  struct Guard {
+    DavState& d;
+    std::vector<void*> dev, host;
+    ~Guard() {
+      if (d.h) cublasDestroy(d.h);
+      for (void* p : dev) cudaFree(p);
+      for (void* p : host) cudaFreeHost(p);
     }
-    for (int j = 0; j < nw; ++j) {
-      double* wj = W.p + (size_t)j * N;
-      for (int pass = 0; pass < 2; ++pass)
-        for (int i = 0; i < added; ++i) {
-          double d = 0.0;
-          CUBLAS_TRY(cublasDdot(h, (int)N, V.p + (size_t)(m + i) * N, 1, wj, 1, &d));
-          const double md = -d;
-          CUBLAS_TRY(cublasDaxpy(h, (int)N, &md, V.p + (size_t)(m + i) * N, 1, wj, 1));
-        }
-      double nrm = 0.0;
-      CUBLAS_TRY(cublasDnrm2(h, (int)N, wj, 1, &nrm));
-      if (!(nrm > 1e-10) || m + added >= mmax) continue;
-      const double inv = 1.0 / nrm;
-      CUBLAS_TRY(cublasDscal(h, (int)N, &inv, wj, 1));
-      CUDA_TRY_S(cudaMemcpyAsync(V.p + (size_t)(m + added) * N, wj, (size_t)N * 8, cudaMemcpyDeviceToDevice, s));
-      ++added;
+  } guard{d, {}, {}};
+  auto dalloc = [&](double** p, size_t n) -> int {
+    CUDA_TRY_S(cudaMalloc(p, std::max<size_t>(n, 1) * 8));
+    guard.dev.push_back(*p);
+    return EVR_OK;
+  };
+  const int n0 = nguess > 0 && guess ? std::min(nguess, mmax - blk) : nev;
+  const int wcols = std::max(blk, n0);
+  if ((rc = dalloc(&d.V, (size_t)N * mmax)) || (rc = dalloc(&d.HV, (size_t)N * mmax)) ||
+      (rc = dalloc(&d.X, (size_t)N * nev)) || (rc = dalloc(&d.R, (size_t)N * nev)) ||
+      (rc = dalloc(&d.W, (size_t)N * wcols)) || (rc = dalloc(&d.HW, (size_t)N * wcols)) ||
+      (rc = dalloc(&d.tmp, (size_t)N * std::max(wcols, nev))) || (rc = dalloc(&d.Tt, (size_t)mmax * wcols)) ||
+      (rc = dalloc(&d.T, (size_t)mmax * mmax)) || (rc = dalloc(&d.cv, (size_t)wcols)) ||
+      (rc = dalloc(&d.nrm, (size_t)nev + wcols)))
+    return rc;
+  double* ws = nullptr;  // cuBLAS workspace: no allocation while a graph is recorded
+  if ((rc = dalloc(&ws, (size_t)4 << 20))) return rc;
+  CUBLAS_TRY(cublasSetWorkspace(d.h, ws, (size_t)32 << 20));
+  d.params_bytes = sizeof(DavParams) + d.cols_bytes() + (size_t)(nev + (size_t)mmax * nev) * 8;
+  {
+    void* p = nullptr;
+    CUDA_TRY_S(cudaMalloc(&p, d.params_bytes));
+    guard.dev.push_back(p);
+    d.dparams = (unsigned char*)p;
+    CUDA_TRY_S(cudaMalloc(&p, (size_t)wcols * sizeof(int)));
+    guard.dev.push_back(p);
+    d.d_alive = (int*)p;
+    CUDA_TRY_S(cudaMallocHost(&p, d.params_bytes));
+    guard.host.push_back(p);
+    d.hparams = (unsigned char*)p;
+    memset(p, 0, d.params_bytes);
+    CUDA_TRY_S(cudaMallocHost(&p, (size_t)mmax * mmax * 8));
+    guard.host.push_back(p);
+    d.h_T = (double*)p;
+    CUDA_TRY_S(cudaMallocHost(&p, (size_t)(nev + wcols) * 8));
+    guard.host.push_back(p);
+    d.h_nrm = (double*)p;
+    CUDA_TRY_S(cudaMallocHost(&p, (size_t)wcols * sizeof(int)));
+    guard.host.push_back(p);
+    d.h_alive = (int*)p;
+  }
+  CUDA_TRY_S(cudaMemsetAsync(d.V, 0, (size_t)N * mmax * 8, s));
+  CUDA_TRY_S(cudaMemsetAsync(d.HV, 0, (size_t)N * mmax * 8, s));
+  // one fixed H.psi (and H^T.psi) per block width W -> HW (-> tmp), recordable
+  struct Bound {
+    BoundApply *H = nullptr, *HT = nullptr;
+  };
+  std::vector<Bound> bound(wcols + 1);
+  struct BGuard {
+    std::vector<Bound>& b;
+    ~BGuard() {
+      for (Bound& x : b) {
+        bound_apply_destroy(x.H);
+        bound_apply_destroy(x.HT);
+      }
     }
+  } bguard{bound};
+  long long nslices = 0;
+  if ((rc = evr_sg4_field_slices(c, &nslices))) return rc;
+  const bool graph = !o->no_graph && nslices == 0;  // streamed fields: eager launches
+  auto apply_block = [&](int nw, cudaStream_t st) -> int {
+    if (!graph) return apply_hs(c, N, nw, d.W, d.HW, d.tmp, d.sym, st);
+    Bound& b = bound[nw];
+    int r = EVR_OK;
+    if (!b.H && (r = bound_apply_create(c, nw, 0, d.W, d.HW, &b.H))) return r;
+    if (d.sym && !b.HT && (r = bound_apply_create(c, nw, 1, d.W, d.tmp, &b.HT))) return r;
+    if ((r = bound_apply_launch(b.H, st))) return r;
+    if (d.sym) {
+      if ((r = bound_apply_launch(b.HT, st))) return r;
+      average_kernel<<<256, 256, 0, st>>>(d.HW, d.HW, d.tmp, N * nw);
+      CUDA_TRY_S(cudaGetLastError());
+    }
+    return EVR_OK;
+  };
+  // the apply inside the expansion goes through apply_block
+  DavGraphs gr;
+  gr.exec.assign(2 + wcols, nullptr);
+  gr.seen.assign(2 + wcols, 0);
+  auto expand = [&](int nw, bool precond) -> int {
+    auto enq = [&](cudaStream_t st) -> int { return dav_phase_expand(d, nw, precond, st, apply_block); };
+    // the initial block is never recorded (its width may differ from blk and it runs once)
+    int r = precond ? dav_run(gr, 1 + nw, graph, s, enq) : enq(s);
+    if (r) return r;
+    CUDA_TRY_S(cudaStreamSynchronize(s));
     return EVR_OK;
   };
 
   // initial block: the caller's guess, or the first packed functions (lowest L)
-  int m = 0, added = 0;
-  const int n0 = nguess > 0 && guess ? std::min(nguess, mmax - blk) : nev;
   if (guess && nguess > 0) {
-    CUDA_TRY_S(cudaMemcpyAsync(W.p, guess, (size_t)N * std::min(n0, std::max(nev, blk)) * 8,
-                               cudaMemcpyDeviceToDevice, s));
+    CUDA_TRY_S(cudaMemcpyAsync(d.W, guess, (size_t)N * n0 * 8, cudaMemcpyDeviceToDevice, s));
   } else {
-    unit_block_kernel<<<256, 256, 0, s>>>(W.p, N, n0, 0);
+    unit_block_kernel<<<256, 256, 0, s>>>(d.W, N, n0, 0);
   }
-  if ((rc = add_block(0, std::min(n0, std::max(nev, blk)), added))) return rc;
-  if ((rc = apply_hs(c, N, added, V.p, HV.p, tmp.p, sym, s))) return rc;
-  m = added;
+  DavParams* hp = (DavParams*)d.hparams;
+  hp->m = 0;
+  if ((rc = expand(n0, false))) return rc;
+  std::vector<char> live(mmax, 0);  // slot holds a (non-zero) basis vector
+  int m = 0;
+  for (int j = 0; j < n0; ++j)
+    if (d.h_alive[j]) live[m++] = 1;
+  if (m == 0) return set_error(EVR_ERR_NUMERIC, "davidson: the initial block is rank deficient");
 
-  std::vector<double> Th, w, Z, theta(nev), rn(nev);
-  int it = 0;
+  std::vector<double> w, Z, theta(nev), rn(nev);
+  int it = 0, k = 0;
   bool converged = false;
   for (it = 0; it < o->max_it; ++it) {
-    // projected matrix T = V^T HV, symmetrised on the host (sub_hermitic_H)
-    CUBLAS_TRY(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, m, m, (int)N, &one, V.p, (int)N, HV.p, (int)N, &zero, T.p, m));
-    Th.resize((size_t)m * m);
-    CUDA_TRY_S(cudaMemcpyAsync(Th.data(), T.p, (size_t)m * m * 8, cudaMemcpyDeviceToHost, s));
-    CUDA_TRY_S(cudaStreamSynchronize(s));
-    std::vector<double> A((size_t)m * m);
+    // projected matrix (live slots), symmetrised on the host (sub_hermitic_H)
+    std::vector<int> slot;
     for (int i = 0; i < m; ++i)
-      for (int j = 0; j < m; ++j) A[(size_t)i * m + j] = 0.5 * (Th[i + (size_t)m * j] + Th[j + (size_t)m * i]);
-    jacobi_eigen(m, A, w, Z);
-    const int k = std::min(nev, m);
-    std::vector<double> Yh((size_t)m * k);
+      if (live[i]) slot.push_back(i);
+    const int ml = (int)slot.size();
+    std::vector<double> A((size_t)ml * ml);
+    for (int i = 0; i < ml; ++i)
+      for (int j = 0; j < ml; ++j)
+        A[(size_t)i * ml + j] = 0.5 * (d.h_T[slot[i] + (size_t)mmax * slot[j]] + d.h_T[slot[j] + (size_t)mmax * slot[i]]);
+    jacobi_eigen(ml, A, w, Z);
+    k = std::min(nev, ml);
+    double* Y = d.hY();
+    memset(Y, 0, (size_t)mmax * nev * 8);
     for (int j = 0; j < k; ++j)
-      for (int i = 0; i < m; ++i) Yh[i + (size_t)m * j] = Z[(size_t)i * m + j];
+      for (int i = 0; i < ml; ++i) Y[slot[i] + (size_t)mmax * j] = Z[(size_t)i * ml + j];
+    for (int j = 0; j < nev; ++j) d.htheta()[j] = j < k ? w[j] : 0.0;
     for (int j = 0; j < k; ++j) theta[j] = w[j];
-    CUDA_TRY_S(cudaMemcpyAsync(Y.p, Yh.data(), Yh.size() * 8, cudaMemcpyHostToDevice, s));
-    CUDA_TRY_S(cudaMemcpyAsync(th.p, theta.data(), (size_t)k * 8, cudaMemcpyHostToDevice, s));
-    // Ritz vectors and residuals
-    CUBLAS_TRY(cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)N, k, m, &one, V.p, (int)N, Y.p, m, &zero, X.p, (int)N));
-    CUBLAS_TRY(cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)N, k, m, &one, HV.p, (int)N, Y.p, m, &zero, R.p, (int)N));
-    residual_kernel<<<256, 256, 0, s>>>(R.p, X.p, th.p, N, k);
-    CUDA_TRY_S(cudaGetLastError());
-    for (int j = 0; j < k; ++j) CUBLAS_TRY(cublasDnrm2(h, (int)N, R.p + (size_t)j * N, 1, &rn[j]));
+    // Ritz vectors, residuals and their norms
+    if ((rc = dav_run(gr, 0, graph, s, [&](cudaStream_t st) { return dav_phase_ritz(d, st); }))) return rc;
     CUDA_TRY_S(cudaStreamSynchronize(s));
     std::vector<int> todo;
-    for (int j = 0; j < k; ++j)
+    for (int j = 0; j < k; ++j) {
+      rn[j] = d.h_nrm[j];
+      if (!std::isfinite(rn[j])) return set_error(EVR_ERR_NUMERIC, "davidson: non-finite residual");
       if (!(rn[j] < o->conv_resi)) todo.push_back(j);
+    }
     if (k == nev && todo.empty()) {
       converged = true;
       break;
     }
-    for (int j = 0; j < k; ++j)
-      if (!std::isfinite(rn[j])) return set_error(EVR_ERR_NUMERIC, "davidson: non-finite residual");
     // restart (keep the Ritz vectors) when the new block does not fit
     const int nnew = std::min((int)todo.size(), blk);
     if (m + nnew > mmax) {
-      CUDA_TRY_S(cudaMemcpyAsync(V.p, X.p, (size_t)N * k * 8, cudaMemcpyDeviceToDevice, s));
-      CUBLAS_TRY(cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)N, k, m, &one, HV.p, (int)N, Y.p, m, &zero, tmp.p,
-                             (int)N));
-      CUDA_TRY_S(cudaMemcpyAsync(HV.p, tmp.p, (size_t)N * k * 8, cudaMemcpyDeviceToDevice, s));
+      const double one = 1.0, zero = 0.0;
+      CUBLAS_TRY(cublasSetStream(d.h, s));
+      CUBLAS_TRY(cublasDgemm(d.h, CUBLAS_OP_N, CUBLAS_OP_N, (int)N, k, mmax, &one, d.HV, (int)N, d.dY(), mmax, &zero,
+                             d.tmp, (int)N));
+      CUDA_TRY_S(cudaMemsetAsync(d.V, 0, (size_t)N * mmax * 8, s));
+      CUDA_TRY_S(cudaMemsetAsync(d.HV, 0, (size_t)N * mmax * 8, s));
+      CUDA_TRY_S(cudaMemcpyAsync(d.V, d.X, (size_t)N * k * 8, cudaMemcpyDeviceToDevice, s));
+      CUDA_TRY_S(cudaMemcpyAsync(d.HV, d.tmp, (size_t)N * k * 8, cudaMemcpyDeviceToDevice, s));
+      std::fill(live.begin(), live.end(), 0);
+      for (int j = 0; j < k; ++j) live[j] = 1;
       m = k;
     }
-    CUDA_TRY_S(cudaMemcpyAsync(cols, todo.data(), (size_t)nnew * sizeof(int), cudaMemcpyHostToDevice, s));
-    precond_kernel<<<256, 256, 0, s>>>(W.p, R.p, diag, th.p, cols, N, nnew);
-    CUDA_TRY_S(cudaGetLastError());
-    if ((rc = add_block(m, nnew, added))) return rc;
+    hp->m = m;
+    hp->ncols = nnew;
+    for (int j = 0; j < nnew; ++j) d.hcols()[j] = todo[j];
+    if ((rc = expand(nnew, true))) return rc;
+    int added = 0;
+    for (int j = 0; j < nnew; ++j) {
+      live[m + j] = d.h_alive[j] ? 1 : 0;
+      added += d.h_alive[j] ? 1 : 0;
+    }
     if (added == 0) return set_error(EVR_ERR_NUMERIC, "davidson: no new direction survived orthogonalisation");
-    if ((rc = apply_hs(c, N, added, V.p + (size_t)m * N, HV.p + (size_t)m * N, tmp.p, sym, s))) return rc;
-    m += added;
+    m += nnew;
   }
   for (int j = 0; j < nev; ++j) evals[j] = theta[j];
   if (resid)
     for (int j = 0; j < nev; ++j) resid[j] = rn[j];
-  if (evecs) CUDA_TRY_S(cudaMemcpyAsync(evecs, X.p, (size_t)N * nev * 8, cudaMemcpyDeviceToDevice, s));
+  if (evecs) CUDA_TRY_S(cudaMemcpyAsync(evecs, d.X, (size_t)N * nev * 8, cudaMemcpyDeviceToDevice, s));
   CUDA_TRY_S(cudaStreamSynchronize(s));
   if (iterations) *iterations = it + 1;
   if (!converged) return set_error(EVR_ERR_NUMERIC, "davidson: not converged after %d iterations", o->max_it);
@@ -416,6 +657,12 @@ __global__ void cdot_cols_kernel(const double2* a, const double2* b, long long N
   }
 }
 
+// Element-wise kernels on complex vectors: 64-thread blocks, enough of them
+// to cover n once (up to 32 per SM of a 152-SM GB300), so short vectors
+// spread their FP64 work over many SMs.
+static inline int ew_grid(long long n) { return (int)std::max<long long>(1, std::min<long long>((n + 63) / 64, 32 * 152)); }
+#define EW_THREADS 64
+
 // One fixed-order step, enqueued on s (recorded once as a CUDA graph and
 // replayed): save <- psi, the recurrence of order npoly on w1/w2, |w|^2 of
 // the last term into hb[0] (pinned), psi = out e^{-i E0 dt}, and the
@@ -434,8 +681,8 @@ struct ChebyStep {
 
 static int enqueue_cheby_step(const ChebyStep& st, const std::vector<double>& cf, double E0, double Esc, double ph,
                               cudaStream_t s) {
-  const int G = 2 * 152, B = 256;
   const long long n = st.n;
+  const int G = ew_grid(n), B = EW_THREADS;
   double *a = st.w1, *b = st.w2;
   CUDA_TRY_S(cudaMemcpyAsync(st.save, st.psi, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
   CUDA_TRY_S(cudaMemcpyAsync(a, st.save, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
@@ -511,7 +758,7 @@ extern "C" int evr_sg4_cheby_propagate(evr_sg4_ctx* c, const evr_cheby_opts* o, 
     CUDA_TRY_S(cudaMemcpyAsync(p0copy.p, psi, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
     P0 = (const double2*)p0copy.p;
   }
-  const int G = 2 * 152, B = 256;
+  const int G = ew_grid(n), B = EW_THREADS;
   double Hmin = o->Hmin, Hmax = o->Hmax;
   int used = 0;
   std::vector<double> J;
@@ -635,9 +882,11 @@ extern "C" int evr_sg4_cheby_propagate(evr_sg4_ctx* c, const evr_cheby_opts* o, 
 //   dpsi/dt = -i (H0 - E(t) mu) psi,  E held at E[k] over step k ('grid'
 //   field, :483-510), classic RK4 stages on (H0 - E0) with the phase
 //   exp(-i E0 dt) restored after each step, as fcn_field does with
-//   para_H%E0 (E0 near the middle of the spectrum keeps RK4 stable).  H0 and mu are two contexts on the
-// same basis (mu a type-0 operator).  The optimal-control gradient is the
-// exact adjoint of those discrete steps: with S = <target|psi_N>,
+//   para_H%E0 (E0 near the middle of the spectrum keeps RK4 stable).  H0 and
+//   mu are two contexts on the same basis (mu a type-0 operator).  Several
+//   packets can be propagated together, each with its own field (packet b
+//   sees E[k*nb + b]).  The optimal-control gradient is the exact adjoint of
+//   those discrete steps: with S = <target|psi_N>,
 //   J = |S|^2,  lambda_N = S target,  and for each step the stage costates
 //   kb4 = h/6 l, kb3 = h/3 l + h sb4, kb2 = h/3 l + h/2 sb3, kb1 = h/6 l + h/2 sb2,
 //   sb_i = A^dagger kb_i = i (H0^T - E mu^T) kb_i,  lambda_{k-1} = l + sum sb_i,
@@ -650,103 +899,175 @@ extern "C" int evr_sg4_cheby_propagate(evr_sg4_ctx* c, const evr_cheby_opts* o, 
 // The reference's control update (build_field, SRC/sub_propagation/
 // sub_control.f90:907-1010) uses the continuous-time form of the same
 // derivative, -2 Im(S* <chi(t)|mu|psi(t)>).
+//
+// Every kernel of a field interval takes the interval index from a device
+// counter (SweepCtl) instead of a launch argument, so one field interval --
+// nsub steps x 4 stages x (H0/mu launch, chunk sums, stage update), then the
+// counter update -- is recorded once as a CUDA graph and replayed for every
+// interval; the eager path launches the same kernels in the same order.
 // ------------------------------------------------------------------------
+
+// Device-side position of a sweep: the current field interval and which
+// interval's stage inputs are recorded (-1: none, -2: every interval, else
+// the intervals of checkpoint segment rec_seg).
+struct SweepCtl {
+  int k;
+  int rec_seg;
+};
 
 // The two operators of a stage (H0 and mu, or both transposed) run in one
 // persistent launch (field_pair_apply); the kernels below join their chunk
 // partials in the same order as evr_sg4_hpsi and fuse the stage arithmetic.
 struct StageIn {
-  const double2* part;         // [2][n_chunks][2] (s, c) partials, H0 first
+  const double2* part;         // [2][n_chunks][nrhs_v] (s, c) partials, H0 first
   const long long* fun_chunk;  // [N+1]
-  long long nch2;              // 2 n_chunks: offset of mu's partials
+  long long nch2;              // n_chunks * nrhs_v: offset of mu's partials
   long long N;
-  double2* x;                  // stage input, overwritten by the next stage's input
-  double E, E0, h;
+  int nb, nrhs_v;              // packets, 2 nb virtual columns
+  double2* x;                  // stage input [nb][N], overwritten by the next stage's input
+  const double* E;             // field samples [nsteps][nb] (device)
+  const SweepCtl* ctl;         // current interval
+  double E0, h;
+  int C, nsub;                 // checkpoint spacing, RK4 steps per interval
+  double2* rec;                // stage-input records: two alternating segment buffers, or NULL
+  long long seg_rec;           // complex elements per segment buffer
 };
 
-__device__ __forceinline__ void stage_sums(const StageIn& a, long long n, double2 xv, double& re, double& im,
-                                           double& mr, double& mi) {
-  const long long c0 = a.fun_chunk[n], c1 = a.fun_chunk[n + 1];
-  double hr = join_chunks(a.part, c0, c1, 2, 0), hi = join_chunks(a.part, c0, c1, 2, 1);
-  mr = join_chunks(a.part + a.nch2, c0, c1, 2, 0);
-  mi = join_chunks(a.part + a.nch2, c0, c1, 2, 1);
+// stage inputs of step u of interval k, stage `stage`, when interval k is recorded
+__device__ __forceinline__ double2* rec_at(const StageIn& a, int k, int u, int stage) {
+  if (!a.rec) return nullptr;
+  const int seg = k / a.C;
+  if (a.ctl->rec_seg != -2 && a.ctl->rec_seg != seg) return nullptr;
+  return a.rec + (size_t)(seg & 1) * a.seg_rec + (((size_t)(k - seg * a.C) * a.nsub + u) * 4 + (stage - 1)) * a.N * a.nb;
+}
+
+// The four ordered sums of element (n, packet b) -- H0 re, H0 im, mu re,
+// mu im -- are joined by four lanes of a warp, one sum each, and gathered
+// with shuffles: GB300's FP64 pipe does about two operations per clock per
+// SM, so these joins must be spread over many SMs (a block of 32 threads
+// handles 8 elements); with one thread per element and 256-thread blocks the
+// stage kernels of a small operator ran on two SMs and took longer than its
+// H.psi launch.  Each sum is the join of evr_sg4_hpsi in its order.  Call
+// from every lane of a warp with the same e0 (the first element of the
+// warp's eight); lane q of group g handles element e0 + g.
+__device__ __forceinline__ bool stage_sums4(const StageIn& a, long long e0, long long& e, int& b, double2& xv,
+                                            double& E, double& re, double& im, double& mr, double& mi) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
+  e = e0 + g;
+  const long long ne = a.N * a.nb;
+  double v = 0.0;
+  b = 0;
+  long long n = 0;
+  if (e < ne) {
+    b = (int)(e / a.N);
+    n = e - (long long)b * a.N;
+    const long long c0 = a.fun_chunk[n], c1 = a.fun_chunk[n + 1];
+    v = join_chunks(a.part + (q >> 1) * a.nch2, c0, c1, a.nrhs_v, 2 * b + (q & 1));
+  }
+  const double hr0 = __shfl_sync(0xffffffffu, v, lane & ~3), hi0 = __shfl_sync(0xffffffffu, v, (lane & ~3) | 1);
+  mr = __shfl_sync(0xffffffffu, v, (lane & ~3) | 2);
+  mi = __shfl_sync(0xffffffffu, v, (lane & ~3) | 3);
+  if (q != 0 || e >= ne) return false;
+  xv = a.x[e];
+  E = a.E[(long long)a.ctl->k * a.nb + b];
+  double hr = hr0, hi = hi0;
   if (a.E0 != 0.0) {  // (H0 - E0) x, as the scaled H.psi writes it
     hr = hr - a.E0 * xv.x;
     hi = hi - a.E0 * xv.y;
   }
-  re = hr - a.E * mr;
-  im = hi - a.E * mi;
+  re = hr - E * mr;
+  im = hi - E * mi;
+  return true;
 }
 
 __device__ __forceinline__ double2 cmul(double2 t, double cr, double ci) {
   return make_double2(cr * t.x - ci * t.y, cr * t.y + ci * t.x);
 }
 
-// forward stage i of an RK4 step y -> y (h = step):
+// first element of this warp's eight, and the element stride of the grid
+__device__ __forceinline__ long long warp_elem0() {
+  return ((long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 8;
+}
+__device__ __forceinline__ long long grid_elem_stride() { return (long long)gridDim.x * (blockDim.x >> 5) * 8; }
+
+// forward stage i of RK4 step u of the current interval, y -> y (h = step):
 //   k = -i ((H0 - E0) x - E mu x);  [rec = x]
 //   i=1: acc = y + h/6 k, x = y + h/2 k     i=2: acc += h/3 k, x = y + h/2 k
 //   i=3: acc += h/3 k,    x = y + h k       i=4: y = (acc + h/6 k) e^{-i E0 h}, x = y
-__global__ void __launch_bounds__(256) rk_stage_kernel(StageIn a, int stage, double2* y, double2* acc, double2* rec,
+__global__ void __launch_bounds__(256) rk_stage_kernel(StageIn a, int u, int stage, double2* y, double2* acc,
                                                        double cr, double ci) {
-  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < a.N; n += (long long)gridDim.x * blockDim.x) {
-    const double2 xv = a.x[n];
-    double re, im, mr, mi;
-    stage_sums(a, n, xv, re, im, mr, mi);
+  const long long ne = a.N * a.nb;
+  double2* rec = rec_at(a, a.ctl->k, u, stage);
+  for (long long e0 = warp_elem0(); e0 < ne; e0 += grid_elem_stride()) {
+    long long e;
+    int b;
+    double2 xv;
+    double E, re, im, mr, mi;
+    if (!stage_sums4(a, e0, e, b, xv, E, re, im, mr, mi)) continue;
     const double2 k = make_double2(im, -re);  // -i (re + i im)
-    if (rec) rec[n] = xv;
-    const double2 yv = y[n];
+    if (rec) rec[e] = xv;
+    const double2 yv = y[e];
     const double h = a.h;
     if (stage == 1) {
-      acc[n] = make_double2(fma(h / 6.0, k.x, yv.x), fma(h / 6.0, k.y, yv.y));
-      a.x[n] = make_double2(fma(0.5 * h, k.x, yv.x), fma(0.5 * h, k.y, yv.y));
+      acc[e] = make_double2(fma(h / 6.0, k.x, yv.x), fma(h / 6.0, k.y, yv.y));
+      a.x[e] = make_double2(fma(0.5 * h, k.x, yv.x), fma(0.5 * h, k.y, yv.y));
     } else if (stage < 4) {
-      const double2 ac = acc[n];
-      acc[n] = make_double2(fma(h / 3.0, k.x, ac.x), fma(h / 3.0, k.y, ac.y));
+      const double2 ac = acc[e];
+      acc[e] = make_double2(fma(h / 3.0, k.x, ac.x), fma(h / 3.0, k.y, ac.y));
       const double c = stage == 2 ? 0.5 * h : h;
-      a.x[n] = make_double2(fma(c, k.x, yv.x), fma(c, k.y, yv.y));
+      a.x[e] = make_double2(fma(c, k.x, yv.x), fma(c, k.y, yv.y));
     } else {
-      const double2 ac = acc[n];
+      const double2 ac = acc[e];
       double2 t = make_double2(fma(h / 6.0, k.x, ac.x), fma(h / 6.0, k.y, ac.y));
       if (a.E0 != 0.0) t = cmul(t, cr, ci);
-      y[n] = t;
-      a.x[n] = t;
+      y[e] = t;
+      a.x[e] = t;
     }
   }
 }
 
-// adjoint stage i (taken 4, 3, 2, 1) of one RK4 step, costate l (phased):
-//   sb = +i ((H0^T - E0) kb - E mu^T kb),  kb = x;
-//   gpart[block] = -2 Im((mu^T kb)^dagger s_i) = -2 Im(kb^dagger mu s_i), s_i the stage input;
+// adjoint stage i (taken 4, 3, 2, 1) of RK4 step u of the current interval,
+// costate l (phased); kb = x, s_i = the recorded stage input:
+//   sb = +i ((H0^T - E0) kb - E mu^T kb);
+//   gpart[...] = -2 Im((mu^T kb)^dagger s_i) = -2 Im(kb^dagger mu s_i), one per block;
 //   i=4: yb = l + sb, x = h/3 l + h sb       i=3: yb += sb, x = h/3 l + h/2 sb
 //   i=2: yb += sb, x = h/6 l + h/2 sb        i=1: l = (yb + sb) e^{+i E0 h}, x = h/6 l
-// (the last form also prepares the previous step's stage 4)
-__global__ void __launch_bounds__(256) rk_adjoint_stage_kernel(StageIn a, int stage, double2* l, double2* yb,
-                                                               const double2* s, double* gpart, double cr,
-                                                               double ci) {
+// (the last form also prepares the previous step's stage 4).  The block
+// partials of interval k, step u (taken nsub-1 .. 0), stage i go to
+// gpart[((k nsub + nsub-1-u) 4 + 4-i) nblk + block].
+__global__ void __launch_bounds__(256) rk_adjoint_stage_kernel(StageIn a, int u, int stage, double2* l, double2* yb,
+                                                               double* gpart, double cr, double ci) {
+  const int k = a.ctl->k;
+  const int seg = k / a.C;
+  const double2* s = a.rec + (size_t)(seg & 1) * a.seg_rec +
+                     (((size_t)(k - seg * a.C) * a.nsub + u) * 4 + (stage - 1)) * a.N * a.nb;
+  const long long ne = a.N * a.nb;
   double g = 0.0;
-  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < a.N; n += (long long)gridDim.x * blockDim.x) {
-    const double2 xv = a.x[n];
-    double re, im, mr, mi;
-    stage_sums(a, n, xv, re, im, mr, mi);
+  for (long long e0 = warp_elem0(); e0 < ne; e0 += grid_elem_stride()) {
+    long long e;
+    int b;
+    double2 xv;
+    double E, re, im, mr, mi;
+    if (!stage_sums4(a, e0, e, b, xv, E, re, im, mr, mi)) continue;
     const double2 sb = make_double2(-im, re);  // +i (re + i im)
-    const double2 sv = s[n];
+    const double2 sv = s[e];
     g = fma(mr, sv.y, fma(-mi, sv.x, g));
-    const double2 lv = l[n];
+    const double2 lv = l[e];
     const double h = a.h;
     if (stage == 4) {
-      yb[n] = make_double2(fma(1.0, sb.x, lv.x), fma(1.0, sb.y, lv.y));
-      a.x[n] = make_double2(fma(h, sb.x, (h / 3.0) * lv.x), fma(h, sb.y, (h / 3.0) * lv.y));
+      yb[e] = make_double2(fma(1.0, sb.x, lv.x), fma(1.0, sb.y, lv.y));
+      a.x[e] = make_double2(fma(h, sb.x, (h / 3.0) * lv.x), fma(h, sb.y, (h / 3.0) * lv.y));
     } else if (stage > 1) {
-      const double2 b = yb[n];
-      yb[n] = make_double2(fma(1.0, sb.x, b.x), fma(1.0, sb.y, b.y));
+      const double2 bb = yb[e];
+      yb[e] = make_double2(fma(1.0, sb.x, bb.x), fma(1.0, sb.y, bb.y));
       const double c = stage == 3 ? h / 3.0 : h / 6.0;
-      a.x[n] = make_double2(fma(0.5 * h, sb.x, c * lv.x), fma(0.5 * h, sb.y, c * lv.y));
+      a.x[e] = make_double2(fma(0.5 * h, sb.x, c * lv.x), fma(0.5 * h, sb.y, c * lv.y));
     } else {
-      const double2 b = yb[n];
-      double2 t = make_double2(fma(1.0, sb.x, b.x), fma(1.0, sb.y, b.y));
+      const double2 bb = yb[e];
+      double2 t = make_double2(fma(1.0, sb.x, bb.x), fma(1.0, sb.y, bb.y));
       if (a.E0 != 0.0) t = cmul(t, cr, ci);
-      l[n] = t;
-      a.x[n] = make_double2((h / 6.0) * t.x, (h / 6.0) * t.y);
+      l[e] = t;
+      a.x[e] = make_double2((h / 6.0) * t.x, (h / 6.0) * t.y);
     }
   }
   __shared__ double sh[32];
@@ -755,9 +1076,21 @@ __global__ void __launch_bounds__(256) rk_adjoint_stage_kernel(StageIn a, int st
   __syncthreads();
   if (threadIdx.x == 0) {
     double t = 0.0;
-    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += sh[k];
-    gpart[blockIdx.x] = -2.0 * t;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += sh[q];
+    gpart[(((size_t)k * a.nsub + (a.nsub - 1 - u)) * 4 + (4 - stage)) * gridDim.x + blockIdx.x] = -2.0 * t;
   }
+}
+
+// sweep counter updates (one thread): the next interval, or the previous one
+__global__ void sweep_step_kernel(SweepCtl* ctl, int delta) { ctl->k += delta; }
+
+// checkpoint of the forward sweep: ck[k / C] = y at the start of every C-th interval
+__global__ void checkpoint_kernel(const SweepCtl* ctl, int C, const double2* y, double2* ck, long long n) {
+  const int k = ctl->k;
+  if (k % C) return;
+  double2* dst = ck + (size_t)(k / C) * n;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+    dst[e] = y[e];
 }
 
 // l = lambda e^{+i E0 h}, x = h/6 l: the start of the backward sweep
@@ -781,27 +1114,103 @@ __global__ void rk_grad_sum_kernel(const double* gpart, int nsteps, int nsub, in
   }
 }
 
+__global__ void ctl_set_kernel(SweepCtl* ctl, int k, int rec_seg) {
+  ctl->k = k;
+  ctl->rec_seg = rec_seg;
+}
+
 namespace evr {
 
-// RK4 steps driven by a FieldPair (forward operators), fused per stage
-struct FwdSweep {
-  FieldPair* fp;
-  FieldPairView v;
-  double* y;    // device complex N
-  double* acc;
-  int nblk;
+// Stage-kernel geometry: four lanes per element (eight elements per warp),
+// one-warp blocks for small blocks of vectors so the joins spread over many SMs.
+static int stage_threads(long long ne) { return ne <= 32768 ? 32 : 256; }
+static int join_blocks(long long ne) {
+  const long long per = stage_threads(ne) / 4;
+  return (int)std::max<long long>(1, std::min<long long>((ne + per - 1) / per, 4096));
+}
+
+// The kernels of one field interval of a forward or adjoint sweep, launched
+// eagerly or recorded once as a CUDA graph and replayed.
+struct Sweep {
+  FieldPair* fp = nullptr;
+  StageIn a{};
+  double2* y = nullptr;     // forward: the state; adjoint: the costate l
+  double2* acc = nullptr;   // forward: the RK4 accumulator; adjoint: yb
+  double* gpart = nullptr;  // adjoint: gradient partials
+  double2* ck = nullptr;    // forward: checkpoints (NULL: none)
+  bool adjoint = false;
+  double cr = 1.0, ci = 0.0;
+  int nblk = 1, nthr = 32;
+  cudaStream_t cs = nullptr;  // capture stream
+  cudaGraphExec_t exec = nullptr;
+  ~Sweep() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (cs) cudaStreamDestroy(cs);
+  }
 };
 
-static int rk4_step_fused(FwdSweep& w, double E, double E0, double h, double* rec, cudaStream_t s) {
-  StageIn a{(const double2*)w.v.part, w.v.fun_chunk, 2 * w.v.n_chunks, w.v.N, (double2*)w.v.x, E, E0, h};
-  const double cr = std::cos(E0 * h), ci = -std::sin(E0 * h);
-  for (int stage = 1; stage <= 4; ++stage) {
-    int rc = field_pair_apply(w.fp, s);
-    if (rc) return rc;
-    rk_stage_kernel<<<w.nblk, 256, 0, s>>>(a, stage, (double2*)w.y, (double2*)w.acc,
-                                           rec ? (double2*)rec + (size_t)(stage - 1) * w.v.N : nullptr, cr, ci);
+static void sweep_init(Sweep& w, FieldPair* fp, SweepCtl* ctl, const double* Edev, int nb, const evr_rk4_opts* o,
+                       bool adjoint) {
+  const FieldPairView v = field_pair_view(fp);
+  w.fp = fp;
+  w.adjoint = adjoint;
+  const double h = o->dt / o->nsub;
+  w.a = StageIn{(const double2*)v.part, v.fun_chunk, v.n_chunks * 2 * nb, v.N, nb, 2 * nb, (double2*)v.x,
+                Edev, ctl, o->E0, h, o->checkpoint, o->nsub, nullptr, 0};
+  w.cr = std::cos(o->E0 * h);
+  w.ci = adjoint ? std::sin(o->E0 * h) : -std::sin(o->E0 * h);  // e^{+i E0 h} backward, e^{-i E0 h} forward
+  w.nblk = join_blocks(v.N * nb);
+  w.nthr = stage_threads(v.N * nb);
+}
+
+static int enqueue_interval(Sweep& w, cudaStream_t s) {
+  const long long ne = w.a.N * w.a.nb;
+  const int nsub = w.a.nsub;
+  int rc;
+  if (!w.adjoint) {
+    if (w.ck)
+      checkpoint_kernel<<<(unsigned)std::max<long long>(1, std::min<long long>((ne + 255) / 256, 1024)), 256, 0, s>>>(
+          w.a.ctl, w.a.C, w.y, w.ck, ne);
+    for (int u = 0; u < nsub; ++u)
+      for (int stage = 1; stage <= 4; ++stage) {
+        if ((rc = field_pair_apply(w.fp, s))) return rc;
+        rk_stage_kernel<<<w.nblk, w.nthr, 0, s>>>(w.a, u, stage, w.y, w.acc, w.cr, w.ci);
+      }
+    sweep_step_kernel<<<1, 1, 0, s>>>(const_cast<SweepCtl*>(w.a.ctl), 1);
+  } else {
+    sweep_step_kernel<<<1, 1, 0, s>>>(const_cast<SweepCtl*>(w.a.ctl), -1);
+    for (int u = nsub - 1; u >= 0; --u)
+      for (int stage = 4; stage >= 1; --stage) {
+        if ((rc = field_pair_apply(w.fp, s))) return rc;
+        rk_adjoint_stage_kernel<<<w.nblk, w.nthr, 0, s>>>(w.a, u, stage, w.y, w.acc, w.gpart, w.cr, w.ci);
+      }
   }
   CUDA_TRY_S(cudaGetLastError());
+  return EVR_OK;
+}
+
+// one field interval on s: eager launches, or the recorded graph (recorded on first use)
+static int run_interval(Sweep& w, bool graph, cudaStream_t s) {
+  if (!graph) return enqueue_interval(w, s);
+  if (!w.exec) {
+    if (!w.cs) CUDA_TRY_S(cudaStreamCreateWithFlags(&w.cs, cudaStreamNonBlocking));
+    cudaGraph_t g = nullptr;
+    CUDA_TRY_S(cudaStreamBeginCapture(w.cs, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue_interval(w, w.cs);
+    cudaError_t ec = cudaStreamEndCapture(w.cs, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (ec != cudaSuccess) return set_error(EVR_ERR_CUDA, "rk4: graph capture: %s", cudaGetErrorString(ec));
+    ec = cudaGraphInstantiate(&w.exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ec != cudaSuccess) {
+      w.exec = nullptr;
+      return set_error(EVR_ERR_CUDA, "rk4: graph instantiate: %s", cudaGetErrorString(ec));
+    }
+  }
+  CUDA_TRY_S(cudaGraphLaunch(w.exec, s));
   return EVR_OK;
 }
 
@@ -821,54 +1230,66 @@ struct StreamGuard {
 
 }  // namespace evr
 
-static int check_field_args(evr_sg4_ctx* H0, evr_sg4_ctx* mu, const evr_rk4_opts* o, const double* E, long long* N) {
+static int check_field_args(evr_sg4_ctx* H0, evr_sg4_ctx* mu, const evr_rk4_opts* o, int nb, const double* E,
+                            long long* N) {
   if (!H0 || !mu || !o || !E) return set_error(EVR_ERR_ARG, "rk4: NULL argument");
   long long a[8], b[8];
   int rc = evr_sg4_ctx_sizes(H0, a);
   if (!rc) rc = evr_sg4_ctx_sizes(mu, b);
   if (rc) return rc;
   if (a[0] != b[0] || a[1] != b[1] || a[3] != b[3]) return set_error(EVR_ERR_ARG, "rk4: H0 and mu are on different bases");
-  if (o->nsteps < 1 || !(o->dt > 0) || o->checkpoint < 1 || o->nsub < 1)
-    return set_error(EVR_ERR_ARG, "rk4: need nsteps >= 1, dt > 0, checkpoint >= 1, nsub >= 1");
-  for (int k = 0; k < o->nsteps; ++k)
-    if (!std::isfinite(E[k])) return set_error(EVR_ERR_NUMERIC, "rk4: field sample %d is not finite", k);
+  if (o->nsteps < 1 || !(o->dt > 0) || o->checkpoint < 1 || o->nsub < 1 || nb < 1)
+    return set_error(EVR_ERR_ARG, "rk4: need nsteps >= 1, dt > 0, checkpoint >= 1, nsub >= 1, packets >= 1");
+  for (long long k = 0; k < (long long)o->nsteps * nb; ++k)
+    if (!std::isfinite(E[k])) return set_error(EVR_ERR_NUMERIC, "rk4: field sample %lld is not finite", k);
   *N = a[0];
   return EVR_OK;
 }
 
-static int join_blocks(long long N) { return (int)std::max<long long>(1, std::min<long long>((N + 255) / 256, 1024)); }
-
-extern "C" int evr_sg4_rk4_field(evr_sg4_ctx* H0, evr_sg4_ctx* mu, const evr_rk4_opts* o, const double* E, double* psi,
-                                 void* stream) {
+extern "C" int evr_sg4_rk4_field_batch(evr_sg4_ctx* H0, evr_sg4_ctx* mu, const evr_rk4_opts* o, int nb,
+                                       const double* E, double* psi, void* stream) {
   long long N = 0;
-  int rc = check_field_args(H0, mu, o, E, &N);
+  int rc = check_field_args(H0, mu, o, nb, E, &N);
   if (rc) return rc;
   if (!psi) return set_error(EVR_ERR_ARG, "rk4: psi is NULL");
   cudaStream_t s = (cudaStream_t)stream;
   PairGuard fp;
-  if ((rc = field_pair_create(H0, mu, 0, &fp.p))) return rc;
-  DevBuf acc;
-  CUDA_TRY_S(cudaMalloc(&acc.p, (size_t)N * 16));
-  FwdSweep w{fp.p, field_pair_view(fp.p), psi, acc.p, join_blocks(N)};
-  CUDA_TRY_S(cudaMemcpyAsync(w.v.x, psi, (size_t)N * 16, cudaMemcpyDeviceToDevice, s));
-  const double hs = o->dt / o->nsub;
-  for (int st = 0; st < o->nsteps; ++st)
-    for (int u = 0; u < o->nsub; ++u)
-      if ((rc = rk4_step_fused(w, E[st], o->E0, hs, nullptr, s))) return rc;
+  if ((rc = field_pair_create(H0, mu, 0, nb, &fp.p))) return rc;
+  const size_t vb = (size_t)N * nb * 16;
+  DevBuf acc, Ed, ctl;
+  CUDA_TRY_S(cudaMalloc(&acc.p, vb));
+  CUDA_TRY_S(cudaMalloc(&Ed.p, (size_t)o->nsteps * nb * 8));
+  CUDA_TRY_S(cudaMalloc(&ctl.p, sizeof(SweepCtl)));
+  CUDA_TRY_S(cudaMemcpyAsync(Ed.p, E, (size_t)o->nsteps * nb * 8, cudaMemcpyHostToDevice, s));
+  ctl_set_kernel<<<1, 1, 0, s>>>((SweepCtl*)ctl.p, 0, -1);
+  Sweep w;
+  sweep_init(w, fp.p, (SweepCtl*)ctl.p, Ed.p, nb, o, false);
+  w.y = (double2*)psi;
+  w.acc = (double2*)acc.p;
+  CUDA_TRY_S(cudaMemcpyAsync(w.a.x, psi, vb, cudaMemcpyDeviceToDevice, s));
+  const bool graph = !o->no_graph;
+  for (int k = 0; k < o->nsteps; ++k)
+    if ((rc = run_interval(w, graph, s))) return rc;
   CUDA_TRY_S(cudaStreamSynchronize(s));
   return EVR_OK;
 }
 
+extern "C" int evr_sg4_rk4_field(evr_sg4_ctx* H0, evr_sg4_ctx* mu, const evr_rk4_opts* o, const double* E, double* psi,
+                                 void* stream) {
+  return evr_sg4_rk4_field_batch(H0, mu, o, 1, E, psi, stream);
+}
+
 // Optimal-control gradient.  Stream A runs the forward sweep (checkpoints
-// every C field intervals, the stages of the last segment kept), then the
-// backward sweep segment by segment; stream B recomputes segment k-1 from
+// every C field intervals, the stage inputs of the last segment kept), then
+// the backward sweep segment by segment; stream B recomputes segment k-1 from
 // its checkpoint (keeping its stage inputs) while stream A runs the adjoint
 // of segment k, with two stage buffers alternating between them.  Both
-// streams' launches are small, so they share the SMs.
+// streams' launches are small, so they share the SMs.  Each sweep replays
+// the CUDA graph of one field interval (or launches the same kernels).
 extern "C" int evr_sg4_oc_gradient(evr_sg4_ctx* H0, evr_sg4_ctx* mu, const evr_rk4_opts* o, const double* E,
                                    const double* psi0, const double* target, double* J, double* grad, void* stream) {
   long long N = 0;
-  int rc = check_field_args(H0, mu, o, E, &N);
+  int rc = check_field_args(H0, mu, o, 1, E, &N);
   if (rc) return rc;
   if (!psi0 || !target || !J || !grad) return set_error(EVR_ERR_ARG, "oc_gradient: NULL argument");
   cudaStream_t sA = (cudaStream_t)stream;
@@ -879,30 +1300,45 @@ extern "C" int evr_sg4_oc_gradient(evr_sg4_ctx* H0, evr_sg4_ctx* mu, const evr_r
   const int C = o->checkpoint, ns = o->nsteps, nseg = (ns + C - 1) / C, nsub = o->nsub;
   const double hs = o->dt / nsub;
   const size_t vb = (size_t)N * 16;
-  const int nblk = join_blocks(N);
+  const bool graph = !o->no_graph;
   PairGuard fwd, adj;
-  if ((rc = field_pair_create(H0, mu, 0, &fwd.p)) || (rc = field_pair_create(H0, mu, 1, &adj.p))) return rc;
-  DevBuf y, acc, ck, rec, lam, l, yb, gpart, g, ov;
+  if ((rc = field_pair_create(H0, mu, 0, 1, &fwd.p)) || (rc = field_pair_create(H0, mu, 1, 1, &adj.p))) return rc;
+  DevBuf y, acc, ck, rec, lam, l, yb, gpart, g, ov, Ed, ctl;
   for (DevBuf* b : {&y, &acc, &lam, &l, &yb}) CUDA_TRY_S(cudaMalloc(&b->p, vb));
-  CUDA_TRY_S(cudaMalloc(&ck.p, vb * nseg));                                // checkpoints
-  const size_t seg_rec = (size_t)C * nsub * 4 * 2 * N;                    // doubles: stage inputs of a segment
-  CUDA_TRY_S(cudaMalloc(&rec.p, seg_rec * 2 * 8));                         // two alternating segment buffers
-  CUDA_TRY_S(cudaMalloc(&gpart.p, (size_t)ns * nsub * 4 * nblk * 8));
+  CUDA_TRY_S(cudaMalloc(&ck.p, vb * nseg));                                 // checkpoints
+  const size_t seg_rec = (size_t)C * nsub * 4 * N;                         // complex: stage inputs of a segment
+  CUDA_TRY_S(cudaMalloc(&rec.p, seg_rec * 2 * 16));                         // two alternating segment buffers
   CUDA_TRY_S(cudaMalloc(&g.p, (size_t)ns * 8));
   CUDA_TRY_S(cudaMalloc(&ov.p, 16));
-  FwdSweep w{fwd.p, field_pair_view(fwd.p), y.p, acc.p, nblk};
-  auto rec_of = [&](int seg, int stp, int u) {
-    return rec.p + (size_t)(seg & 1) * seg_rec + ((size_t)(stp - seg * C) * nsub + u) * 4 * 2 * N;
-  };
-  // forward sweep (stream A)
-  CUDA_TRY_S(cudaMemcpyAsync(y.p, psi0, vb, cudaMemcpyDeviceToDevice, sA));
-  CUDA_TRY_S(cudaMemcpyAsync(w.v.x, psi0, vb, cudaMemcpyDeviceToDevice, sA));
-  for (int stp = 0; stp < ns; ++stp) {
-    const int seg = stp / C;
-    if (stp % C == 0) CUDA_TRY_S(cudaMemcpyAsync(ck.p + (size_t)seg * 2 * N, y.p, vb, cudaMemcpyDeviceToDevice, sA));
-    for (int u = 0; u < nsub; ++u)
-      if ((rc = rk4_step_fused(w, E[stp], o->E0, hs, seg == nseg - 1 ? rec_of(seg, stp, u) : nullptr, sA))) return rc;
+  CUDA_TRY_S(cudaMalloc(&Ed.p, (size_t)ns * 8));
+  CUDA_TRY_S(cudaMalloc(&ctl.p, 3 * sizeof(SweepCtl)));                    // forward (A), recompute (B), adjoint (A)
+  SweepCtl* cF = (SweepCtl*)ctl.p;
+  SweepCtl* cB = cF + 1;
+  SweepCtl* cA = cF + 2;
+  CUDA_TRY_S(cudaMemcpyAsync(Ed.p, E, (size_t)ns * 8, cudaMemcpyHostToDevice, sA));
+  Sweep wf, wb, wa;
+  sweep_init(wf, fwd.p, cF, Ed.p, 1, o, false);
+  sweep_init(wb, fwd.p, cB, Ed.p, 1, o, false);
+  sweep_init(wa, adj.p, cA, Ed.p, 1, o, true);
+  CUDA_TRY_S(cudaMalloc(&gpart.p, (size_t)ns * nsub * 4 * wa.nblk * 8));
+  for (Sweep* w : {&wf, &wb}) {
+    w->y = (double2*)y.p;
+    w->acc = (double2*)acc.p;
+    w->a.rec = (double2*)rec.p;
+    w->a.seg_rec = (long long)seg_rec;
   }
+  wf.ck = (double2*)ck.p;
+  wa.y = (double2*)l.p;
+  wa.acc = (double2*)yb.p;
+  wa.gpart = gpart.p;
+  wa.a.rec = (double2*)rec.p;
+  wa.a.seg_rec = (long long)seg_rec;
+  // forward sweep (stream A): checkpoints, the stage inputs of the last segment kept
+  ctl_set_kernel<<<1, 1, 0, sA>>>(cF, 0, nseg - 1);
+  CUDA_TRY_S(cudaMemcpyAsync(y.p, psi0, vb, cudaMemcpyDeviceToDevice, sA));
+  CUDA_TRY_S(cudaMemcpyAsync(wf.a.x, psi0, vb, cudaMemcpyDeviceToDevice, sA));
+  for (int stp = 0; stp < ns; ++stp)
+    if ((rc = run_interval(wf, graph, sA))) return rc;
   // S = <target|psi_N>, J = |S|^2, lambda_N = S target
   cdot_cols_kernel<<<1, 256, 0, sA>>>((const double2*)target, (const double2*)y.p, N, N, (double2*)ov.p);
   double2 S;
@@ -910,43 +1346,29 @@ extern "C" int evr_sg4_oc_gradient(evr_sg4_ctx* H0, evr_sg4_ctx* mu, const evr_r
   CUDA_TRY_S(cudaStreamSynchronize(sA));  // also: the forward pair and its buffers are free for stream B
   *J = S.x * S.x + S.y * S.y;
   cscale_kernel<<<64, 256, 0, sA>>>((double2*)lam.p, (const double2*)target, N, S.x, S.y);
-  const FieldPairView av = field_pair_view(adj.p);
-  const double cr = std::cos(o->E0 * hs), ci = std::sin(o->E0 * hs);  // e^{+i E0 h}
-  rk_adjoint_start_kernel<<<nblk, 256, 0, sA>>>((double2*)l.p, (const double2*)lam.p, (double2*)av.x, N, hs, cr, ci,
-                                                o->E0 != 0.0);
+  rk_adjoint_start_kernel<<<64, 256, 0, sA>>>((double2*)l.p, (const double2*)lam.p, wa.a.x, N, hs, wa.cr, wa.ci,
+                                             o->E0 != 0.0);
+  ctl_set_kernel<<<1, 1, 0, sA>>>(cA, ns, -1);
   CUDA_TRY_S(cudaGetLastError());
   cudaEvent_t ready[2] = {sg.ev[0], sg.ev[1]}, freed[2] = {sg.ev[2], sg.ev[3]};
-  StageIn a{(const double2*)av.part, av.fun_chunk, 2 * av.n_chunks, N, (double2*)av.x, 0.0, o->E0, hs};
   for (int seg = nseg - 1; seg >= 0; --seg) {
     if (seg > 0) {  // stream B: recompute segment seg-1 into the other buffer
       const int ps = seg - 1;
       if (seg + 1 < nseg) CUDA_TRY_S(cudaStreamWaitEvent(sB, freed[ps & 1], 0));
+      ctl_set_kernel<<<1, 1, 0, sB>>>(cB, ps * C, -2);
       CUDA_TRY_S(cudaMemcpyAsync(y.p, ck.p + (size_t)ps * 2 * N, vb, cudaMemcpyDeviceToDevice, sB));
-      CUDA_TRY_S(cudaMemcpyAsync(w.v.x, y.p, vb, cudaMemcpyDeviceToDevice, sB));
+      CUDA_TRY_S(cudaMemcpyAsync(wb.a.x, y.p, vb, cudaMemcpyDeviceToDevice, sB));
       for (int stp = ps * C; stp < std::min(ns, (ps + 1) * C); ++stp)
-        for (int u = 0; u < nsub; ++u)
-          if ((rc = rk4_step_fused(w, E[stp], o->E0, hs, rec_of(ps, stp, u), sB))) return rc;
+        if ((rc = run_interval(wb, graph, sB))) return rc;
       CUDA_TRY_S(cudaEventRecord(ready[ps & 1], sB));
     }
     if (seg < nseg - 1) CUDA_TRY_S(cudaStreamWaitEvent(sA, ready[seg & 1], 0));
     const int a0 = seg * C, b0 = std::min(ns, a0 + C);
-    for (int stp = b0 - 1; stp >= a0; --stp) {  // stream A: adjoint of segment seg
-      a.E = E[stp];
-      for (int u = nsub - 1; u >= 0; --u) {
-        const double2* st = (const double2*)rec_of(seg, stp, u);
-        double* gp = gpart.p + ((size_t)stp * nsub + (nsub - 1 - u)) * 4 * nblk;
-        for (int stage = 4; stage >= 1; --stage) {
-          if ((rc = field_pair_apply(adj.p, sA))) return rc;
-          rk_adjoint_stage_kernel<<<nblk, 256, 0, sA>>>(a, stage, (double2*)l.p, (double2*)yb.p,
-                                                        st + (size_t)(stage - 1) * N, gp + (4 - stage) * nblk, cr,
-                                                        ci);
-        }
-      }
-    }
-    CUDA_TRY_S(cudaGetLastError());
+    for (int stp = b0 - 1; stp >= a0; --stp)  // stream A: adjoint of segment seg
+      if ((rc = run_interval(wa, graph, sA))) return rc;
     CUDA_TRY_S(cudaEventRecord(freed[seg & 1], sA));
   }
-  rk_grad_sum_kernel<<<(ns + 255) / 256, 256, 0, sA>>>(gpart.p, ns, nsub, nblk, g.p);
+  rk_grad_sum_kernel<<<(ns + 255) / 256, 256, 0, sA>>>(gpart.p, ns, nsub, wa.nblk, g.p);
   CUDA_TRY_S(cudaMemcpyAsync(grad, g.p, (size_t)ns * 8, cudaMemcpyDeviceToHost, sA));
   CUDA_TRY_S(cudaStreamSynchronize(sA));
   CUDA_TRY_S(cudaStreamSynchronize(sB));
@@ -1005,7 +1427,7 @@ extern "C" int evr_sg4_multi_cheby_propagate(evr_sg4_multi* m, const evr_cheby_o
     w2[k] = buf(1, k);
     CUDA_TRY_S(cudaMemcpyAsync(buf(4, k), psi[k], (size_t)len[k] * 16, cudaMemcpyDeviceToDevice, s));
   }
-  const int G = 2 * 152, B = 256;
+  const int B = EW_THREADS;
   auto autocorr_at = [&](int step) -> int {
     if (!autocorr) return EVR_OK;
     for (int k = 0; k < n; ++k) {
@@ -1048,7 +1470,7 @@ extern "C" int evr_sg4_multi_cheby_propagate(evr_sg4_multi* m, const evr_cheby_o
         w1[k] = buf(0, k);
         w2[k] = buf(1, k);
         CUDA_TRY_S(cudaMemcpyAsync(w1[k], psi[k], (size_t)len[k] * 16, cudaMemcpyDeviceToDevice, s));
-        cscale_kernel<<<G, B, 0, s>>>(buf(3, k), w1[k], len[k], cf[k][0], 0.0);
+        cscale_kernel<<<ew_grid(len[k]), B, 0, s>>>(buf(3, k), w1[k], len[k], cf[k][0], 0.0);
         CUDA_TRY_S(cudaMemsetAsync(w2[k], 0, (size_t)len[k] * 16, s));
       }
       // w2 = -i Hs w1, out += c_2 w2 ; then w3 = w1 - 2i Hs w2, out += c_k w3
@@ -1064,10 +1486,10 @@ extern "C" int evr_sg4_multi_cheby_propagate(evr_sg4_multi* m, const evr_cheby_o
         for (int k = 0; k < n; ++k) {
           if (!pending[k]) continue;
           if (ord == 2) {
-            cheby_update_kernel<<<G, B, 0, s>>>(w2[k], buf(2, k), buf(3, k), len[k], 0.0, 0.0, -1.0, cf[k][1],
+            cheby_update_kernel<<<ew_grid(len[k]), B, 0, s>>>(w2[k], buf(2, k), buf(3, k), len[k], 0.0, 0.0, -1.0, cf[k][1],
                                                 last ? nrm.p + k : nullptr);
           } else {
-            cheby_update_kernel<<<G, B, 0, s>>>(w1[k], buf(2, k), buf(3, k), len[k], 1.0, 0.0, -2.0,
+            cheby_update_kernel<<<ew_grid(len[k]), B, 0, s>>>(w1[k], buf(2, k), buf(3, k), len[k], 1.0, 0.0, -2.0,
                                                 cf[k][ord - 1], last ? nrm.p + k : nullptr);
             std::swap(w1[k], w2[k]);
           }
@@ -1086,7 +1508,7 @@ extern "C" int evr_sg4_multi_cheby_propagate(evr_sg4_multi* m, const evr_cheby_o
           continue;
         }
         const double ph = -E0[k] * dt;  // psi = out exp(-i E0 dt)
-        cscale_kernel<<<G, B, 0, s>>>((double2*)psi[k], buf(3, k), len[k], std::cos(ph), std::sin(ph));
+        cscale_kernel<<<ew_grid(len[k]), B, 0, s>>>((double2*)psi[k], buf(3, k), len[k], std::cos(ph), std::sin(ph));
         pending[k] = 0;
       }
       CUDA_TRY_S(cudaGetLastError());

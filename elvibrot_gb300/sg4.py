@@ -69,7 +69,8 @@ class Desc(ctypes.Structure):
 
 class DavidsonOpts(ctypes.Structure):
     _fields_ = [("nev", ctypes.c_int), ("block", ctypes.c_int), ("max_subspace", ctypes.c_int),
-                ("max_it", ctypes.c_int), ("conv_resi", ctypes.c_double), ("symmetrize", ctypes.c_int)]
+                ("max_it", ctypes.c_int), ("conv_resi", ctypes.c_double), ("symmetrize", ctypes.c_int),
+                ("no_graph", ctypes.c_int)]
 
 
 class ChebyOpts(ctypes.Structure):
@@ -78,9 +79,14 @@ class ChebyOpts(ctypes.Structure):
                 ("no_graph", ctypes.c_int)]
 
 
+class TuneResult(ctypes.Structure):
+    _fields_ = [("geo", ctypes.c_int), ("rmax", ctypes.c_int), ("split", ctypes.c_int), ("ms", ctypes.c_double),
+                ("default_ms", ctypes.c_double), ("from_cache", ctypes.c_int)]
+
+
 class RK4Opts(ctypes.Structure):
     _fields_ = [("dt", ctypes.c_double), ("nsteps", ctypes.c_int), ("checkpoint", ctypes.c_int),
-                ("E0", ctypes.c_double), ("nsub", ctypes.c_int)]
+                ("E0", ctypes.c_double), ("nsub", ctypes.c_int), ("no_graph", ctypes.c_int)]
 
 
 class OpDesc(ctypes.Structure):
@@ -113,8 +119,13 @@ def _declare(L):
         "evr_sg4_last_launches": [vp, ctypes.POINTER(ll)],
         "evr_sg4_last_geometry": [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)],
         "evr_probe_fp64_peak": [dp],
+        "evr_probe_fp64_pipes": [dp, dp, dp],
+        "evr_sg4_set_plan": [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int],
+        "evr_sg4_get_plan": [vp, ip, ip, ip],
+        "evr_sg4_tune_plan": [vp, ctypes.c_int, ctypes.c_int, ctypes.c_char_p, ctypes.POINTER(TuneResult)],
         "evr_sg4_ctx_sizes": [vp, ctypes.POINTER(ll)],
         "evr_sg4_rk4_field": [vp, vp, ctypes.POINTER(RK4Opts), dp, vp, vp],
+        "evr_sg4_rk4_field_batch": [vp, vp, ctypes.POINTER(RK4Opts), ctypes.c_int, dp, vp, vp],
         "evr_sg4_oc_gradient": [vp, vp, ctypes.POINTER(RK4Opts), dp, vp, vp, dp, dp, vp],
         "evr_sg4_cheby_propagate": [vp, ctypes.POINTER(ChebyOpts), ctypes.c_int, vp, vp, dp,
                                     ctypes.POINTER(ctypes.c_int), vp],
@@ -319,6 +330,23 @@ class ParamOp:
         check(lib().evr_sg4_tune(self._h, int(nrhs), 2 if complex_ else 0, ctypes.byref(r), ctypes.byref(t)))
         return r.value, t.value
 
+    def tune_plan(self, nrhs: int, complex_: bool = False, cache_path: Optional[str] = None) -> dict:
+        """Times the plan candidates on nrhs vectors and applies the fastest
+        (evr_sg4_tune_plan); with cache_path the winner is recorded / reused."""
+        r = TuneResult()
+        path = cache_path.encode() if cache_path else None
+        check(lib().evr_sg4_tune_plan(self._h, int(nrhs), 2 if complex_ else 0, path, ctypes.byref(r)))
+        return {"geo": r.geo, "rmax": r.rmax, "split": r.split, "ms": r.ms, "default_ms": r.default_ms,
+                "from_cache": bool(r.from_cache)}
+
+    def set_plan(self, geo: int = -1, rmax: int = 32, split: int = 0):
+        check(lib().evr_sg4_set_plan(self._h, int(geo), int(rmax), int(split)))
+
+    def get_plan(self):
+        g, r, sp = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(lib().evr_sg4_get_plan(self._h, ctypes.byref(g), ctypes.byref(r), ctypes.byref(sp)))
+        return g.value, r.value, sp.value
+
     @property
     def field_slices(self) -> int:
         """Slices the analytic operator fields are evaluated in per H.psi (0: resident)."""
@@ -379,13 +407,13 @@ class ParamOp:
         return d
 
     def davidson(self, nev: int, block: int = 0, max_subspace: int = 0, max_it: int = 500,
-                 conv_resi: float = 1e-8, symmetrize: bool = False, guess=None, diag=None):
+                 conv_resi: float = 1e-8, symmetrize: bool = False, guess=None, diag=None, graph: bool = True):
         """Lowest nev levels (sub_propagation_Davidson).  Returns (evals, evecs
         (CUDA tensor nev x N), residual norms, iterations); raises EVRError
         when max_it is reached."""
         import torch
         N = self.basis.nvec
-        o = DavidsonOpts(nev, block, max_subspace, max_it, conv_resi, 1 if symmetrize else 0)
+        o = DavidsonOpts(nev, block, max_subspace, max_it, conv_resi, 1 if symmetrize else 0, 0 if graph else 1)
         ev = np.zeros(nev)
         rs = np.zeros(nev)
         vec = torch.empty((nev, N), dtype=torch.float64, device="cuda")
@@ -414,19 +442,32 @@ class ParamOp:
         a = ac.reshape(nsteps + 1, nrhs, 2)
         return a[..., 0] + 1j * a[..., 1], used.value
 
-    def rk4_field(self, mu: "ParamOp", E: np.ndarray, psi, dt: float, E0: float = 0.0, nsub: int = 1):
+    def rk4_field(self, mu: "ParamOp", E: np.ndarray, psi, dt: float, E0: float = 0.0, nsub: int = 1,
+                  graph: bool = True):
         """march_RK4_field: propagates the CUDA complex128 vector psi (N,) in place
         under H0 - E(t) mu, E held at E[k] over step k."""
         E = np.ascontiguousarray(E, dtype=np.float64)
-        o = RK4Opts(dt, len(E), 1, E0, nsub)
+        o = RK4Opts(dt, len(E), 1, E0, nsub, 0 if graph else 1)
         check(lib().evr_sg4_rk4_field(self._h, mu._h, ctypes.byref(o), _dp(E), psi.data_ptr(), 0))
         return psi
 
+    def rk4_field_batch(self, mu: "ParamOp", E: np.ndarray, psi, dt: float, E0: float = 0.0, nsub: int = 1,
+                        graph: bool = True):
+        """Several packets at once, each with its own field: E is (nsteps, nb),
+        psi a contiguous CUDA complex128 (nb, N) tensor (row b = packet b),
+        propagated in place."""
+        E = np.ascontiguousarray(E, dtype=np.float64)
+        if E.ndim != 2 or psi.dim() != 2 or psi.shape[0] != E.shape[1] or not psi.is_contiguous():
+            raise EVRError(1, "rk4_field_batch: E (nsteps, nb) and a contiguous psi (nb, N)")
+        o = RK4Opts(dt, E.shape[0], 1, E0, nsub, 0 if graph else 1)
+        check(lib().evr_sg4_rk4_field_batch(self._h, mu._h, ctypes.byref(o), E.shape[1], _dp(E), psi.data_ptr(), 0))
+        return psi
+
     def oc_gradient(self, mu: "ParamOp", E: np.ndarray, psi0, target, dt: float, checkpoint: int = 45,
-                    E0: float = 0.0, nsub: int = 1):
+                    E0: float = 0.0, nsub: int = 1, graph: bool = True):
         """(J, dJ/dE) for J = |<target|psi(T)>|^2 by the adjoint of the RK4 steps."""
         E = np.ascontiguousarray(E, dtype=np.float64)
-        o = RK4Opts(dt, len(E), checkpoint, E0, nsub)
+        o = RK4Opts(dt, len(E), checkpoint, E0, nsub, 0 if graph else 1)
         J = ctypes.c_double()
         g = np.zeros(len(E))
         check(lib().evr_sg4_oc_gradient(self._h, mu._h, ctypes.byref(o), _dp(E), psi0.data_ptr(), target.data_ptr(),
@@ -589,3 +630,10 @@ def fp64_peak_tflops() -> float:
     t = ctypes.c_double()
     check(lib().evr_probe_fp64_peak(ctypes.byref(t)))
     return t.value
+
+
+def fp64_pipes_tflops() -> dict:
+    """DFMA, FP64 tensor-core MMA and both interleaved, in TFLOP/s."""
+    a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    check(lib().evr_probe_fp64_pipes(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+    return {"dfma": a.value, "dmma": b.value, "dmma_plus_dfma": c.value}

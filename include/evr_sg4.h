@@ -224,13 +224,38 @@ int evr_sg4_set_field_budget(evr_sg4_ctx* c, long long bytes);
 /* Number of field slices of the current operator (0: resident fields). */
 int evr_sg4_field_slices(const evr_sg4_ctx* c, long long* nslices);
 
-/* Autotuner (the counterpart of Tune_SG4threads_HPsi, SRC/sub_main/vib.f90:2013,
- * which times H.psi for each OpenMP thread count): times H.psi on nrhs
- * vectors (flags: EVR_APPLY_COMPLEX or 0) for each cap on the right-hand
- * sides one work item carries (1, 2, 4, ..., 32; larger blocks reuse the 1-D
- * matrices and fields more, smaller ones balance better) and keeps the
- * fastest for this context.  best_rmax/best_ms may be NULL.  Results do not
- * depend on the cap. */
+/* Plan knobs of a context, applied from its next H.psi (no reference
+ * interface: the reference's tunable is the OpenMP thread count of
+ * Tune_SG4threads_HPsi, SRC/sub_main/vib.f90:2013-2123):
+ *   geo   : launch geometry, -1 automatic (per work plan), 0 wide (4 CTAs
+ *           per SM), 1 narrow (8 per SM, D <= 6 only), 2 mid (6 per SM);
+ *   rmax  : most right-hand sides one work item carries, 1..32;
+ *   split : mode passes, 0 thread mapping chosen per pass, 1 one thread per
+ *           fibre, 2 one thread per output element.
+ * Results do not depend on them: every setting runs the same arithmetic per
+ * Smolyak term and right-hand side (the same bits). */
+int evr_sg4_set_plan(evr_sg4_ctx* c, int geo, int rmax, int split);
+int evr_sg4_get_plan(const evr_sg4_ctx* c, int* geo, int* rmax, int* split);
+
+/* Autotuner (the counterpart of Tune_SG4threads_HPsi, SRC/sub_main/
+ * vib.f90:2013-2123, which times H.psi for each OpenMP thread count and
+ * keeps the fastest): times H.psi on nrhs vectors (flags: EVR_APPLY_COMPLEX
+ * or 0) with the automatic plan and with every candidate (geometry x rmax in
+ * {4, 8, 16, 32} x split mode; best of three after one untimed call), and
+ * applies the fastest to the context.  With cache_path (a JSON file, created
+ * if absent) the winner is recorded under a key of the workload's shape (D,
+ * L, LB, type, channels, N, nrhs, complex, G given), and a later call with
+ * the same shape applies the recorded plan without timing (from_cache = 1).
+ * out may be NULL. */
+typedef struct {
+  int geo, rmax, split;  /* the plan applied */
+  double ms;             /* its H.psi time (best of three) */
+  double default_ms;     /* the automatic plan's H.psi time */
+  int from_cache;        /* 1: read from cache_path, nothing timed */
+} evr_tune_result;
+int evr_sg4_tune_plan(evr_sg4_ctx* c, int nrhs, int flags, const char* cache_path, evr_tune_result* out);
+/* Short form of evr_sg4_tune_plan without a cache: returns the winning rmax
+ * and its time. */
 int evr_sg4_tune(evr_sg4_ctx* c, int nrhs, int flags, int* best_rmax, double* best_ms);
 
 /* Sizes of a context: out[0..7] as evr_sg4_desc_sizes, except out[0] = the
@@ -267,6 +292,12 @@ typedef struct {
   int max_it;          /* iterations */
   double conv_resi;    /* residual 2-norm threshold */
   int symmetrize;      /* 1: work on (H + H^T)/2 */
+  int no_graph;        /* 0: each iteration is two recorded CUDA graphs (Ritz vectors,
+                          residuals and their norms; then the expansion: correction,
+                          Gram-Schmidt against the basis and within the block, H.psi,
+                          projected matrix), replayed with the host's small dense
+                          eigenproblem between them -- two host synchronisations per
+                          iteration; 1: the same steps launched one by one */
 } evr_davidson_opts;
 int evr_sg4_davidson(evr_sg4_ctx* c, const evr_davidson_opts* o, const double* guess, int nguess,
                      const double* diag, double* evals, double* evecs, double* resid, int* iterations,
@@ -348,9 +379,21 @@ typedef struct {
   double E0;           /* energy shift: stages use H0 - E0, then psi *= exp(-i E0 dt)
                           (fcn_field's para_H%E0; mid-spectrum keeps RK4 stable) */
   int nsub;            /* RK4 steps per field interval (dt/nsub each, E held) */
+  int no_graph;        /* 0: every field interval (nsub steps x 4 stages, each one H0/mu
+                          launch, one chunk-sum launch and one stage update) is recorded
+                          once as a CUDA graph and replayed, the interval index kept on
+                          the device; 1: the same kernels launched one by one (same bits) */
 } evr_rk4_opts;
 int evr_sg4_rk4_field(evr_sg4_ctx* H0, evr_sg4_ctx* mu, const evr_rk4_opts* o, const double* E, double* psi,
                       void* stream);
+/* nb packets propagated together, packet b under its own field E[k*nb + b]
+ * (E: host [nsteps*nb]); psi: device complex128 N x nb (ld N), in place.
+ * One H0/mu launch per stage serves all packets (the reference propagates
+ * its nb_WP packets together, sub_propagation25, sub_control.f90).  Each
+ * packet's result is that of evr_sg4_rk4_field under its own field, to
+ * rounding. */
+int evr_sg4_rk4_field_batch(evr_sg4_ctx* H0, evr_sg4_ctx* mu, const evr_rk4_opts* o, int nb, const double* E,
+                            double* psi, void* stream);
 
 /* Optimal-control objective J = |<target|psi(T)>|^2 after the RK4 propagation
  * above from psi0, and its exact gradient dJ/dE[k] for every field sample,
@@ -377,6 +420,12 @@ const char* evr_sg4_last_error(void);
 /* Measured FP64 FMA throughput of the current device in TFLOP/s (a short
  * in-bounds DFMA loop; used as the roofline denominator). */
 int evr_probe_fp64_peak(double* tflops);
+
+/* The FP64 pipes of the current device, each in TFLOP/s: the DFMA loop
+ * above, FP64 tensor-core MMA alone (mma.sync m8n8k4 f64, registers only),
+ * and MMA with DFMA chains interleaved in the same warps (their sum, which
+ * shows whether the two run on separate units or share one). */
+int evr_probe_fp64_pipes(double* dfma_tflops, double* dmma_tflops, double* mixed_tflops);
 
 #ifdef __cplusplus
 }

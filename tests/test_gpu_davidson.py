@@ -86,3 +86,19 @@ def test_davidson_benchmark_6d_20_levels():
     ref = np.linalg.eigvalsh(0.5 * (H + H.T))[:20]
     print(f"6-D L=8 Davidson: {its} iterations, max |dE| {np.max(np.abs(ev - ref)):.2e} hartree")
     assert np.max(np.abs(ev - ref)) <= TOL_E
+
+
+def test_davidson_graph_replay_is_bit_identical():
+    """Each iteration replays two recorded CUDA graphs (Ritz vectors and
+    residual norms; the expansion with its H.psi and projected matrix); the
+    same steps launched one by one give the same bits."""
+    need_cuda()
+    m = make_model(5, 6, 10, 78)
+    op = m.operator()
+    d = op.diagonal()
+    runs = [op.davidson(12, block=6, max_subspace=30, conv_resi=1e-9, symmetrize=True, diag=d, max_it=500,
+                        graph=g) for g in (False, True)]
+    assert runs[0][3] == runs[1][3]                      # iterations
+    assert np.array_equal(runs[0][0], runs[1][0])        # eigenvalues
+    assert torch.equal(runs[0][1], runs[1][1])           # Ritz vectors
+    assert np.array_equal(runs[0][2], runs[1][2])        # residual norms

@@ -213,3 +213,57 @@ def test_multi_chebyshev_redoes_diverging_contexts_alone():
     for k, (w, U) in enumerate(spec):
         ex = U @ (np.exp(-1j * w * 10.0)[:, None] * (U.T @ start[k]))
         assert np.max(np.abs(psis[k].cpu().numpy().T - ex)) < 1e-9
+
+
+def test_uneven_64_instances_lock_step_chebyshev():
+    """The uneven-instance workload itself: 64 seeded Hamiltonians (D 3..9,
+    L 4..10, type 1) with 8 complex packets each, propagated 5 steps of an
+    order-30 Chebyshev expansion (dt = 10 a.u.) in lock-step, one merged
+    H.psi launch per expansion order.  Each instance's packets keep their
+    norm to 1e-11, and the 56 smallest instances (the per-instance reruns of
+    the 8 largest would double the test's minutes) agree with their own
+    single-context evr_sg4_cheby_propagate at the same fixed order to 1e-14
+    (the bar of the small lock-step test above)."""
+    need_cuda()
+    from elvibrot_gb300.configs import uneven_instances
+    models = uneven_instances(64)
+    ops = [m.operator() for m in models]
+    n, nrhs, dt, npoly, nsteps = len(ops), 8, 10.0, 30, 5
+    # spectral bounds: power iteration on H and on Hmax - H, one real vector per instance
+    p1 = MultiOp(ops, [1] * n)
+    g = torch.Generator(device="cpu").manual_seed(5)
+    v = [torch.randn((1, op.basis.N), generator=g, dtype=torch.float64).cuda() for op in ops]
+    hv = [torch.empty_like(x) for x in v]
+    for _ in range(40):
+        v = [x / torch.linalg.vector_norm(x) for x in v]
+        p1.hpsi(v, hv)
+        top = np.array([float((a * b).sum()) for a, b in zip(v, hv)])
+        v, hv = hv, v
+    Hmax = top * 1.1
+    v = [torch.randn((1, op.basis.N), generator=g, dtype=torch.float64).cuda() for op in ops]
+    for _ in range(40):
+        v = [x / torch.linalg.vector_norm(x) for x in v]
+        p1.hpsi(v, hv, E0=list(Hmax), Esc=[-1.0] * n)
+        low = Hmax - np.array([float((a * b).sum()) for a, b in zip(v, hv)])
+        v, hv = hv, v
+    Hmin = low - 0.1 * (Hmax - low)
+    psis = []
+    for k, op in enumerate(ops):
+        P = _rand(op, nrhs, True, 500 + k)
+        psis.append(P / torch.linalg.vector_norm(P, dim=1, keepdim=True))
+    start = [P.clone() for P in psis]
+    plan = MultiOp(ops, [nrhs] * n, complex_=True)
+    ac = plan.cheby_propagate(psis, list(Hmin), list(Hmax), dt, npoly, nsteps)
+    torch.cuda.synchronize()
+    drift = max(float(torch.linalg.vector_norm(P, dim=1).sub(1.0).abs().max()) for P in psis)
+    print(f"64 instances x 8 packets, {nsteps} lock-step order-{npoly} steps: max norm drift {drift:.2e}")
+    assert drift <= 1e-11
+    sizes = [op.basis.sum_nq for op in ops]
+    small = sorted(range(n), key=lambda k: sizes[k])[:56]
+    for k in small:
+        P = start[k].clone()
+        a1, used = ops[k].cheby_propagate(P, Hmin[k], Hmax[k], dt, npoly=npoly, nsteps=nsteps, poly_tol=0.0,
+                                          graph=False)
+        d = (P - psis[k]).abs().max().item()
+        assert d <= 1e-14, (k, d)
+        assert np.max(np.abs(a1 - ac[k])) <= 1e-14, k

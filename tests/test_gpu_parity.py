@@ -288,3 +288,50 @@ def test_autotuner_keeps_results_bitwise():
     op.hpsi_dev(P, after)
     torch.cuda.synchronize()
     assert torch.equal(before, after)
+
+
+def _time_hpsi(op, P, reps=5):
+    out = torch.empty_like(P)
+    op.hpsi_dev(P, out)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = 1e30
+    for _ in range(reps):
+        e0.record()
+        op.hpsi_dev(P, out)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    return best, out
+
+
+def test_plan_tuner_every_plan_same_bits_and_cached(tmp_path):
+    """The autotuner's search space (geometry x RHS cap x mode-pass mapping)
+    never changes the bits; the tuned plan is not slower than the automatic
+    one beyond timing noise; its JSON cache gives the same plan without
+    timing."""
+    need_cuda()
+    m = make_model(6, 6, 10, 20261215)
+    op = m.operator()
+    P = torch.from_numpy(np.ascontiguousarray(random_psi(op.basis.N, 20, 4).T)).cuda()
+    t_auto, ref = _time_hpsi(op, P)
+    for geo in (0, 1, 2):
+        for rmax, split in ((32, 0), (4, 1), (8, 2)):
+            op.set_plan(geo, rmax, split)
+            out = torch.empty_like(P)
+            op.hpsi_dev(P, out)
+            torch.cuda.synchronize()
+            assert torch.equal(out, ref), (geo, rmax, split)
+    op.set_plan(-1, 32, 0)
+    cache = str(tmp_path / "tune.json")
+    r = op.tune_plan(20, cache_path=cache)
+    assert not r["from_cache"] and r["ms"] <= r["default_ms"]
+    assert op.get_plan() == (r["geo"], r["rmax"], r["split"])
+    t_tuned, out = _time_hpsi(op, P)
+    assert torch.equal(out, ref)
+    print(f"tuned plan {r}: {t_tuned:.3f} ms vs automatic {t_auto:.3f} ms")
+    assert t_tuned <= 1.05 * t_auto
+    op2 = m.operator()
+    r2 = op2.tune_plan(20, cache_path=cache)
+    assert r2["from_cache"] and (r2["geo"], r2["rmax"], r2["split"]) == (r["geo"], r["rmax"], r["split"])
+    import json
+    assert len(json.load(open(cache))) == 1

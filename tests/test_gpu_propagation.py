@@ -219,3 +219,69 @@ def test_oc_gradient_converges_to_the_build_field_formula():
         print(f"nsub={nsub}: J={J:.10e} (formula {Jref:.10e}), max|g-g_formula|/max|g| = {errs[nsub]:.3e}")
     assert errs[40] <= 2e-5
     assert errs[20] / errs[40] >= 10.0
+
+
+def test_rk4_and_gradient_graph_replay_is_bit_identical():
+    """Each field interval replayed from its recorded CUDA graph gives the same
+    bits as the same kernels launched one by one (forward sweep, and the
+    gradient's forward, recompute and adjoint sweeps)."""
+    need_cuda()
+    H0, mu, H, Mu, U, E, E0 = _oc_setup(30)
+    E = E * 50.0
+    psi0 = torch.from_numpy(U[:, 0].astype(np.complex128)).cuda()
+    target = torch.from_numpy(U[:, 2].astype(np.complex128)).cuda()
+    outs = []
+    for graph in (False, True):
+        P = psi0.clone()
+        H0.rk4_field(mu, E, P, 5.0, E0=E0, nsub=4, graph=graph)
+        J, g = H0.oc_gradient(mu, E, psi0, target, 5.0, checkpoint=7, E0=E0, nsub=4, graph=graph)
+        outs.append((P.cpu(), J, g))
+    assert torch.equal(outs[0][0], outs[1][0])
+    assert outs[0][1] == outs[1][1]
+    assert np.array_equal(outs[0][2], outs[1][2])
+
+
+def test_rk4_batch_packets_match_single_packet_runs():
+    """Three packets, each under its own field, propagated together: every
+    packet gets the bits of its own single-packet propagation."""
+    need_cuda()
+    H0, mu, H, Mu, U, E, E0 = _oc_setup(25)
+    rng = np.random.default_rng(77)
+    Eb = np.stack([E * 50.0, -E * 20.0, rng.normal(0.0, 0.05, size=len(E))], axis=1)   # (nsteps, 3)
+    psi0 = np.stack([U[:, 0], U[:, 1] + 1j * U[:, 2], U[:, 3]]).astype(np.complex128)  # (3, N)
+    P = torch.from_numpy(psi0.copy()).cuda()
+    H0.rk4_field_batch(mu, Eb, P, 5.0, E0=E0, nsub=3)
+    for b in range(3):
+        Q = torch.from_numpy(psi0[b].copy()).cuda()
+        H0.rk4_field(mu, Eb[:, b], Q, 5.0, E0=E0, nsub=3)
+        assert torch.equal(P[b], Q), b
+
+
+def test_oc_gradient_full_size_matches_central_differences():
+    """The optimal-control workload at full size: 4-D L=7, 2000 field samples
+    of 5 a.u. (10 RK4 steps each), psi checkpointed every 45 samples; the
+    adjoint gradient against central differences (h = 1e-6) on 20 random
+    samples, the 40 perturbed fields propagated together as one batch."""
+    need_cuda()
+    from elvibrot_gb300.configs import config
+    cfg = config(3)
+    nsteps, dt, h, nsub = 2000, 5.0, 1e-6, 10
+    H0, mu, H, Mu, U, _, E0 = _oc_setup(8, seed=cfg["seed"])
+    E = np.random.Generator(np.random.PCG64(cfg["seed"])).normal(0.0, 1e-3, size=nsteps)
+    psi0 = torch.from_numpy(U[:, 0].astype(np.complex128)).cuda()
+    target = torch.from_numpy(U[:, 2].astype(np.complex128)).cuda()
+    J, g = H0.oc_gradient(mu, E, psi0, target, dt, checkpoint=45, E0=E0, nsub=nsub)
+    ks = np.random.default_rng(2000).choice(nsteps, size=20, replace=False)
+    Eb = np.repeat(E[:, None], 2 * len(ks) + 1, axis=1)
+    for i, k in enumerate(ks):
+        Eb[k, 2 * i] += h
+        Eb[k, 2 * i + 1] -= h
+    P = psi0[None, :].repeat(Eb.shape[1], 1).contiguous()
+    H0.rk4_field_batch(mu, Eb, P, dt, E0=E0, nsub=nsub)
+    Js = np.abs((target.conj()[None, :] * P).sum(dim=1).cpu().numpy()) ** 2
+    assert abs(Js[-1] - J) <= 1e-12 * J                  # the unperturbed field: the gradient's own J
+    fd = (Js[0:-1:2] - Js[1:-1:2]) / (2 * h)
+    scale = np.max(np.abs(g))
+    err = np.max(np.abs(g[ks] - fd))
+    print(f"OC gradient, 2000 samples: J={J:.6e} max|g|={scale:.3e} max|g-fd|={err:.3e} ({err / scale:.2e})")
+    assert err <= 1e-7 * scale
