@@ -81,6 +81,8 @@ int desc_sizes(const evr_sg4_desc* d, DescSizes* z) {
       nb *= d->nb_of_l[i * (d->L + 1) + l];
       nq *= d->nq_of_l[i * (d->L + 1) + l];
     }
+    if (nq >= (1LL << 27))  // the kernels' exact multiply-high divisions assume nq_t < 2^27
+      return set_error(EVR_ERR_ARG, "term %lld has %lld grid points (at most 2^27 - 1 per term)", t, nq);
     z->sum_nb += nb;
     z->sum_nq += nq;
     z->max_nb = std::max(z->max_nb, nb);
@@ -251,7 +253,8 @@ __device__ void point_coords(const int* nq_of_l, const double* xcat, const int* 
 __global__ void fields_kernel(const TermInfo* terms, long long nb_SG, const long long* pt_term_start,
                               const int* nq_of_l, const double* xcat, const int* x_off, int D, int Lp1,
                               int V_nterms, const double* V_coef, const int* V_fac, double* V,
-                              const double* G0, const double* G1, double* G, long long gp0, long long gp1) {
+                              const double* G0, const double* G1, double* G, long long gp0, long long gp1, int nb0,
+                              long long vstride) {
   for (long long gp = gp0 + blockIdx.x * (long long)blockDim.x + threadIdx.x; gp < gp1;
        gp += (long long)gridDim.x * blockDim.x) {
     // binary search of the term owning global point gp
@@ -265,18 +268,24 @@ __global__ void fields_kernel(const TermInfo* terms, long long nb_SG, const long
     double Q[EVR_MAXD];
     point_coords(nq_of_l, xcat, x_off, D, Lp1, T, q, Q);
     if (V) {
-      double v = 0.0;
-      for (int t = 0; t < V_nterms; ++t) {
-        double m = V_coef[t];
-        for (int f = 0; f < EVR_VFAC; ++f) {
-          const int code = V_fac[t * EVR_VFAC + f];
-          if (code < 0) break;
-          const double x = Q[code >> 8];
-          for (int k = 0; k < (code & 255); ++k) m *= x;
+      // with nb0 > 1 channels, element (a, b) of the electronic matrix has its
+      // own coefficients over the same monomials (get_d0MatOp_AT_Qact gives
+      // the nb0 x nb0 matrix at each point)
+      for (int ab = 0; ab < nb0 * nb0; ++ab) {
+        const double* cf = V_coef + (long long)ab * V_nterms;
+        double v = 0.0;
+        for (int t = 0; t < V_nterms; ++t) {
+          double m = cf[t];
+          for (int f = 0; f < EVR_VFAC; ++f) {
+            const int code = V_fac[t * EVR_VFAC + f];
+            if (code < 0) break;
+            const double x = Q[code >> 8];
+            for (int k = 0; k < (code & 255); ++k) m *= x;
+          }
+          v += m;
         }
-        v += m;
+        V[(long long)ab * vstride + gp - gp0] = v;
       }
-      V[gp - gp0] = v;
     }
     if (G) {
       const long long nqt = T.nq;
@@ -347,6 +356,8 @@ struct evr_sg4_ctx {
   DescSizes z;
   int device = 0, num_sms = 0;
   std::vector<int> nb_of_l, nq_of_l, mat_off, x_off;
+  std::vector<int> diag_off;            // [D*(L+1)*5] offsets of the diagonal pattern matrices
+  int* d_diag_off = nullptr;
   std::vector<TermInfo> terms;  // host copy (r filled per nrhs)
   // device
   int* d_map = nullptr;
@@ -442,7 +453,7 @@ static int nbuf_for(const evr_sg4_ctx* c) {
 }
 
 static void free_ctx(evr_sg4_ctx* c) {
-  void* ptrs[] = {c->d_map, c->d_mats, c->d_mat_off, c->d_nb_of_l, c->d_nq_of_l, c->d_x, c->d_x_off,
+  void* ptrs[] = {c->d_map, c->d_mats, c->d_mat_off, c->d_diag_off, c->d_nb_of_l, c->d_nq_of_l, c->d_x, c->d_x_off,
                   c->d_terms, c->d_items, c->d_plain_items, c->d_params, c->d_counter, c->d_inv_ptr,
                   c->d_inv_idx, c->d_contrib, c->d_chunk_q, c->d_fun_chunk, c->d_part,
                   c->d_scratch, c->d_V, c->d_G, c->d_Jac, c->d_cfac,
@@ -528,6 +539,42 @@ extern "C" int evr_sg4_create(const evr_sg4_desc* d, evr_sg4_ctx** out) {
     c->mat_off[k * 8 + 4 + M_D2] = (int)mats.size();
     for (int r = 0; r < nq; ++r)
       for (int s = 0; s < nq; ++s) mats.push_back(d->d2GG[o_gg + s + (size_t)nq * r]);
+    // the diagonal's pattern matrices, [nb][nq] row-major (see diag_kernel):
+    //   E = B o C^T, L1 = (B d1) o C^T, R1 = B o (d1 C)^T, LR = (B d1) o (d1 C)^T,
+    //   L2 = (B d2) o C^T,  with B = RBGwrho, C = RGB, o the elementwise product
+    {
+      auto B = [&](int b, int q) { return d->RBGwrho[o_gb + b + (size_t)nb * q]; };
+      auto C = [&](int q, int b) { return d->RGB[o_rgb + q + (size_t)nq * b]; };
+      auto d1 = [&](int r, int s2) { return d->d1GG[o_gg + r + (size_t)nq * s2]; };
+      auto d2 = [&](int r, int s2) { return d->d2GG[o_gg + r + (size_t)nq * s2]; };
+      std::vector<double> Bd1((size_t)nb * nq), Bd2((size_t)nb * nq), d1C((size_t)nq * nb);
+      for (int b = 0; b < nb; ++b)
+        for (int q = 0; q < nq; ++q) {
+          double a1 = 0.0, a2 = 0.0;
+          for (int r = 0; r < nq; ++r) {
+            a1 += B(b, r) * d1(r, q);
+            a2 += B(b, r) * d2(r, q);
+          }
+          Bd1[(size_t)b * nq + q] = a1;
+          Bd2[(size_t)b * nq + q] = a2;
+        }
+      for (int q = 0; q < nq; ++q)
+        for (int b = 0; b < nb; ++b) {
+          double a = 0.0;
+          for (int r = 0; r < nq; ++r) a += d1(q, r) * C(r, b);
+          d1C[(size_t)q * nb + b] = a;
+        }
+      if (c->diag_off.empty()) c->diag_off.resize((size_t)D * Lp1 * 5);
+      for (int pat = 0; pat < 5; ++pat) {
+        c->diag_off[(size_t)k * 5 + pat] = (int)mats.size();
+        for (int b = 0; b < nb; ++b)
+          for (int q = 0; q < nq; ++q) {
+            const double l = (pat == 1 || pat == 3) ? Bd1[(size_t)b * nq + q] : (pat == 4 ? Bd2[(size_t)b * nq + q] : B(b, q));
+            const double r = (pat == 2 || pat == 3) ? d1C[(size_t)q * nb + b] : C(q, b);
+            mats.push_back(l * r);
+          }
+      }
+    }
     o_rgb += (size_t)nq * nb;
     o_gb += (size_t)nq * nb;
     o_gg += (size_t)nq * nq;
@@ -582,6 +629,7 @@ extern "C" int evr_sg4_create(const evr_sg4_desc* d, evr_sg4_ctx** out) {
   if ((rc = upload(&c->d_map, d->map, (size_t)z.sum_nb)) ||
       (rc = upload(&c->d_mats, mats.data(), mats.size())) ||
       (rc = upload(&c->d_mat_off, c->mat_off.data(), c->mat_off.size())) ||
+      (rc = upload(&c->d_diag_off, c->diag_off.data(), c->diag_off.size())) ||
       (rc = upload(&c->d_nb_of_l, c->nb_of_l.data(), c->nb_of_l.size())) ||
       (rc = upload(&c->d_nq_of_l, c->nq_of_l.data(), c->nq_of_l.size())) ||
       (rc = upload(&c->d_x, d->x, o_x)) ||
@@ -619,7 +667,7 @@ static int eval_fields(evr_sg4_ctx* c, long long g0, long long g1, bool V, bool 
   fields_kernel<<<(unsigned)blocks, 256, 0, s>>>(c->d_terms, c->nb_SG, c->d_pt_start, c->d_nq_of_l, c->d_x,
                                                  c->d_x_off, c->D, c->L + 1, V ? c->V_nterms : 0, c->d_Vcoef,
                                                  c->d_Vfac, V ? c->d_V : nullptr, c->d_G0, c->d_G1,
-                                                 G ? c->d_G : nullptr, g0, g1);
+                                                 G ? c->d_G : nullptr, g0, g1, c->nb0, c->z.sum_nq);
   CUDA_TRY(cudaGetLastError());
   return EVR_OK;
 }
@@ -660,10 +708,6 @@ extern "C" int evr_sg4_set_operator(evr_sg4_ctx* c, const evr_sg4_op_desc* op) {
   c->type = op->type;
   c->items_nrhs = -1;  // work split depends on the operator's buffer count and the slices
   int rc;
-  if (c->nb0 > 1) {  // electronic matrices: V(:, a, b) given on the grid
-    if (op->V_nterms > 0 && !op->V_grid)
-      return set_error(EVR_ERR_ARG, "nb0=%d: pass V as V_grid[nb0*nb0*sum_nq]", c->nb0);
-  }
   const long long nvg = snq * c->nb0 * c->nb0;  // V_grid entries
   const bool polyV = !op->V_grid && op->V_nterms > 0;
   const bool affG = op->type == 10 && !op->G_grid && (op->G0 || op->G1);
@@ -686,6 +730,8 @@ extern "C" int evr_sg4_set_operator(evr_sg4_ctx* c, const evr_sg4_op_desc* op) {
   const bool grids = op->V_grid || (op->type == 10 && (op->G_grid || op->Jac_grid || op->sqRho_grid));
   const double bpp = 8.0 * (polyV ? 1 : 0) + 8.0 * D * D * (affG ? 1 : 0);  // bytes per grid point
   const bool stream = c->field_budget > 0 && !grids && (polyV || affG) && bpp * (double)snq > (double)c->field_budget;
+  if (stream && c->nb0 > 1)
+    return set_error(EVR_ERR_ARG, "field budget: streamed fields take one channel (nb0 = %d)", c->nb0);
   long long slice_pts = snq;
   if (stream) {
     const long long cap = (long long)((double)c->field_budget / bpp);
@@ -711,7 +757,7 @@ extern "C" int evr_sg4_set_operator(evr_sg4_ctx* c, const evr_sg4_op_desc* op) {
       if (!std::isfinite(op->V_grid[k])) return set_error(EVR_ERR_NUMERIC, "V_grid[%lld] is not finite", k);
     if ((rc = upload(&c->d_V, op->V_grid, (size_t)nvg))) return rc;
   }
-  if (polyV) CUDA_TRY(cudaMalloc(&c->d_V, (size_t)slice_pts * 8));
+  if (polyV) CUDA_TRY(cudaMalloc(&c->d_V, (size_t)slice_pts * 8 * c->nb0 * c->nb0));
   if (op->type == 10) {
     if (op->G_grid) {
       if ((rc = upload(&c->d_G, op->G_grid, (size_t)snq * D * D))) return rc;
@@ -752,7 +798,7 @@ extern "C" int evr_sg4_set_operator(evr_sg4_ctx* c, const evr_sg4_op_desc* op) {
     for (long long t = 0; t < c->nb_SG; ++t) start[t] = c->terms[t].off_nq;
     CUDA_TRY(cudaMemcpy(c->d_terms, c->terms.data(), c->terms.size() * sizeof(TermInfo), cudaMemcpyHostToDevice));
     if ((rc = upload(&c->d_pt_start, start.data(), start.size()))) return rc;
-    if (polyV && ((rc = upload(&c->d_Vcoef, op->V_coef, (size_t)op->V_nterms)) ||
+    if (polyV && ((rc = upload(&c->d_Vcoef, op->V_coef, (size_t)op->V_nterms * c->nb0 * c->nb0)) ||
                   (rc = upload(&c->d_Vfac, vfac.data(), vfac.size()))))
       return rc;
     c->V_nterms = polyV ? op->V_nterms : 0;
@@ -1821,6 +1867,190 @@ evr::FieldPairView evr::field_pair_view(const FieldPair* f) {
   return v;
 }
 
+
+
+// ------------------------------------------------------------------------
+// diag(H) term by term.  The term operator is B A C (C = RGB basis->grid,
+// B = RBGwrho grid->basis, Kronecker products over the modes), and
+// A = V + sum of terms f(q) D_i D_j with D_i a 1-D matrix on mode i, so its
+// diagonal element at DP index k is
+//   sum_q f(q) prod_l P_l[k_l][q_l],  P_l = (B_l M1_l) o (M2_l C_l)^T,
+// M1_l = the outer 1-D matrix on mode l (d1GG or d2GG, else I), M2_l the
+// inner one: a grid->basis transform of the field f with the "pattern"
+// matrices P_l in place of RBGwrho.  Per term: one transform per pattern
+// (V; D^2 G_ij terms for type 10, -1/2 each; F2/F1 terms for type 1), the
+// weighted result into the contribution buffer, then the ordered
+// accumulation of evr_sg4_hpsi.  A few H.psi-equivalents of work instead of
+// N/64 H.psi calls on blocks of unit vectors.  Type 10 with Jac or rho (the
+// -1/2/(Jac s) factor does not factor per mode), several channels and
+// streamed fields keep the unit-vector method.
+// ------------------------------------------------------------------------
+namespace evr {
+
+struct DiagPat {
+  int field;   // 0: V, 1: ones, 2: G(i, j)
+  int i, j;    // modes with an outer / inner 1-D matrix (-1: none)
+  int pi, pj;  // their pattern sets (1 L1, 2 R1, 3 LR, 4 L2); 0 = E elsewhere
+  double coef;
+};
+
+__global__ void __launch_bounds__(128) diag_kernel(KParams p, const int* __restrict__ diag_off,
+                                                   const DiagPat* __restrict__ pats, int npat,
+                                                   const int* __restrict__ order, int nterms, unsigned int* counter) {
+  extern __shared__ double smem[];
+  __shared__ ItemShared it;
+  __shared__ int next;
+  for (;;) {
+    if (threadIdx.x == 0) next = (int)atomicAdd(counter, 1u);
+    __syncthreads();
+    const int idx = next;
+    __syncthreads();
+    if (idx >= nterms) break;
+    const int term = order[idx];
+    if (threadIdx.x == 0) {
+      const TermInfo& T = p.terms[term];
+      it.term = term;
+      it.rhs0 = 0;
+      it.r = 1;
+      it.off_nb = T.off_nb;
+      it.off_nq = T.off_nq;
+      it.nb_t = T.nb;
+      it.nq_t = T.nq;
+      it.w = T.w;
+      const long long need = 3LL * T.nq;
+      it.base = (need <= p.smem_doubles) ? smem : p.gscratch + (long long)blockIdx.x * p.scratch_per_cta;
+    }
+    if (threadIdx.x < p.D) {
+      const int i = threadIdx.x;
+      const int k = i * p.Lp1 + p.terms[term].l[i];
+      it.nb[i] = p.nb_of_l[k];
+      it.nq[i] = p.nq_of_l[k];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {  // the mode order of the grid->basis passes, as run_item
+      for (int i = 0; i < p.D; ++i) {
+        int j = i;
+        const int ni = it.nq[i] - it.nb[i], di = it.nb[i] * it.nq[i];
+        while (j > 0) {
+          const int o = it.ord[j - 1];
+          if ((it.nq[o] - it.nb[o]) * di <= ni * (it.nb[o] * it.nq[o])) break;
+          it.ord[j] = o;
+          --j;
+        }
+        it.ord[j] = i;
+      }
+      for (int k = 0; k < p.D; ++k) it.pos[it.ord[k]] = k;
+    }
+    __syncthreads();
+    const int nqt = it.nq_t, nbt = it.nb_t;
+    double* A = it.base;
+    double* Bf = A + nqt;
+    double* acc = A + 2 * nqt;
+    for (int e = threadIdx.x; e < nbt; e += blockDim.x) acc[e] = 0.0;
+    const long long oq = it.off_nq;
+    const long long GD = (long long)p.D * p.D;
+    for (int t = 0; t < npat; ++t) {
+      const DiagPat pt = pats[t];
+      for (int q = threadIdx.x; q < nqt; q += blockDim.x) {
+        double f = 1.0;
+        if (pt.field == 0) f = p.V[oq + q];
+        else if (pt.field == 2) f = p.G[oq * GD + (long long)nqt * (p.D * pt.i + pt.j) + q];
+        A[q] = f;
+      }
+      if (threadIdx.x < p.D) {
+        const int l = threadIdx.x;
+        const int set = (l == pt.i) ? pt.pi : ((l == pt.j) ? pt.pj : 0);
+        it.mo[l][M_GB] = diag_off[(l * p.Lp1 + p.terms[term].l[l]) * 5 + set];
+      }
+      __syncthreads();
+      const double* yb = transform(p, it, false, A, Bf);
+      for (int e = threadIdx.x; e < nbt; e += blockDim.x) acc[e] = fma(pt.coef, yb[e], acc[e]);
+      __syncthreads();
+    }
+    store_contrib(p, it, acc);
+  }
+}
+
+}  // namespace evr
+
+extern "C" int evr_sg4_diagonal(evr_sg4_ctx* c, double* diag, void* stream) {
+  if (!c || !diag) return set_error(EVR_ERR_ARG, "diagonal: NULL argument");
+  if (!c->have_op) return set_error(EVR_ERR_STATE, "diagonal: set_operator was not called");
+  if (c->nb0 > 1 || c->streamed || c->d_Jac || c->d_sqRho)
+    return evr_sg4_diagonal_by_apply(c, diag, stream);
+  cudaStream_t s = (cudaStream_t)stream;
+  const int D = c->D;
+  std::vector<DiagPat> pats;
+  if (c->d_V) pats.push_back(DiagPat{0, -1, -1, 0, 0, 1.0});
+  if (c->type == 1) {
+    for (int i = 0; i < D; ++i)
+      if (c->F2[i * D + i] != 0.0) pats.push_back(DiagPat{1, i, -1, 4, 0, c->F2[i * D + i]});
+    for (int i = 0; i < D; ++i)
+      for (int j = i + 1; j < D; ++j)
+        if (c->F2[i * D + j] != 0.0) pats.push_back(DiagPat{1, i, j, 1, 1, c->F2[i * D + j]});
+    for (int i = 0; i < D; ++i)
+      if (c->F1[i] != 0.0) pats.push_back(DiagPat{1, i, -1, 1, 0, c->F1[i]});
+  } else if (c->type == 10) {
+    for (int i = 0; i < D; ++i)
+      for (int j = 0; j < D; ++j) {
+        if (!c->d_G && i != j) continue;
+        pats.push_back(DiagPat{c->d_G ? 2 : 1, i, j, i == j ? 3 : 1, 2, -0.5});
+      }
+  }
+  if (pats.empty()) {  // the zero operator
+    CUDA_TRY(cudaMemsetAsync(diag, 0, (size_t)c->N * 8, s));
+    return EVR_OK;
+  }
+  // terms by decreasing grid size (the persistent CTAs then end balanced)
+  std::vector<int> order(c->nb_SG);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return c->terms[a].nq > c->terms[b].nq; });
+  const int smem_doubles = 6144;    // 48 KB of dynamic shared memory per CTA
+  const int grid = 4 * c->num_sms;  // four resident per SM (registers)
+  const long long per_cta = 3LL * c->z.max_nq > smem_doubles ? 3LL * c->z.max_nq : 0;
+  std::vector<TermInfo> terms = c->terms;
+  for (TermInfo& T : terms) T.r = 1;
+  double *d_contrib = nullptr, *d_part = nullptr, *d_scratch = nullptr;
+  DiagPat* d_pats = nullptr;
+  int* d_order = nullptr;
+  TermInfo* d_terms = nullptr;
+  unsigned int* d_counter = nullptr;
+  auto cleanup = [&]() {
+    void* ptrs[] = {d_contrib, d_part, d_scratch, d_pats, d_order, d_terms, d_counter};
+    for (void* q : ptrs)
+      if (q) cudaFree(q);
+  };
+  if (cudaMalloc(&d_contrib, (size_t)c->z.sum_nb * 8) != cudaSuccess ||
+      cudaMalloc(&d_part, (size_t)c->n_chunks * 16) != cudaSuccess ||
+      (per_cta && cudaMalloc(&d_scratch, (size_t)per_cta * grid * 8) != cudaSuccess) ||
+      cudaMalloc(&d_pats, pats.size() * sizeof(DiagPat)) != cudaSuccess ||
+      cudaMalloc(&d_order, order.size() * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&d_terms, terms.size() * sizeof(TermInfo)) != cudaSuccess ||
+      cudaMalloc(&d_counter, sizeof(unsigned int)) != cudaSuccess) {
+    cudaGetLastError();
+    cleanup();
+    return set_error(EVR_ERR_ALLOC, "diagonal: device allocation failed");
+  }
+  cudaMemcpyAsync(d_pats, pats.data(), pats.size() * sizeof(DiagPat), cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(d_order, order.data(), order.size() * sizeof(int), cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(d_terms, terms.data(), terms.size() * sizeof(TermInfo), cudaMemcpyHostToDevice, s);
+  cudaMemsetAsync(d_counter, 0, sizeof(unsigned int), s);
+  KParams p = make_params(c, 1, 0, diag, c->N, diag, c->N, 1.0);
+  p.terms = d_terms;
+  p.smem_doubles = smem_doubles;
+  p.gscratch = d_scratch;
+  p.scratch_per_cta = per_cta;
+  p.contrib = d_contrib;
+  p.split = 0;
+  diag_kernel<<<grid, 128, (size_t)smem_doubles * 8, s>>>(p, c->d_diag_off, d_pats, (int)pats.size(), d_order,
+                                                          (int)c->nb_SG, d_counter);
+  cudaError_t e = cudaGetLastError();
+  int rc = e == cudaSuccess ? launch_reduce(c, d_contrib, (double2*)d_part, 1, 0, diag, c->N, diag, c->N, 0.0, 1.0, s)
+                            : set_error(EVR_ERR_CUDA, "diagonal: %s", cudaGetErrorString(e));
+  if (!rc && cudaStreamSynchronize(s) != cudaSuccess) rc = set_error(EVR_ERR_CUDA, "diagonal: kernel failed");
+  cleanup();
+  return rc;
+}
 
 // ------------------------------------------------------------------------
 // Plan knobs and the autotuner (the counterpart of Tune_SG4threads_HPsi,

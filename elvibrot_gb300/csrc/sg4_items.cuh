@@ -48,6 +48,9 @@ namespace evr {
 #ifndef EVR_NARROW_INC
 #define EVR_NARROW_INC 0  // the narrow kernel takes the point digits from divisions
 #endif
+#ifndef EVR_FASTDIV
+#define EVR_FASTDIV 1     // those divisions by multiply-high with per-item magic numbers
+#endif
 
 struct TermInfo {
   long long off_nb;   // into map
@@ -150,6 +153,8 @@ struct ItemShared {
   int pos[EVR_MAXD];          // rank of each mode in that order (inverse of ord)
   int st[EVR_MAXD];           // grid stride of each mode (product of the nq before it)
   int mo[EVR_MAXD][4];
+  unsigned mg[EVR_MAXD];      // ceil(2^32 / nq[i]) (0 for nq = 1): rem / nq[i] = umulhi(rem, mg) for rem < 2^28
+  unsigned long long mgt;     // ceil(2^64 / nq_t) (0 for nq_t = 1): e / nq_t = umul64hi(e, mgt)
   long long off_nb, off_nq;
   int nb_t, nq_t, r, rhs0, term;
   double w;
@@ -422,6 +427,21 @@ __device__ __forceinline__ void point_digits(GridPos<DD>& gp, const MS& ms, int 
 #pragma unroll
     for (int i = 0; i < DD; ++i) idx[i] = gp.dig[i];
   } else {
+#if EVR_FASTDIV
+    // exact quotients by multiply-high: nq_t < 2^27 (checked at context
+    // creation), so e < 2^32 and every digit quotient has rem < 2^28
+    const unsigned long long mt = ms.mgt();
+    const int j = mt ? (int)__umul64hi((unsigned long long)e, mt) : e;
+    q = e - j * nqt;
+    unsigned rem = (unsigned)q;
+#pragma unroll
+    for (int i = 0; i < DD; ++i) {
+      const unsigned n = (unsigned)ms.nq(i), m = ms.mg(i);
+      const unsigned quo = m ? __umulhi(rem, m) : rem;
+      idx[i] = (int)(rem - quo * n);
+      rem = quo;
+    }
+#else
     q = e % nqt;
     int rem = q;
 #pragma unroll
@@ -430,6 +450,7 @@ __device__ __forceinline__ void point_digits(GridPos<DD>& gp, const MS& ms, int 
       idx[i] = rem % n;
       rem /= n;
     }
+#endif
   }
 }
 
@@ -463,6 +484,8 @@ struct ModeSizes<DD, false> {
   __device__ __forceinline__ ModeSizes(const KParams& p, const ItemShared& s) : it(s), mats(p.mats) {}
   __device__ __forceinline__ int nq(int i) const { return it.nq[i]; }
   __device__ __forceinline__ int st(int i) const { return it.st[i]; }
+  __device__ __forceinline__ unsigned mg(int i) const { return it.mg[i]; }
+  __device__ __forceinline__ unsigned long long mgt() const { return it.mgt; }
   __device__ __forceinline__ const double* Md(int i) const { return mats + it.mo[i][M_D1]; }
 };
 
@@ -674,6 +697,7 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ter
     it.w = T.w;
     long long need = (long long)p.nbuf * T.nq * it.r;
     it.base = (need <= p.smem_doubles) ? smem : p.gscratch + (long long)blockIdx.x * p.scratch_per_cta;
+    it.mgt = T.nq > 1 ? 0xFFFFFFFFFFFFFFFFull / (unsigned long long)T.nq + 1ull : 0ull;
   }
   if (threadIdx.x < p.D) {
     const int i = threadIdx.x;
@@ -681,6 +705,7 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ter
     const int k = i * p.Lp1 + l;
     it.nb[i] = p.nb_of_l[k];
     it.nq[i] = p.nq_of_l[k];
+    it.mg[i] = it.nq[i] > 1 ? 0xFFFFFFFFu / (unsigned)it.nq[i] + 1u : 0u;
     for (int q = 0; q < 4; ++q) it.mo[i][q] = p.mat_off[k * 8 + 4 * p.transpose + q];
   }
   __syncthreads();

@@ -158,7 +158,7 @@ static int apply_hs(evr_sg4_ctx* c, long long N, int nb, const double* X, double
 
 using namespace evr;
 
-extern "C" int evr_sg4_diagonal(evr_sg4_ctx* c, double* diag, void* stream) {
+extern "C" int evr_sg4_diagonal_by_apply(evr_sg4_ctx* c, double* diag, void* stream) {
   if (!c || !diag) return set_error(EVR_ERR_ARG, "diagonal: NULL argument");
   long long sz[8];
   evr_sg4_ctx_sizes(c, sz);

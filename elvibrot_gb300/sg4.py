@@ -130,6 +130,7 @@ def _declare(L):
         "evr_sg4_cheby_propagate": [vp, ctypes.POINTER(ChebyOpts), ctypes.c_int, vp, vp, dp,
                                     ctypes.POINTER(ctypes.c_int), vp],
         "evr_sg4_diagonal": [vp, vp, vp],
+        "evr_sg4_diagonal_by_apply": [vp, vp, vp],
         "evr_sg4_set_field_budget": [vp, ll],
         "evr_sg4_field_slices": [vp, ctypes.POINTER(ll)],
         "evr_sg4_tune": [vp, ctypes.c_int, ctypes.c_int, ip, dp],
@@ -310,9 +311,13 @@ class ParamOp:
         coef = expo = None
         nterms = 0
         if V_poly is not None and V is None:
+            # one channel: coef (nterms,); nb0 channels: coef (nb0*nb0, nterms), element (a, b) in row a*nb0 + b
             coef = np.ascontiguousarray(V_poly.coef, dtype=np.float64)
             expo = np.ascontiguousarray(V_poly.expo, dtype=np.int32).reshape(-1, D)
-            nterms = len(coef)
+            nterms = expo.shape[0]
+            if coef.size != nterms * self.basis.nb0 ** 2:
+                raise EVRError(1, f"V_poly: {coef.size} coefficients for {nterms} terms and nb0={self.basis.nb0}")
+            coef = coef.ravel()
         op = OpDesc(self.type_op, _dp(keep["V"]), nterms, _dp(coef), _ip(expo), _dp(keep["G"]),
                     _dp(keep["G0"]), _dp(keep["G1"]), _dp(keep["Jac"]), _dp(keep["sqRho"]),
                     _dp(keep["F2"]), _dp(keep["F1"]))
@@ -399,11 +404,13 @@ class ParamOp:
             check(lib().evr_sg4_hpsi(self._h, nrhs, P.data_ptr(), N, O.data_ptr(), N, E0, Esc, stream))
         return out
 
-    def diagonal(self):
-        """Exact diag(H) as a CUDA tensor (the Davidson preconditioner)."""
+    def diagonal(self, by_apply: bool = False):
+        """Exact diag(H) as a CUDA tensor (the Davidson preconditioner): term by
+        term (evr_sg4_diagonal), or from H on blocks of unit vectors (by_apply)."""
         import torch
         d = torch.empty(self.basis.nvec, dtype=torch.float64, device="cuda")
-        check(lib().evr_sg4_diagonal(self._h, d.data_ptr(), 0))
+        fn = lib().evr_sg4_diagonal_by_apply if by_apply else lib().evr_sg4_diagonal
+        check(fn(self._h, d.data_ptr(), 0))
         return d
 
     def davidson(self, nev: int, block: int = 0, max_subspace: int = 0, max_it: int = 500,

@@ -121,7 +121,11 @@ int evr_sg4_destroy(evr_sg4_ctx* c);
  * polynomial sum_t coef_t prod_i Q_i^expo_ti evaluated on the device.  With
  * nb0 > 1 channels V is the electronic matrix on the grid:
  * V_grid[(a*nb0 + b)*sum_nq + point] couples channel b into channel a
- * (OpGrid(iterm)%Grid(:,a,b)), and the derivative terms act on every channel.
+ * (OpGrid(iterm)%Grid(:,a,b)), and the derivative terms act on every channel;
+ * as a polynomial, V_coef holds nb0*nb0 blocks of V_nterms coefficients over
+ * the same monomials (element (a, b) at V_coef[(a*nb0 + b)*V_nterms + t]),
+ * the matrix the reference's get_d0MatOp_AT_Qact gives at each point
+ * (SRC/sub_Operator/sub_PrimOp.f90:257); such fields stay resident.
  * G (type 10) is a grid GGiq(iq,j,i) per term, concatenated (sum_nq*D*D),
  * or the affine form G_ij(Q) = G0_ij + sum_k G1_ijk Q_k ([D*D], [D*D*D],
  * row-major ijk); neither = identity.  Jac / sqRho grids: NULL = 1.
@@ -303,9 +307,18 @@ int evr_sg4_davidson(evr_sg4_ctx* c, const evr_davidson_opts* o, const double* g
                      const double* diag, double* evals, double* evecs, double* resid, int* iterations,
                      void* stream);
 
-/* Exact diagonal of H on the device (diag: device N), from H applied to
- * blocks of unit vectors; the Davidson preconditioner. */
+/* Exact diagonal of H on the device (diag: device N), the Davidson
+ * preconditioner (the reference's correction uses the H diagonal,
+ * sub_NewVec_Davidson, sub_module_Davidson.f90:1306).  Computed term by
+ * term: each Smolyak term's diagonal is a grid->basis transform of its
+ * fields with per-mode matrices (RBGwrho.D o (D.RGB)^T), one transform per
+ * field term, then the weighted, term-ordered accumulation of H.psi.  Type 10
+ * with Jac or rho grids, several channels and streamed fields use
+ * evr_sg4_diagonal_by_apply. */
 int evr_sg4_diagonal(evr_sg4_ctx* c, double* diag, void* stream);
+/* The same diagonal from H applied to blocks of 64 unit vectors (N/64 H.psi
+ * calls): valid for every operator, and the check of the term-wise form. */
+int evr_sg4_diagonal_by_apply(evr_sg4_ctx* c, double* diag, void* stream);
 
 /* Chebyshev propagation of complex wave packets (march_cheby,
  * SRC/sub_propagation/sub_module_propa_march.f90:4145-4437; coefficients

@@ -167,10 +167,34 @@ def test_channels_type10_matches_oracle_blocks():
             assert err <= 1e-12
 
 
-def test_channels_reject_polynomial_v():
+def test_channels_polynomial_v_matches_grid_v():
+    """The nb0 x nb0 electronic matrix given as polynomials (one coefficient
+    block per element over shared monomials, evaluated on the device) gives
+    the operator of the same matrix given as grids, for types 1 and 10; the
+    grid form is itself checked against the oracle's channel blocks above."""
     need_cuda()
     from elvibrot_gb300 import Polynomial
-    basis = SG4Basis(3, 3, 3, 1, 1, 2, 1, nb0=2)
-    with pytest.raises(EVRError):
-        ParamOp(basis, 1, V_poly=Polynomial(np.array([1.0]), np.zeros((1, 3), dtype=np.int32)),
-                F2=-0.5 * np.eye(3))
+    D, L, nb0 = 3, 5, 3
+    basis = SG4Basis(D, L, L, 1, 1, 2, 1, nb0=nb0)
+    Q = basis.grid_points()
+    rng = np.random.default_rng(71)
+    expo = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1], [2, 0, 0], [0, 2, 0], [0, 0, 2], [1, 1, 1]],
+                     dtype=np.int32)
+    coef = rng.normal(0.0, 0.05, size=(nb0 * nb0, len(expo)))
+    for a in range(nb0):
+        coef[a * nb0 + a, 4:7] += 0.5                              # harmonic diagonal elements
+    Vg = np.stack([Polynomial(coef[k], expo)(Q) for k in range(nb0 * nb0)])
+    G1 = 0.02 * rng.normal(size=(D, D, D))
+    G1 = 0.5 * (G1 + G1.transpose(1, 0, 2))
+    for type_op in (1, 10):
+        kw = dict(F2=-0.5 * np.eye(D)) if type_op == 1 else dict(G0=np.eye(D), G1=G1)
+        a_op = ParamOp(basis, type_op, V_poly=Polynomial(coef, expo), **kw)
+        b_op = ParamOp(basis, type_op, V=Vg.reshape(nb0 * nb0, -1), **kw)
+        for cplx, tr in ((False, False), (True, True)):
+            Ha = gpu_dense(a_op, basis.nvec, cplx, tr)
+            Hb = gpu_dense(b_op, basis.nvec, cplx, tr)
+            err = np.max(np.abs(Ha - Hb)) / np.max(np.abs(Hb))
+            print(f"type {type_op}, nb0={nb0}, cplx={cplx}, transpose={tr}: polynomial vs grid V {err:.2e}")
+            assert err <= 1e-13
+    with pytest.raises(EVRError):                                  # wrong number of coefficients
+        ParamOp(basis, 1, V_poly=Polynomial(coef[0], expo), F2=-0.5 * np.eye(D))
