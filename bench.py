@@ -332,6 +332,47 @@ def bench_uneven(seconds_cap=90.0):
     return res
 
 
+def bench_config0(reps=200):
+    """The 3-D L=6 type-1 workload (one real vector): batched and per-term GPU
+    H.psi, the CPU restatement on all host threads, the largest relative
+    difference from it, and Davidson for the lowest 10 levels."""
+    import torch
+    from elvibrot_gb300.configs import config, random_psi
+    cfg = config(0)
+    m = cfg["model"]
+    op = m.operator()
+    N = op.basis.N
+    psi = random_psi(N, 1, cfg["seed"])
+    P = torch.from_numpy(np.ascontiguousarray(psi.T)).cuda()
+    H = torch.empty_like(P)
+    res = {"workload": "3-D SG4 L=6 type 1 (constant G), 1 real vector", "N": N, "nb_SG": op.basis.nb_SG}
+    for plain in (False, True):
+        op.hpsi_dev(P, H, plain=plain)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            op.hpsi_dev(P, H, plain=plain)
+        b.record()
+        torch.cuda.synchronize()
+        res["plain_hpsi_per_s" if plain else "batched_hpsi_per_s"] = reps / (a.elapsed_time(b) / 1e3)
+    op.hpsi_dev(P, H)
+    got = H.cpu().numpy().T
+    O, kw = build_oracle_inputs(m)
+    ref = O.hpsi(psi, **kw)
+    res["max_rel_err_vs_cpu"] = float(np.max(np.abs(got - ref)) / np.max(np.abs(ref)))
+    v, steps, dt, threads = time_oracle(m, 1, min_seconds=0.5, min_steps=3, max_steps=2000, seed=cfg["seed"])
+    res.update({"cpu_hpsi_per_s": v, "cpu_threads": threads})
+    ev, vec, rs, its = op.davidson(10, conv_resi=1e-9, max_it=300)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ev, vec, rs, its = op.davidson(10, conv_resi=1e-9, max_it=300)
+    torch.cuda.synchronize()
+    res.update({"davidson_10_levels_s": time.perf_counter() - t0, "davidson_iterations": its,
+                "lowest_levels_hartree": [float(x) for x in ev[:3]]})
+    return res
+
+
 def bench_cheby_graph(nsteps=200):
     """Fixed-order Chebyshev (order 30, dt = 10 a.u.) of one complex packet on the
     4-D L=7 type-1 system: every step eagerly launched vs replayed from a CUDA
@@ -586,6 +627,8 @@ def run_ours(args, ws, rank, local):
     extras = {}
     if not args.no_extras:
         want = set(args.extras.split(","))
+        if "config0" in want:
+            extras["config0"] = bench_config0()
         if "davidson" in want:
             extras["davidson"] = bench_davidson(op)
         if "oc" in want:
@@ -688,8 +731,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-extras", action="store_true", help="skip the timings of the callers")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner's plan")
-    ap.add_argument("--extras", default="davidson,oc,uneven,graph,stream12",
-                    help="callers to time: davidson, oc (optimal-control gradient), uneven (64-instance batching), "
+    ap.add_argument("--extras", default="config0,davidson,oc,uneven,graph,stream12",
+                    help="callers to time: config0 (the 3-D L=6 workload), davidson, oc (optimal-control gradient), "
+                         "uneven (64-instance batching), "
                          "graph (Chebyshev steps replayed from a CUDA graph), stream12 (12-D type 10, streamed fields); "
                          "also on request: stream12_L10 (the 12-D workload at L=10, minutes)")
     args = ap.parse_args()

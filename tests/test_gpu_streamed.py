@@ -52,8 +52,13 @@ def test_streamed_fields_are_bit_identical_to_resident(D, L, type_op, parts):
         st.hpsi_dev(P, b, E0=0.1, Esc=2.0, transpose=transpose)
         torch.cuda.synchronize()
         assert torch.equal(a, b), f"cplx={cplx} transpose={transpose}: {(a - b).abs().max().item():.3e}"
-    # the diagonal (and so Davidson) runs on the streamed operator unchanged
-    assert torch.equal(res.diagonal(), st.diagonal())
+    # the diagonal (and so Davidson) runs on the streamed operator: from H on
+    # unit vectors, the same bits as on the resident operator, and within
+    # rounding of the resident operator's term-wise diagonal
+    d_st = st.diagonal()
+    assert torch.equal(res.diagonal(by_apply=True), d_st)
+    d_res = res.diagonal()
+    assert float((d_res - d_st).abs().max() / d_st.abs().max()) <= 1e-12
 
 
 def test_streamed_12d_matches_oracle():
