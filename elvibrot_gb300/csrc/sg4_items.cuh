@@ -51,9 +51,6 @@ namespace evr {
 #ifndef EVR_FASTDIV
 #define EVR_FASTDIV 1     // those divisions by multiply-high with per-item magic numbers
 #endif
-#ifndef EVR_FASTDIV_PASS
-#define EVR_FASTDIV_PASS 1  // the mode passes' fibre and output indices likewise (a magic number per pass)
-#endif
 
 struct TermInfo {
   long long off_nb;   // into map
@@ -228,30 +225,12 @@ static __device__ __noinline__ void channels_prologue(const KParams& p, long lon
 // matrix loads are warp-uniform, and four outputs are formed at once as
 // independent FMA chains (GB300's FP64 pipe has a long latency, one chain per
 // warp cannot keep it busy).  MODE 0 stores, 1 adds, 2 adds scale times.
-// Quotients of the fibre and output indices: by multiply-high with a magic
-// number computed once per pass (one division per thread and pass instead of
-// one per fibre or output), exact when n * (m d - 2^32) < 2^32, i.e. for
-// dividend and divisor below 2^16 (fibre index / S) or 2^14 x 16 (output index
-// / nf); larger passes divide.  Exact either way, so the bits do not change.
-struct PassDiv {
-  unsigned m;  // ceil(2^32 / d), or 0: divide
-  int d;
-  __device__ __forceinline__ PassDiv(int dd, bool exact) : m(0u), d(dd) {
-    if (EVR_FASTDIV_PASS && exact && dd > 1) m = 0xFFFFFFFFu / (unsigned)dd + 1u;
-  }
-  __device__ __forceinline__ int div(int n) const {
-    if (EVR_FASTDIV_PASS && m) return (int)__umulhi((unsigned)n, m);
-    return d == 1 ? n : n / d;
-  }
-};
-
 template <int NIN, int MODE>
 __device__ __forceinline__ void mode_pass_t(const double* __restrict__ M, int nout, int S, int R,
                                             const double* in, double* out, double scale) {
   const int nf = S * R;
-  const PassDiv dS(S, nf < 65536);
   for (int f = threadIdx.x; f < nf; f += blockDim.x) {
-    const int b = dS.div(f), a = f - b * S;
+    const int b = f / S, a = f - b * S;
     const double* fi = in + a + S * NIN * b;
     double v[NIN];
 #pragma unroll
@@ -301,10 +280,9 @@ template <int NIN, int MODE>
 __device__ __forceinline__ void mode_pass_split(const double* __restrict__ M, int nout, int S, int R,
                                                 const double* in, double* out, double scale) {
   const int nf = S * R;
-  const PassDiv dF(nf, nf < 16384), dS(S, nf < 65536);
   for (int u = threadIdx.x; u < nf * nout; u += blockDim.x) {
-    const int k = dF.div(u), f = u - k * nf;
-    const int b = dS.div(f), a = f - b * S;
+    const int k = u / nf, f = u - k * nf;
+    const int b = f / S, a = f - b * S;
     const double* fi = in + a + S * NIN * b;
     const double* Mk = M + k * NIN;
     double s0 = 0.0;

@@ -247,7 +247,9 @@ int evr_sg4_get_plan(const evr_sg4_ctx* c, int* geo, int* rmax, int* split);
  * or 0) with the automatic plan and with every candidate (geometry x rmax in
  * {4, 8, 16, 32} x split mode; best of three, each after a 256 MB write that
  * clears L2, after one untimed call), and applies the fastest -- a candidate
- * replaces the best so far only when more than 1 % faster.  With cache_path (a JSON file, created
+ * replaces the best so far only when more than 1 % faster, and the winner is
+ * then timed again against the automatic plan, alternately, five times each:
+ * it is kept only if its median is more than 1 % faster.  With cache_path (a JSON file, created
  * if absent) the winner is recorded under a key of the workload's shape (D,
  * L, LB, type, channels, N, nrhs, complex, G given), and a later call with
  * the same shape applies the recorded plan without timing (from_cache = 1).
