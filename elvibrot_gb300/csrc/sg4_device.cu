@@ -1429,6 +1429,7 @@ struct evr_sg4_multi {
   std::vector<double*> d_part;
   double* d_scratch = nullptr;   // global-scratch slabs, shared by the groups (launched in turn)
   KParams* d_params = nullptr;
+  KParams* d_pslot[2] = {nullptr, nullptr};  // parameter blocks bound to fixed vectors (multi_bind)
   long long last_launches = 0;
 };
 
@@ -1449,7 +1450,7 @@ static void free_multi(evr_sg4_multi* m) {
     void* gp[] = {g.d_items, g.d_sub, g.d_counter};
     for (void* q : gp) if (q) cudaFree(q);
   }
-  void* ptrs[] = {m->d_scratch, m->d_params};
+  void* ptrs[] = {m->d_scratch, m->d_params, m->d_pslot[0], m->d_pslot[1]};
   for (void* q : ptrs) if (q) cudaFree(q);
   delete m;
 }
@@ -1650,6 +1651,53 @@ extern "C" int evr_sg4_multi_hpsi(evr_sg4_multi* m, const double* const* psi, co
   }
   // `params` is pageable: the copy above is staged before cudaMemcpyAsync returns
   m->last_launches = launched + 2LL * active;
+  return EVR_OK;
+}
+
+// Parameter blocks of every context bound to fixed vectors (psi[k] -> hpsi[k],
+// ld = nb0*N, in slot 0 or 1), uploaded once: multi_launch_bound then enqueues
+// kernels and memsets only, so a caller can record it in a CUDA graph.  The
+// same parameters, items and kernels as evr_sg4_multi_hpsi with every
+// context active, so the same bits.
+int evr::multi_bind(evr_sg4_multi* m, int slot, const double* const* psi, double* const* hpsi) {
+  if (!m || slot < 0 || slot > 1 || !psi || !hpsi) return set_error(EVR_ERR_ARG, "multi_bind: bad arguments");
+  std::vector<KParams> params(m->n);
+  for (int k = 0; k < m->n; ++k) {
+    evr_sg4_ctx* c = m->ctxs[k];
+    if (!psi[k] || !hpsi[k]) return set_error(EVR_ERR_ARG, "multi_bind: NULL vector of context %d", k);
+    KParams& p = params[k];
+    p = make_params(c, m->nrhs_v[k], m->cshift, psi[k], c->nvec << m->cshift, hpsi[k], c->nvec << m->cshift, 1.0);
+    const MGroup& g = m->groups[m->group[k]];
+    p.transpose = m->transpose;
+    p.smem_doubles = g.smem_doubles;
+    p.terms = m->d_terms[k];
+    p.contrib = m->d_contrib[k];
+    p.gscratch = m->d_scratch;
+    p.scratch_per_cta = g.scratch_per_cta;
+    p.counter = nullptr;
+    p.items = nullptr;
+  }
+  if (!m->d_pslot[slot]) CUDA_TRY(cudaMalloc(&m->d_pslot[slot], (size_t)m->n * sizeof(KParams)));
+  CUDA_TRY(cudaMemcpy(m->d_pslot[slot], params.data(), (size_t)m->n * sizeof(KParams), cudaMemcpyHostToDevice));
+  return EVR_OK;
+}
+
+int evr::multi_launch_bound(evr_sg4_multi* m, int slot, const double* const* psi, double* const* hpsi,
+                            const double* E0, const double* Esc, void* stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!m->d_pslot[slot]) return set_error(EVR_ERR_STATE, "multi_launch_bound: slot %d is not bound", slot);
+  for (MGroup& g : m->groups) {
+    CUDA_TRY(cudaMemsetAsync(g.d_counter, 0, sizeof(unsigned int), s));
+    launch_multi(g.geo, g.grid, (size_t)g.smem_doubles * 8, s, m->d_pslot[slot], g.d_items, (int)g.sorted.size(), 0,
+                 g.d_counter);
+    CUDA_TRY(cudaGetLastError());
+  }
+  for (int k = 0; k < m->n; ++k) {
+    const long long ld = m->ctxs[k]->nvec << m->cshift;
+    int rc = launch_reduce(m->ctxs[k], m->d_contrib[k], (double2*)m->d_part[k], m->nrhs_v[k], m->cshift, psi[k], ld,
+                           hpsi[k], ld, E0[k], Esc[k], s);
+    if (rc) return rc;
+  }
   return EVR_OK;
 }
 

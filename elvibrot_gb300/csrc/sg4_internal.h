@@ -53,6 +53,11 @@ struct BoundApply;
 int bound_apply_create(evr_sg4_ctx* c, int nrhs, int transpose, const double* psi, double* hpsi, BoundApply** out);
 int bound_apply_launch(BoundApply* b, void* stream);
 void bound_apply_destroy(BoundApply* b);
+// A multi-context plan's parameter blocks bound to fixed vectors (slot 0 or
+// 1, ld = nb0*N): a bound launch enqueues kernels and memsets only.
+int multi_bind(evr_sg4_multi* m, int slot, const double* const* psi, double* const* hpsi);
+int multi_launch_bound(evr_sg4_multi* m, int slot, const double* const* psi, double* const* hpsi, const double* E0,
+                       const double* Esc, void* stream);
 // Contexts, right-hand sides per context, complex shift and transpose flag
 // of a multi-context plan.
 void multi_shape(const evr_sg4_multi* m, std::vector<evr_sg4_ctx*>* ctxs, std::vector<int>* nrhs, int* cshift,

@@ -1454,9 +1454,124 @@ extern "C" int evr_sg4_multi_cheby_propagate(evr_sg4_multi* m, const evr_cheby_o
   std::vector<double*> dst(n);
   std::vector<long long> ld(N.begin(), N.end());
   std::vector<char> pending(n);
+  // Recorded steps: with every context in its step and its (E0, Esc, c_k)
+  // unchanged since the recording, one whole step -- the start of every
+  // context's recurrence, each order's merged H.psi (bound parameter blocks:
+  // the source vector alternates between two buffers, so two blocks) with the
+  // contexts' ordered accumulations and recurrence updates, and the norms of
+  // the last terms into pinned memory -- replays as one CUDA graph.  A context
+  // whose step diverges is then redone eagerly, alone with the other diverged
+  // ones; the same kernels run either way, so the bits are those of the eager
+  // path.
+  const bool use_graph = !o[0].no_graph;
+  struct StepGraph {
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t cs = nullptr;
+    double* hnrm = nullptr;
+    ~StepGraph() {
+      if (exec) cudaGraphExecDestroy(exec);
+      if (cs) cudaStreamDestroy(cs);
+      if (hnrm) cudaFreeHost(hnrm);
+    }
+  } sgr;
+  std::vector<double> rec_E0(n, 0.0), rec_Esc(n, 0.0);
+  std::vector<const double*> src0(n), src1(n);
+  std::vector<double*> dstb(n);
+  if (use_graph) {
+    for (int k = 0; k < n; ++k) {
+      src0[k] = (const double*)buf(0, k);
+      src1[k] = (const double*)buf(1, k);
+      dstb[k] = (double*)buf(2, k);
+    }
+    if ((rc = multi_bind(m, 0, src0.data(), dstb.data())) || (rc = multi_bind(m, 1, src1.data(), dstb.data())))
+      return rc;
+    CUDA_TRY_S(cudaStreamCreateWithFlags(&sgr.cs, cudaStreamNonBlocking));
+    CUDA_TRY_S(cudaMallocHost(&sgr.hnrm, (size_t)n * 8));
+  }
+  auto enqueue_step = [&](cudaStream_t st) -> int {  // every context, fixed (E0, Esc, c_k)
+    for (int k = 0; k < n; ++k) {
+      CUDA_TRY_S(cudaMemcpyAsync(buf(0, k), psi[k], (size_t)len[k] * 16, cudaMemcpyDeviceToDevice, st));
+      cscale_kernel<<<ew_grid(len[k]), B, 0, st>>>(buf(3, k), buf(0, k), len[k], cf[k][0], 0.0);
+      CUDA_TRY_S(cudaMemsetAsync(buf(1, k), 0, (size_t)len[k] * 16, st));
+    }
+    for (int ord = 2; ord <= npoly; ++ord) {
+      const bool odd = ord & 1;
+      int r = multi_launch_bound(m, (ord == 2 || !odd) ? 0 : 1, (ord == 2 || !odd) ? src0.data() : src1.data(),
+                                 dstb.data(), E0.data(), Esc.data(), st);
+      if (r) return r;
+      const bool last = ord == npoly;
+      if (last) CUDA_TRY_S(cudaMemsetAsync(nrm.p, 0, (size_t)n * 8, st));
+      for (int k = 0; k < n; ++k) {
+        if (ord == 2) {
+          cheby_update_kernel<<<ew_grid(len[k]), B, 0, st>>>(buf(1, k), buf(2, k), buf(3, k), len[k], 0.0, 0.0, -1.0,
+                                                             cf[k][1], last ? nrm.p + k : nullptr);
+        } else {
+          cheby_update_kernel<<<ew_grid(len[k]), B, 0, st>>>(odd ? buf(0, k) : buf(1, k), buf(2, k), buf(3, k),
+                                                             len[k], 1.0, 0.0, -2.0, cf[k][ord - 1],
+                                                             last ? nrm.p + k : nullptr);
+        }
+      }
+      CUDA_TRY_S(cudaGetLastError());
+    }
+    CUDA_TRY_S(cudaMemcpyAsync(sgr.hnrm, nrm.p, (size_t)n * 8, cudaMemcpyDeviceToHost, st));
+    return EVR_OK;
+  };
   for (int step = 0; step < nsteps; ++step) {
     std::fill(pending.begin(), pending.end(), 1);
     for (int attempt = 0; attempt < 10; ++attempt) {
+      if (use_graph && attempt == 0) {  // every context pending: the recorded step
+        bool same = sgr.exec != nullptr;
+        for (int k = 0; k < n; ++k) {
+          const double dE = Hmax[k] - Hmin[k], r0 = 0.5 * dE * dt;
+          E0[k] = Hmin[k] + 0.5 * dE;
+          Esc[k] = 0.5 * dE;
+          if (E0[k] != rec_E0[k] || Esc[k] != rec_Esc[k]) same = false;
+          bessel_j(r0, npoly, J);
+          cf[k].assign(npoly, 0.0);
+          cf[k][0] = J[0];
+          for (int q = 1; q < npoly; ++q) cf[k][q] = 2.0 * J[q];
+        }
+        if (!same) {
+          if (sgr.exec) cudaGraphExecDestroy(sgr.exec);
+          sgr.exec = nullptr;
+          CUDA_TRY_S(cudaStreamSynchronize(s));
+          cudaGraph_t gr = nullptr;
+          CUDA_TRY_S(cudaStreamBeginCapture(sgr.cs, cudaStreamCaptureModeThreadLocal));
+          rc = enqueue_step(sgr.cs);
+          cudaError_t ec = cudaStreamEndCapture(sgr.cs, &gr);
+          if (rc) {
+            if (gr) cudaGraphDestroy(gr);
+            return rc;
+          }
+          if (ec != cudaSuccess) return set_error(EVR_ERR_CUDA, "multi_cheby: graph capture: %s", cudaGetErrorString(ec));
+          ec = cudaGraphInstantiate(&sgr.exec, gr, 0);
+          cudaGraphDestroy(gr);
+          if (ec != cudaSuccess) {
+            sgr.exec = nullptr;
+            return set_error(EVR_ERR_CUDA, "multi_cheby: graph instantiate: %s", cudaGetErrorString(ec));
+          }
+          rec_E0 = E0;
+          rec_Esc = Esc;
+        }
+        CUDA_TRY_S(cudaGraphLaunch(sgr.exec, s));
+        CUDA_TRY_S(cudaStreamSynchronize(s));
+        bool any = false;
+        for (int k = 0; k < n; ++k) {
+          const double norm_exit = std::fabs(sgr.hnrm[k] * cf[k][npoly - 1]);
+          if (!(norm_exit <= 1e15)) {
+            Hmax[k] += 0.1 * (Hmax[k] - Hmin[k]);
+            any = true;
+            continue;
+          }
+          const double ph = -E0[k] * dt;  // psi = out exp(-i E0 dt)
+          cscale_kernel<<<ew_grid(len[k]), B, 0, s>>>((double2*)psi[k], buf(3, k), len[k], std::cos(ph),
+                                                      std::sin(ph));
+          pending[k] = 0;
+        }
+        CUDA_TRY_S(cudaGetLastError());
+        if (!any) break;
+        continue;
+      }
       for (int k = 0; k < n; ++k) {
         src[k] = nullptr;
         if (!pending[k]) continue;

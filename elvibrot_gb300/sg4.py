@@ -593,9 +593,11 @@ class MultiOp:
         check(lib().evr_sg4_multi_last_launches(self._h, ctypes.byref(v)))
         return v.value
 
-    def cheby_propagate(self, psis, Hmin, Hmax, dt: float, npoly: int, nsteps: int, stream: int = 0):
+    def cheby_propagate(self, psis, Hmin, Hmax, dt: float, npoly: int, nsteps: int, stream: int = 0,
+                        graph: bool = True):
         """Fixed-order Chebyshev propagation of every operator's complex packets
-        in lock-step; returns the autocorrelations [(nsteps+1) x nrhs_k] per operator."""
+        in lock-step (each step replayed from a recorded CUDA graph unless
+        graph=False); returns the autocorrelations [(nsteps+1) x nrhs_k] per operator."""
         import torch
         if not self.complex_:
             raise EVRError(1, "cheby_propagate needs a complex plan")
@@ -603,7 +605,7 @@ class MultiOp:
         rows = _check_blocks(self.ops, psis, psis, torch.complex128)
         if rows != self.nrhs:
             raise EVRError(1, "psis do not match the plan's nrhs")
-        opts = (ChebyOpts * n)(*[ChebyOpts(float(Hmin[k]), float(Hmax[k]), dt, npoly, nsteps, 0.0, 0)
+        opts = (ChebyOpts * n)(*[ChebyOpts(float(Hmin[k]), float(Hmax[k]), dt, npoly, nsteps, 0.0, 0 if graph else 1)
                                  for k in range(n)])
         ac = [np.zeros((nsteps + 1, r), dtype=np.complex128) for r in rows]
         used = ctypes.c_int()

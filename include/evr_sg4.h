@@ -374,7 +374,11 @@ int evr_sg4_multi_destroy(evr_sg4_multi* m);
  * equal for all, poly_tol <= 0).  A context whose step diverges redoes it
  * with Hmax raised by (Hmax-Hmin)/10, up to 10 times.  psi[k]: device
  * interleaved complex128 N_k x nrhs_k, propagated in place; autocorr[k]: host
- * complex [(nsteps+1) x nrhs_k] = <psi_k(0) | psi_k(t_j)>, or NULL. */
+ * complex [(nsteps+1) x nrhs_k] = <psi_k(0) | psi_k(t_j)>, or NULL.  Unless
+ * o[0].no_graph, a step with every context in it (each order's merged launch,
+ * the ordered accumulations and recurrence updates of every context) is
+ * recorded once as a CUDA graph and replayed while the bounds stay the same;
+ * diverged contexts are redone eagerly (the same kernels, the same bits). */
 int evr_sg4_multi_cheby_propagate(evr_sg4_multi* m, const evr_cheby_opts* o, double* const* psi,
                                   double* const* autocorr, int* npoly_used, void* stream);
 /* One-shot form: create, apply, synchronize the stream, destroy. */

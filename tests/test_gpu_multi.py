@@ -267,3 +267,31 @@ def test_uneven_64_instances_lock_step_chebyshev():
         d = (P - psis[k]).abs().max().item()
         assert d <= 1e-14, (k, d)
         assert np.max(np.abs(a1 - ac[k])) <= 1e-14, k
+
+
+def test_multi_chebyshev_graph_replay_is_bit_identical():
+    """Lock-step steps replayed from the recorded CUDA graph of a whole step
+    give the same bits as the same kernels launched one by one, also when a
+    diverging context is redone eagerly between replays."""
+    need_cuda()
+    models = [make_model(3, 5, 1, 61), make_model(4, 4, 1, 62), make_model(2, 7, 1, 63)]
+    ops = [m.operator() for m in models]
+    nrhs = [2, 1, 3]
+    spec = [_dense(m) for m in models]
+    Hmin = [w[0] - 0.05 * (w[-1] - w[0]) for w, _ in spec]
+    Hmax = [w[-1] + 0.05 * (w[-1] - w[0]) for w, _ in spec]
+    Hmax[1] = spec[1][0][0] + 0.4 * (spec[1][0][-1] - spec[1][0][0])   # context 1 diverges and is redone
+    start = []
+    for k, (op, r) in enumerate(zip(ops, nrhs)):
+        P = _rand(op, r, True, 600 + k)
+        start.append(P / torch.linalg.vector_norm(P, dim=1, keepdim=True))
+    outs = []
+    for graph in (False, True):
+        psis = [P.clone() for P in start]
+        plan = MultiOp(ops, nrhs, complex_=True)
+        ac = plan.cheby_propagate(psis, Hmin, Hmax, 10.0, 30, 4, graph=graph)
+        torch.cuda.synchronize()
+        outs.append((psis, ac))
+    for k in range(3):
+        assert torch.equal(outs[0][0][k], outs[1][0][k]), k
+        assert np.array_equal(outs[0][1][k], outs[1][1][k]), k
