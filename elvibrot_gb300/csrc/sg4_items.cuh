@@ -51,9 +51,6 @@ namespace evr {
 #ifndef EVR_FASTDIV
 #define EVR_FASTDIV 1     // those divisions by multiply-high with per-item magic numbers
 #endif
-#ifndef EVR_PAIRB
-#define EVR_PAIRB 0       // narrow pass B: two points per thread
-#endif
 
 struct TermInfo {
   long long off_nb;   // into map
@@ -534,54 +531,6 @@ __device__ void type10_fused(const KParams& p, const ItemShared& it, const doubl
     }
   }
   __syncthreads();
-#if EVR_PAIRB
-  if constexpr (!INC) {
-    // two points per thread (e and e + T): two independent FMA chains over
-    // the same modes' fibres, each in the order of the one-point loop below
-    const int T = blockDim.x;
-    for (int e = threadIdx.x; e < NQR; e += 2 * T) {
-      const int e2 = e + T;
-      const bool two = e2 < NQR;
-      int idx[DD], idx2[DD], q, q2;
-      point_digits<DD, INC>(gp, ms, nqt, e, idx, q);
-      point_digits<DD, INC>(gp, ms, nqt, two ? e2 : e, idx2, q2);
-      double sum = 0.0, sum2 = 0.0;
-#pragma unroll
-      for (int i = 0; i < DD; ++i) {
-        const int n = ms.nq(i), sd = ms.st(i);
-        const double* Ui = U + (long long)i * NQR;
-        const double* fib = Ui + (e - idx[i] * sd);
-        const double* fib2 = Ui + ((two ? e2 : e) - idx2[i] * sd);
-        const double* Mi = ms.Md(i);
-        const double* row = Mi + idx[i] * n;
-        const double* row2 = Mi + idx2[i] * n;
-        for (int m = 0; m < n; ++m) {
-          sum = fma(__ldg(row + m), fib[m * sd], sum);
-          sum2 = fma(__ldg(row2 + m), fib2[m * sd], sum2);
-        }
-      }
-      if (inplace) {
-        const double vx = p.V ? __ldg(p.V + oq + q) * O[e] : 0.0;
-        O[e] = fma(-0.5, sum, vx);
-        if (two) {
-          const double vx2 = p.V ? __ldg(p.V + oq + q2) * O[e2] : 0.0;
-          O[e2] = fma(-0.5, sum2, vx2);
-        }
-      } else {
-        const double cf = !p.transpose ? (p.cfac ? __ldg(p.cfac + oq + q) : -0.5)
-                                       : (p.sqRho ? __ldg(p.sqRho + oq + q) : 1.0);
-        O[e] = fma(cf, sum, O[e]);
-        if (two) {
-          const double cf2 = !p.transpose ? (p.cfac ? __ldg(p.cfac + oq + q2) : -0.5)
-                                          : (p.sqRho ? __ldg(p.sqRho + oq + q2) : 1.0);
-          O[e2] = fma(cf2, sum2, O[e2]);
-        }
-      }
-    }
-    __syncthreads();
-    return;
-  }
-#endif
   if constexpr (INC) gp.init(ms.nq_, nqt, threadIdx.x, blockDim.x);
   for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
     int idx[DD], q;
