@@ -254,7 +254,7 @@ __global__ void fields_kernel(const TermInfo* terms, long long nb_SG, const long
                               const int* nq_of_l, const double* xcat, const int* x_off, int D, int Lp1,
                               int V_nterms, const double* V_coef, const int* V_fac, double* V,
                               const double* G0, const double* G1, double* G, long long gp0, long long gp1, int nb0,
-                              long long vstride) {
+                              long long vstride, int Gsym) {
   for (long long gp = gp0 + blockIdx.x * (long long)blockDim.x + threadIdx.x; gp < gp1;
        gp += (long long)gridDim.x * blockDim.x) {
     // binary search of the term owning global point gp
@@ -288,14 +288,18 @@ __global__ void fields_kernel(const TermInfo* terms, long long nb_SG, const long
       }
     }
     if (G) {
+      // a symmetric affine form (G0 and G1 symmetric in i, j, bit for bit)
+      // gives G_ji the same FMA chain as G_ij: formed once, stored twice
       const long long nqt = T.nq;
+      double* Gt = G + (T.off_nq - gp0) * D * D + q;
       for (int i = 0; i < D; ++i)
-        for (int j = 0; j < D; ++j) {
+        for (int j = Gsym ? i : 0; j < D; ++j) {
           double g = G0 ? G0[i * D + j] : (i == j ? 1.0 : 0.0);
           if (G1)
             for (int k = 0; k < D; ++k) g = fma(G1[((long long)i * D + j) * D + k], Q[k], g);
           // GGiq(iq, j, i) of the term
-          G[(T.off_nq - gp0) * D * D + nqt * ((long long)D * i + j) + q] = g;
+          Gt[nqt * ((long long)D * i + j)] = g;
+          if (Gsym) Gt[nqt * ((long long)D * j + i)] = g;
         }
     }
   }
@@ -415,6 +419,7 @@ struct evr_sg4_ctx {
   int* d_Vfac = nullptr;
   double* d_G0 = nullptr;
   double* d_G1 = nullptr;
+  int G_sym = 0;                      // the affine G is symmetric bit for bit (G_ji formed once)
   long long* d_pt_start = nullptr;    // [nb_SG] first grid point of every term
   std::vector<long long> slice_term;  // [nslices+1] term ranges
   std::vector<int> slice_item;        // [nslices+1] ranges of the sorted work list
@@ -667,7 +672,7 @@ static int eval_fields(evr_sg4_ctx* c, long long g0, long long g1, bool V, bool 
   fields_kernel<<<(unsigned)blocks, 256, 0, s>>>(c->d_terms, c->nb_SG, c->d_pt_start, c->d_nq_of_l, c->d_x,
                                                  c->d_x_off, c->D, c->L + 1, V ? c->V_nterms : 0, c->d_Vcoef,
                                                  c->d_Vfac, V ? c->d_V : nullptr, c->d_G0, c->d_G1,
-                                                 G ? c->d_G : nullptr, g0, g1, c->nb0, c->z.sum_nq);
+                                                 G ? c->d_G : nullptr, g0, g1, c->nb0, c->z.sum_nq, c->G_sym);
   CUDA_TRY(cudaGetLastError());
   return EVR_OK;
 }
@@ -802,6 +807,18 @@ extern "C" int evr_sg4_set_operator(evr_sg4_ctx* c, const evr_sg4_op_desc* op) {
                   (rc = upload(&c->d_Vfac, vfac.data(), vfac.size()))))
       return rc;
     c->V_nterms = polyV ? op->V_nterms : 0;
+    c->G_sym = 0;
+    if (affG) {
+      bool sym = true;
+      for (int i = 0; i < D && sym; ++i)
+        for (int j = 0; j < D && sym; ++j) {
+          if (op->G0 && memcmp(&op->G0[i * D + j], &op->G0[j * D + i], sizeof(double)) != 0) sym = false;
+          for (int k = 0; k < D && sym && op->G1; ++k)
+            if (memcmp(&op->G1[((size_t)i * D + j) * D + k], &op->G1[((size_t)j * D + i) * D + k], sizeof(double)))
+              sym = false;
+        }
+      c->G_sym = sym ? 1 : 0;
+    }
     if (affG && op->G0 && (rc = upload(&c->d_G0, op->G0, (size_t)D * D))) return rc;
     if (affG && op->G1 && (rc = upload(&c->d_G1, op->G1, (size_t)D * D * D))) return rc;
     if (!stream) {
