@@ -51,6 +51,9 @@ namespace evr {
 #ifndef EVR_FASTDIV
 #define EVR_FASTDIV 1     // those divisions by multiply-high with per-item magic numbers
 #endif
+#ifndef EVR_SPLIT_RES
+#define EVR_SPLIT_RES 1   // fused type 10: x in shared memory when the other arrays do not fit
+#endif
 
 struct TermInfo {
   long long off_nb;   // into map
@@ -158,7 +161,8 @@ struct ItemShared {
   long long off_nb, off_nq;
   int nb_t, nq_t, r, rhs0, term;
   double w;
-  double* base;
+  double* base;               // the work arrays: base holds the first (x), base2 the rest
+  double* base2;
 };
 
 __device__ __forceinline__ long long vaddr(const KParams& p, int v, int n, long long ld) {
@@ -695,8 +699,21 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ter
     it.nb_t = T.nb;
     it.nq_t = T.nq;
     it.w = T.w;
-    long long need = (long long)p.nbuf * T.nq * it.r;
-    it.base = (need <= p.smem_doubles) ? smem : p.gscratch + (long long)blockIdx.x * p.scratch_per_cta;
+    const long long nqr = (long long)T.nq * it.r;
+    const long long need = (long long)p.nbuf * nqr;
+    double* slab = p.gscratch + (long long)blockIdx.x * p.scratch_per_cta;
+    if (need <= p.smem_doubles) {  // every work array in shared memory
+      it.base = smem;
+      it.base2 = smem + nqr;
+    } else if (EVR_SPLIT_RES && p.type == 10 && p.nbuf == p.D + 1 && p.D <= FMAX && nqr <= p.smem_doubles) {
+      // x -- the array the fused pass A reads along every mode's fibres -- in
+      // shared memory, U_1..U_D in the global-scratch slab
+      it.base = smem;
+      it.base2 = slab;
+    } else {
+      it.base = slab;
+      it.base2 = slab + nqr;
+    }
     it.mgt = T.nq > 1 ? 0xFFFFFFFFFFFFFFFFull / (unsigned long long)T.nq + 1ull : 0ull;
   }
   if (threadIdx.x < p.D) {
@@ -733,7 +750,7 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ter
   const int NQR = nqt * r;
   double* buf = it.base;
   double* X = buf;
-  double* T = buf + NQR;
+  double* T = it.base2;  // buf + NQR unless x alone is in shared memory (fused type 10)
   const int* map = p.map + it.off_nb;
 
   // gather (tabPackedBasis_TO_tabR_AT_iG) into the buffer from which the D
@@ -769,12 +786,12 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ter
     // allocation and cost the type-10 benchmark 1.2 %
     if constexpr (FMAX > EVR_NARROW_FMAX) {
       double* O = T;
-      type1_fused_dispatch<FMAX>(p, it, x, O, buf + 2 * NQR, NQR);
+      type1_fused_dispatch<FMAX>(p, it, x, O, T + NQR, NQR);
       y = O;
     } else {
       // CASE 1: y = V.x + sum F2_ij d_i d_j x + sum F1_i d_i x, term by term
-      double* Y = buf + 2 * NQR;
-      double* C = buf + 3 * NQR;
+      double* Y = T + NQR;
+      double* C = T + 2 * NQR;
       for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
         const int q = e % nqt;
         Y[e] = !p.V ? 0.0 : (p.nb0 == 1 ? __ldg(p.V + oq + q) * x[e] : vmat_apply(p, x, e, nqt, oq, it.rhs0));
@@ -812,7 +829,7 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ter
     // before the rescaling, so in a pass of its own).
     const bool inplace = p.nbuf == D + 1;
     double* O = inplace ? x : T;
-    double* U = buf + (inplace ? 1 : 2) * NQR;
+    double* U = T + (inplace ? 0 : 1) * NQR;
     if (!inplace) {
       if (p.nb0 > 1) {
         channels_prologue(p, oq, nqt, it.rhs0, x, O, NQR);
@@ -831,14 +848,14 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ter
       __syncthreads();
     }
     type10_fused_dispatch<FMAX>(p, it, x, O, U, NQR, inplace);
-    double* yb = transform(p, it, false, O, inplace ? buf + NQR : x);
+    double* yb = transform(p, it, false, O, inplace ? T : x);
     store_contrib(p, it, yb);
     return;
   } else {
     // CASE 10: -1/2 sum_i d_i(Jac sum_j G_ji d_j(s x)) / (Jac s) + V x
-    double* VX = buf + 2 * NQR;
-    double* O = buf + 3 * NQR;
-    double* Phi = buf + 4 * NQR;
+    double* VX = T + NQR;
+    double* O = T + 2 * NQR;
+    double* Phi = T + 3 * NQR;
     // forward: s.x first and -1/2/(Jac s) last; H^T swaps the two scalings;
     // coupled channels' V.x before the rescaling, in a pass of its own
     if (p.nb0 > 1) {
