@@ -526,6 +526,41 @@ def bench_streamed_12d_l10(nrhs=1, budget_gib=64):
             "finite": bool(torch.isfinite(O).all().item())}
 
 
+def bench_davidson12(L=4, nev=50):
+    """The 12-D workload's Davidson (50 levels) at a level where the dense
+    operator can still check it: type 10 with Q-dependent G, L=4 (N = 1820),
+    symmetrised, residual 1e-8, the term-wise diagonal as preconditioner; the
+    levels against a dense diagonalisation of (H + H^T)/2 built from the GPU
+    operator.  About a minute, so only on request (--extras davidson12)."""
+    import torch
+    from elvibrot_gb300.configs import SEED0, make_model
+    CM1 = 4.556335252767e-6
+    m = make_model(12, L, 10, SEED0 + 4)
+    op = m.operator()
+    N = op.basis.N
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    d = op.diagonal()
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    ev, vec, rs, its = op.davidson(nev, block=nev, max_subspace=3 * nev, conv_resi=1e-8, symmetrize=True, diag=d,
+                                   max_it=2000)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    H = np.empty((N, N))
+    for n0 in range(0, N, 256):
+        k = min(256, N - n0)
+        E = torch.zeros((k, N), dtype=torch.float64, device="cuda")
+        E[torch.arange(k), torch.arange(n0, n0 + k)] = 1.0
+        out = torch.empty_like(E)
+        op.hpsi_dev(E, out)
+        H[:, n0:n0 + k] = out.cpu().numpy().T
+    ref = np.linalg.eigvalsh(0.5 * (H + H.T))[:nev]
+    return {"workload": f"12-D SG4 L={L} type 10 (Q-dependent G), lowest {nev} levels of (H + H^T)/2",
+            "N": N, "diagonal_s": t1 - t0, "davidson_s": t2 - t1, "iterations": its, "max_residual": float(np.max(rs)),
+            "max_dev_from_dense_cm1": float(np.max(np.abs(ev - ref)) / CM1)}
+
+
 def run_ours(args, ws, rank, local):
     import torch
     import torch.distributed as dist
@@ -639,6 +674,8 @@ def run_ours(args, ws, rank, local):
             extras["cheby_graph"] = bench_cheby_graph()
         if "stream12" in want:
             extras["streamed_12d"] = bench_streamed_12d()
+        if "davidson12" in want:
+            extras["davidson12"] = bench_davidson12()
         if "stream12_L10" in want:
             extras["streamed_12d_L10"] = bench_streamed_12d_l10()
 
@@ -735,7 +772,8 @@ def main():
                     help="callers to time: config0 (the 3-D L=6 workload), davidson, oc (optimal-control gradient), "
                          "uneven (64-instance batching), "
                          "graph (Chebyshev steps replayed from a CUDA graph), stream12 (12-D type 10, streamed fields); "
-                         "also on request: stream12_L10 (the 12-D workload at L=10, minutes)")
+                         "also on request: stream12_L10 (the 12-D workload at L=10, minutes), davidson12 (50 levels of "
+                         "the 12-D operator at L=4, checked against dense diagonalisation)")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if ws > 1:
