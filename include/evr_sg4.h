@@ -410,8 +410,8 @@ int evr_sg4_rk4_field(evr_sg4_ctx* H0, evr_sg4_ctx* mu, const evr_rk4_opts* o, c
  * (E: host [nsteps*nb]); psi: device complex128 N x nb (ld N), in place.
  * One H0/mu launch per stage serves all packets (the reference propagates
  * its nb_WP packets together, sub_propagation25, sub_control.f90).  Each
- * packet's result is that of evr_sg4_rk4_field under its own field, to
- * rounding. */
+ * packet gets the same bits as evr_sg4_rk4_field under its own field (the
+ * same per-column arithmetic and accumulation order). */
 int evr_sg4_rk4_field_batch(evr_sg4_ctx* H0, evr_sg4_ctx* mu, const evr_rk4_opts* o, int nb, const double* E,
                             double* psi, void* stream);
 
