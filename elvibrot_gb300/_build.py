@@ -18,11 +18,13 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libevrsg4.so")
 
 SOURCES = ["sg4_device.cu", "sg4_solvers.cu", "sg4_setup.cpp", "sg4_items.cu"]
-# translation units: (source, object, extra flags); the item kernels are
-# compiled once per launch geometry (wide, narrow, mid)
-UNITS = [("sg4_device.cu", "sg4_device.o", []), ("sg4_solvers.cu", "sg4_solvers.o", []),
-         ("sg4_setup.cpp", "sg4_setup.o", [])] + [
-    ("sg4_items.cu", f"sg4_items_g{g}.o", [f"-DEVR_GEO={g}"]) for g in range(3)]
+# translation units: (source, object, extra flags); each item kernel is its
+# own unit, per launch geometry (wide, narrow, mid) and kind (single context,
+# merged with the small and the large parameter block)
+UNITS = [("sg4_items.cu", f"sg4_items_g{g}_k{k}.o", [f"-DEVR_GEO={g}", f"-DEVR_KIND={k}"])
+         for g in range(3) for k in range(3)] + [
+    ("sg4_device.cu", "sg4_device.o", []), ("sg4_solvers.cu", "sg4_solvers.o", []),
+    ("sg4_setup.cpp", "sg4_setup.o", [])]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -67,7 +69,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
             print(r.stdout + r.stderr)
         return obj
 
-    with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+    with ThreadPoolExecutor(max_workers=min(len(UNITS), max(4, os.cpu_count() or 4))) as ex:
         objs = list(ex.map(compile_one, UNITS))
     tmp = LIB + ".tmp"
     cmd = [cc, "-shared", "-o", tmp] + objs + ARCH + ["-lcudart", "-lcublas"]

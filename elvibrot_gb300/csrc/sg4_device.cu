@@ -98,40 +98,60 @@ int desc_sizes(const evr_sg4_desc* d, DescSizes* z) {
 namespace evr {
 
 // The kernels of launch geometry geo (0 wide, 1 narrow, 2 mid).
+struct GeoKernels {
+  int ctas;  // resident CTAs per SM
+  const BatchedEntry* batched;
+  const MultiEntry<EVR_PB_SMALL>* multi_small;
+  const MultiEntry<EVR_PB_LARGE>* multi_large;
+};
 static const GeoKernels& geo_kernels(int geo) {
-  return geo == 1 ? geo_kernels_narrow : (geo == 2 ? geo_kernels_mid : geo_kernels_wide);
+  static const GeoKernels t[3] = {
+      {EVR_WIDE_CTAS, &batched_wide, &multi_small_wide, &multi_large_wide},
+      {EVR_NARROW_CTAS, &batched_narrow, &multi_small_narrow, &multi_large_narrow},
+      {EVR_MID_CTAS, &batched_mid, &multi_small_mid, &multi_large_mid}};
+  return t[geo == 1 ? 1 : (geo == 2 ? 2 : 0)];
 }
 
 static void launch_batched(int geo, unsigned grid, size_t smem, cudaStream_t s, const KParams& p) {
-  geo_kernels(geo).batched(grid, smem, s, p);
+  geo_kernels(geo).batched->launch(grid, smem, s, p);
 }
 
-static void launch_multi(int geo, unsigned grid, size_t smem, cudaStream_t s, const KParams* ps, const MItem* items,
-                         int n_items, int item_base, unsigned int* counter) {
-  geo_kernels(geo).multi(grid, smem, s, ps, items, n_items, item_base, counter);
+// A merged launch over n_ctx <= EVR_PB_LARGE contexts whose parameters are
+// ps[0..n_ctx) (host memory; items name their slot).  The launch copies the
+// block, so ps may change as soon as this returns, and a CUDA graph that
+// records the launch keeps the values of the recording.
+static void launch_multi(int geo, unsigned grid, size_t smem, cudaStream_t s, const KParams* ps, int n_ctx,
+                         const MItem* items, int n_items, int item_base, unsigned int* counter) {
+  if (n_ctx <= EVR_PB_SMALL) {
+    ParamBlock<EVR_PB_SMALL> P;
+    std::copy(ps, ps + n_ctx, P.p);
+    geo_kernels(geo).multi_small->launch(grid, smem, s, P, items, n_items, item_base, counter);
+  } else {
+    static thread_local ParamBlock<EVR_PB_LARGE> P;  // 17.5 KB: not on the stack
+    std::copy(ps, ps + n_ctx, P.p);
+    geo_kernels(geo).multi_large->launch(grid, smem, s, P, items, n_items, item_base, counter);
+  }
 }
 
 static int geo_ctas(int geo) { return geo_kernels(geo).ctas; }
 
 // Static shared memory plus the 1 KB the driver reserves per CTA, rounded up
-// to 256 bytes (queried once): for the wide and mid geometries the larger of
-// their two item kernels (the field-driven propagation and multi-context
-// plans run the multi-context kernel there; sized for the single-context
-// kernel alone, it kept three wide CTAs per SM instead of four and the RK4
-// forward ran 8 % slower); for the narrow one the single-context kernel,
-// whose eight CTAs per SM carry the large operators (a narrow multi-context
-// launch, with its larger parameter block, keeps seven).
+// to 256 bytes (queried once): the largest of a geometry's three item kernels,
+// so each of them keeps the geometry's CTAs per SM (sized for the
+// single-context kernel alone, a wide merged launch once kept three CTAs per
+// SM instead of four and the RK4 forward ran 8 % slower).
 static int smem_slack(int geo) {
   static const std::vector<int> slack = [] {
     std::vector<int> v(3, 4096);
     for (int g = 0; g < 3; ++g) {
-      size_t b = 0, m = 0;
-      if (geo_kernels(g).static_smem(&b, &m) != cudaSuccess) {
+      size_t b = 0, ms = 0, ml = 0;
+      const GeoKernels& k = geo_kernels(g);
+      if (k.batched->static_smem(&b) != cudaSuccess || k.multi_small->static_smem(&ms) != cudaSuccess ||
+          k.multi_large->static_smem(&ml) != cudaSuccess) {
         cudaGetLastError();
         continue;
       }
-      const size_t st = g == 1 ? b : std::max(b, m);
-      v[g] = (int)((st + 1024 + 255) / 256 * 256);
+      v[g] = (int)((std::max(b, std::max(ms, ml)) + 1024 + 255) / 256 * 256);
     }
     return v;
   }();
@@ -146,7 +166,13 @@ static int geo_smem_bytes(int geo) { return (228 * 1024 / geo_ctas(geo) - smem_s
 // dynamic shared memory of every geometry's kernels (set at context creation)
 static cudaError_t set_smem_attributes() {
   cudaError_t e = cudaSuccess;
-  for (int g = 0; g < 3 && e == cudaSuccess; ++g) e = geo_kernels(g).set_smem(geo_smem_bytes(g));
+  for (int g = 0; g < 3 && e == cudaSuccess; ++g) {
+    const GeoKernels& k = geo_kernels(g);
+    const int bytes = geo_smem_bytes(g);
+    e = k.batched->set_smem(bytes);
+    if (e == cudaSuccess) e = k.multi_small->set_smem(bytes);
+    if (e == cudaSuccess) e = k.multi_large->set_smem(bytes);
+  }
   return e;
 }
 
@@ -374,7 +400,6 @@ struct evr_sg4_ctx {
   TermInfo* d_terms = nullptr;
   Item* d_items = nullptr;
   MItem* d_plain_items = nullptr;    // term-ordered (context 0) items for the per-term path
-  KParams* d_params = nullptr;       // parameter block of the per-term path
   size_t items_cap = 0;
   int items_nrhs = -1;               // items built for this virtual nrhs
   int n_items = 0;
@@ -459,7 +484,7 @@ static int nbuf_for(const evr_sg4_ctx* c) {
 
 static void free_ctx(evr_sg4_ctx* c) {
   void* ptrs[] = {c->d_map, c->d_mats, c->d_mat_off, c->d_diag_off, c->d_nb_of_l, c->d_nq_of_l, c->d_x, c->d_x_off,
-                  c->d_terms, c->d_items, c->d_plain_items, c->d_params, c->d_counter, c->d_inv_ptr,
+                  c->d_terms, c->d_items, c->d_plain_items, c->d_counter, c->d_inv_ptr,
                   c->d_inv_idx, c->d_contrib, c->d_chunk_q, c->d_fun_chunk, c->d_part,
                   c->d_scratch, c->d_V, c->d_G, c->d_Jac, c->d_cfac,
                   c->d_sqRho, c->d_F2, c->d_F1, c->d_io, c->d_Vcoef, c->d_Vfac, c->d_G0, c->d_G1,
@@ -1077,15 +1102,12 @@ static int hpsi_common(evr_sg4_ctx* c, int nrhs, int cshift, const double* psi, 
     CUDA_TRY(cudaGetLastError());
     launches = 1;
   } else {
-    if (!c->d_params) CUDA_TRY(cudaMalloc(&c->d_params, sizeof(KParams)));
-    CUDA_TRY(cudaMemcpyAsync(c->d_params, &p, sizeof(KParams), cudaMemcpyHostToDevice, s));
     for (long long t = 0; t < c->nb_SG; ++t) {  // one launch per Smolyak term
       const int b0 = c->term_item_start[t], b1 = c->term_item_start[t + 1];
-      launch_multi(c->geo, b1 - b0, smem, s, c->d_params, c->d_plain_items, b1, b0, nullptr);
+      launch_multi(c->geo, b1 - b0, smem, s, &p, 1, c->d_plain_items, b1, b0, nullptr);
       ++launches;
     }
     CUDA_TRY(cudaGetLastError());
-    CUDA_TRY(cudaStreamSynchronize(s));  // the parameter block was copied from the stack
   }
   if ((rc = launch_reduce(c, c->d_contrib, (double2*)c->d_part, nrhs_v, cshift, psi, ldv_psi, hpsi, ldv_h, E0, Esc,
                           s)))
@@ -1424,11 +1446,12 @@ extern "C" int evr_sg4_hpsi_noalloc(evr_sg4_ctx* c, int nrhs, const double* psi,
 // shared by all contexts) and the merged cost-sorted item list; the contexts
 // lend their read-only tables and operator grids.
 // ------------------------------------------------------------------------
-// One persistent launch of a plan: the merged items of its contexts, in one
-// launch geometry.
+// One persistent launch of a plan: the merged items of its contexts (at most
+// EVR_PB_LARGE), in one launch geometry.
 struct MGroup {
   int geo = 0, grid = 0, smem_doubles = 0;
-  std::vector<MItem> sorted;     // its contexts' items, decreasing cost
+  std::vector<int> ctx_of;       // slot in the launch's parameter block -> context
+  std::vector<MItem> sorted;     // its contexts' items (ctx = slot), decreasing cost
   MItem* d_items = nullptr;      // the full list
   MItem* d_sub = nullptr;        // a filtered list (some contexts skipped)
   unsigned int* d_counter = nullptr;
@@ -1440,13 +1463,14 @@ struct evr_sg4_multi {
   std::vector<evr_sg4_ctx*> ctxs;
   std::vector<int> nrhs_v, type, nbuf;  // per context; type and work arrays per point fix the plan
   std::vector<int> group;        // per context: its launch group
-  std::vector<MGroup> groups;    // one, or two when D <= 6 contexts fill a narrow launch of their own
+  std::vector<int> slot;         // per context: its slot in that group's parameter block
+  std::vector<MGroup> groups;    // one, or two when D <= 6 contexts fill a narrow launch of their own;
+                                 // each split into launches of at most EVR_PB_LARGE contexts
   std::vector<TermInfo*> d_terms;
   std::vector<double*> d_contrib;
   std::vector<double*> d_part;
   double* d_scratch = nullptr;   // global-scratch slabs, shared by the groups (launched in turn)
-  KParams* d_params = nullptr;
-  KParams* d_pslot[2] = {nullptr, nullptr};  // parameter blocks bound to fixed vectors (multi_bind)
+  std::vector<KParams> pslot[2]; // parameters bound to fixed vectors (multi_bind), per context
   long long last_launches = 0;
 };
 
@@ -1467,8 +1491,7 @@ static void free_multi(evr_sg4_multi* m) {
     void* gp[] = {g.d_items, g.d_sub, g.d_counter};
     for (void* q : gp) if (q) cudaFree(q);
   }
-  void* ptrs[] = {m->d_scratch, m->d_params, m->d_pslot[0], m->d_pslot[1]};
-  for (void* q : ptrs) if (q) cudaFree(q);
+  if (m->d_scratch) cudaFree(m->d_scratch);
   delete m;
 }
 
@@ -1538,7 +1561,38 @@ extern "C" int evr_sg4_multi_create(int n, evr_sg4_ctx* const* ctxs, const int* 
     m->groups.resize(1);
     m->groups[0].geo = choose_geo(dmax, all_items, sms);
   }
+  {  // each group split into launches of at most EVR_PB_LARGE contexts, in context order
+    std::vector<MGroup> split;
+    std::vector<int> to(n, 0);
+    for (size_t gi = 0; gi < m->groups.size(); ++gi) {
+      int cnt = 0;
+      for (int k = 0; k < n; ++k) {
+        if (m->group[k] != (int)gi) continue;
+        if (cnt++ % EVR_PB_LARGE == 0) {
+          split.emplace_back();
+          split.back().geo = m->groups[gi].geo;
+        }
+        to[k] = (int)split.size() - 1;
+      }
+    }
+    m->groups.swap(split);
+    m->group.swap(to);
+  }
+  m->slot.assign(n, 0);
+  for (int k = 0; k < n; ++k) {
+    MGroup& g = m->groups[m->group[k]];
+    m->slot[k] = (int)g.ctx_of.size();
+    g.ctx_of.push_back(k);
+  }
   const int ng = (int)m->groups.size();
+  // a geometry named by evr_sg4_set_plan on every context of a group is the
+  // group's (set_plan keeps the narrow geometry to D <= 6)
+  for (int gi = 0; gi < ng; ++gi) {
+    int want = -2;
+    for (int k = 0; k < n; ++k)
+      if (m->group[k] == gi) want = (want == -2 || want == ctxs[k]->geo_override) ? ctxs[k]->geo_override : -1;
+    if (want >= 0) m->groups[gi].geo = want;
+  }
   std::vector<std::vector<MItem>> all(ng);
   std::vector<std::vector<float>> allcost(ng);
   long long scratch_doubles = 0;
@@ -1561,7 +1615,7 @@ extern "C" int evr_sg4_multi_create(int n, evr_sg4_ctx* const* ctxs, const int* 
     plan_work(c, nv, g.smem_doubles, terms, items, cost, need);
     if (need > g.smem_doubles) g.scratch_per_cta = std::max(g.scratch_per_cta, need);
     for (size_t q = 0; q < items.size(); ++q) {
-      all[gk].push_back(MItem{k, items[q].term, items[q].rhs0, 0});
+      all[gk].push_back(MItem{m->slot[k], items[q].term, items[q].rhs0, 0});
       allcost[gk].push_back(cost[q]);
     }
     if (cudaMalloc(&m->d_terms[k], terms.size() * sizeof(TermInfo)) != cudaSuccess ||
@@ -1590,12 +1644,21 @@ extern "C" int evr_sg4_multi_create(int n, evr_sg4_ctx* const* ctxs, const int* 
       return fail(set_error(EVR_ERR_CUDA, "multi_create: device allocation failed"));
     }
   }
-  if ((scratch_doubles && cudaMalloc(&m->d_scratch, (size_t)scratch_doubles * 8) != cudaSuccess) ||
-      cudaMalloc(&m->d_params, (size_t)n * sizeof(KParams)) != cudaSuccess) {
+  if (scratch_doubles && cudaMalloc(&m->d_scratch, (size_t)scratch_doubles * 8) != cudaSuccess) {
     cudaGetLastError();
     return fail(set_error(EVR_ERR_CUDA, "multi_create: device allocation failed"));
   }
   *out = m;
+  return EVR_OK;
+}
+
+extern "C" int evr_sg4_multi_groups(const evr_sg4_multi* m, int* n_groups, int* geo, long long* n_items) {
+  if (!m || !n_groups) return set_error(EVR_ERR_ARG, "multi_groups: NULL argument");
+  *n_groups = (int)m->groups.size();
+  for (size_t g = 0; g < m->groups.size(); ++g) {
+    if (geo) geo[g] = m->groups[g].geo;
+    if (n_items) n_items[g] = (long long)m->groups[g].sorted.size();
+  }
   return EVR_OK;
 }
 
@@ -1604,6 +1667,16 @@ extern "C" int evr_sg4_multi_destroy(evr_sg4_multi* m) {
   cudaDeviceSynchronize();
   free_multi(m);
   return EVR_OK;
+}
+
+// One launch group's merged items: the parameters of its contexts (by
+// context) gathered into the group's slots.
+static void launch_group(const MGroup& g, const std::vector<KParams>& params, const MItem* items, int n_items,
+                         cudaStream_t s) {
+  std::vector<KParams> slots(g.ctx_of.size());
+  for (size_t j = 0; j < g.ctx_of.size(); ++j) slots[j] = params[g.ctx_of[j]];
+  launch_multi(g.geo, g.grid, (size_t)g.smem_doubles * 8, s, slots.data(), (int)slots.size(), items, n_items, 0,
+               g.d_counter);
 }
 
 extern "C" int evr_sg4_multi_hpsi(evr_sg4_multi* m, const double* const* psi, const long long* ldpsi,
@@ -1637,7 +1710,6 @@ extern "C" int evr_sg4_multi_hpsi(evr_sg4_multi* m, const double* const* psi, co
     ++active;
   }
   if (active == 0) return set_error(EVR_ERR_ARG, "multi_hpsi: every context is skipped");
-  CUDA_TRY(cudaMemcpyAsync(m->d_params, params.data(), (size_t)m->n * sizeof(KParams), cudaMemcpyHostToDevice, s));
   int launched = 0;
   for (MGroup& g : m->groups) {  // one after the other: they share the scratch slabs
     const MItem* items = g.d_items;
@@ -1646,7 +1718,7 @@ extern "C" int evr_sg4_multi_hpsi(evr_sg4_multi* m, const double* const* psi, co
       std::vector<MItem> sub;
       sub.reserve(g.sorted.size());
       for (const MItem& q : g.sorted)
-        if (psi[q.ctx]) sub.push_back(q);
+        if (psi[g.ctx_of[q.ctx]]) sub.push_back(q);
       if (!sub.empty())
         CUDA_TRY(cudaMemcpyAsync(g.d_sub, sub.data(), sub.size() * sizeof(MItem), cudaMemcpyHostToDevice, s));
       CUDA_TRY(cudaStreamSynchronize(s));  // `sub` leaves scope
@@ -1655,7 +1727,7 @@ extern "C" int evr_sg4_multi_hpsi(evr_sg4_multi* m, const double* const* psi, co
     }
     if (n_items == 0) continue;
     CUDA_TRY(cudaMemsetAsync(g.d_counter, 0, sizeof(unsigned int), s));
-    launch_multi(g.geo, g.grid, (size_t)g.smem_doubles * 8, s, m->d_params, items, n_items, 0, g.d_counter);
+    launch_group(g, params, items, n_items, s);
     CUDA_TRY(cudaGetLastError());
     ++launched;
   }
@@ -1666,16 +1738,16 @@ extern "C" int evr_sg4_multi_hpsi(evr_sg4_multi* m, const double* const* psi, co
                            Esc ? Esc[k] : 1.0, s);
     if (rc) return rc;
   }
-  // `params` is pageable: the copy above is staged before cudaMemcpyAsync returns
   m->last_launches = launched + 2LL * active;
   return EVR_OK;
 }
 
-// Parameter blocks of every context bound to fixed vectors (psi[k] -> hpsi[k],
-// ld = nb0*N, in slot 0 or 1), uploaded once: multi_launch_bound then enqueues
-// kernels and memsets only, so a caller can record it in a CUDA graph.  The
-// same parameters, items and kernels as evr_sg4_multi_hpsi with every
-// context active, so the same bits.
+// Parameters of every context bound to fixed vectors (psi[k] -> hpsi[k],
+// ld = nb0*N, in binding 0 or 1), formed once: multi_launch_bound then
+// enqueues kernels and memsets only, so a caller can record it in a CUDA graph
+// (the recording keeps the launches' parameter blocks by value).  The same
+// parameters, items and kernels as evr_sg4_multi_hpsi with every context
+// active, so the same bits.
 int evr::multi_bind(evr_sg4_multi* m, int slot, const double* const* psi, double* const* hpsi) {
   if (!m || slot < 0 || slot > 1 || !psi || !hpsi) return set_error(EVR_ERR_ARG, "multi_bind: bad arguments");
   std::vector<KParams> params(m->n);
@@ -1694,19 +1766,18 @@ int evr::multi_bind(evr_sg4_multi* m, int slot, const double* const* psi, double
     p.counter = nullptr;
     p.items = nullptr;
   }
-  if (!m->d_pslot[slot]) CUDA_TRY(cudaMalloc(&m->d_pslot[slot], (size_t)m->n * sizeof(KParams)));
-  CUDA_TRY(cudaMemcpy(m->d_pslot[slot], params.data(), (size_t)m->n * sizeof(KParams), cudaMemcpyHostToDevice));
+  m->pslot[slot].swap(params);
   return EVR_OK;
 }
 
 int evr::multi_launch_bound(evr_sg4_multi* m, int slot, const double* const* psi, double* const* hpsi,
                             const double* E0, const double* Esc, void* stream) {
   cudaStream_t s = (cudaStream_t)stream;
-  if (!m->d_pslot[slot]) return set_error(EVR_ERR_STATE, "multi_launch_bound: slot %d is not bound", slot);
+  if (slot < 0 || slot > 1 || m->pslot[slot].empty())
+    return set_error(EVR_ERR_STATE, "multi_launch_bound: binding %d is not set", slot);
   for (MGroup& g : m->groups) {
     CUDA_TRY(cudaMemsetAsync(g.d_counter, 0, sizeof(unsigned int), s));
-    launch_multi(g.geo, g.grid, (size_t)g.smem_doubles * 8, s, m->d_pslot[slot], g.d_items, (int)g.sorted.size(), 0,
-                 g.d_counter);
+    launch_group(g, m->pslot[slot], g.d_items, (int)g.sorted.size(), s);
     CUDA_TRY(cudaGetLastError());
   }
   for (int k = 0; k < m->n; ++k) {
@@ -1846,6 +1917,7 @@ struct evr::FieldPair {
   int grid = 0;
   int nrhs = 1;
   long long N = 0;
+  KParams ps[2];               // the pair's parameters (slots 0 and 1 of its one launch group)
 };
 
 // Chunk sums of both operators: thread t = (op, chunk, virtual column v),
@@ -1894,8 +1966,8 @@ int evr::field_pair_create(evr_sg4_ctx* a, evr_sg4_ctx* b, int transpose, int nr
     return set_error(EVR_ERR_CUDA, "field pair: device allocation failed");
   }
   evr_sg4_multi* m = f->m;
-  const MGroup& g = m->groups[0];  // one basis, one launch group
-  KParams ps[2];
+  const MGroup& g = m->groups[0];  // one basis, one launch group: context k in slot k
+  KParams* ps = f->ps;
   for (int k = 0; k < 2; ++k) {
     ps[k] = make_params(cs[k], 2 * nrhs, 1, f->x, 2 * a->N, nullptr, 2 * a->N, 1.0);
     ps[k].transpose = m->transpose;
@@ -1907,11 +1979,10 @@ int evr::field_pair_create(evr_sg4_ctx* a, evr_sg4_ctx* b, int transpose, int nr
     ps[k].counter = nullptr;
     ps[k].items = nullptr;
   }
-  if (cudaMemcpy(m->d_params, ps, sizeof(ps), cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemset(g.d_counter, 0, sizeof(unsigned int)) != cudaSuccess) {
+  if (cudaMemset(g.d_counter, 0, sizeof(unsigned int)) != cudaSuccess) {
     cudaGetLastError();
     field_pair_destroy(f);
-    return set_error(EVR_ERR_CUDA, "field pair: parameter upload failed");
+    return set_error(EVR_ERR_CUDA, "field pair: counter reset failed");
   }
   // enough CTAs for every item, so small operators leave SMs to other streams
   f->grid = (int)std::min<size_t>((size_t)g.grid, std::max<size_t>(1, g.sorted.size()));
@@ -1932,7 +2003,7 @@ int evr::field_pair_apply(FieldPair* f, void* stream) {
   evr_sg4_multi* m = f->m;
   evr_sg4_ctx* c = m->ctxs[0];
   const MGroup& g = m->groups[0];
-  launch_multi(g.geo, f->grid, (size_t)g.smem_doubles * 8, s, m->d_params, g.d_items, (int)g.sorted.size(), 0,
+  launch_multi(g.geo, f->grid, (size_t)g.smem_doubles * 8, s, f->ps, 2, g.d_items, (int)g.sorted.size(), 0,
                g.d_counter);
   // 64-thread blocks: the Neumaier sums are FP64 chains, and GB300's FP64
   // pipe (about two operations per clock per SM) wants them on many SMs

@@ -1,11 +1,15 @@
-// sg4_items.cu -- the persistent H.psi kernels of one launch geometry.
-// Compiled once per geometry (EVR_GEO = 0 wide, 1 narrow, 2 mid), in
-// parallel, so each translation unit instantiates one pair of kernels; the
-// host code in sg4_device.cu reaches them through the GeoKernels tables.
+// sg4_items.cu -- one persistent H.psi kernel of one launch geometry.
+// Compiled once per (geometry, kind), in parallel: EVR_GEO = 0 wide, 1 narrow,
+// 2 mid; EVR_KIND = 0 the single-context kernel, 1 and 2 the merged kernel
+// with the small and the large parameter block.  The host code in
+// sg4_device.cu reaches them through the entries defined here.
 #include "sg4_items.cuh"
 
 #ifndef EVR_GEO
 #error "compile with -DEVR_GEO=0 (wide), 1 (narrow) or 2 (mid)"
+#endif
+#ifndef EVR_KIND
+#error "compile with -DEVR_KIND=0 (single context), 1 (merged, small block) or 2 (merged, large block)"
 #endif
 
 namespace evr {
@@ -13,45 +17,67 @@ namespace evr {
 #if EVR_GEO == 0
 #define EVR_G_CTAS EVR_WIDE_CTAS
 #define EVR_G_FMAX EVR_WIDE_FMAX
-#define EVR_G_TABLE geo_kernels_wide
 #elif EVR_GEO == 1
 #define EVR_G_CTAS EVR_NARROW_CTAS
 #define EVR_G_FMAX EVR_NARROW_FMAX
-#define EVR_G_TABLE geo_kernels_narrow
 #else
 #define EVR_G_CTAS EVR_MID_CTAS
 #define EVR_G_FMAX EVR_MID_FMAX
-#define EVR_G_TABLE geo_kernels_mid
 #endif
 
-static void g_batched(unsigned grid, size_t smem, cudaStream_t s, const KParams& p) {
-  hpsi_batched_kernel<EVR_G_CTAS, EVR_G_FMAX><<<grid, EVR_CTA_THREADS, smem, s>>>(p);
+#if EVR_KIND == 0
+
+#define EVR_K_KERNEL hpsi_batched_kernel<EVR_G_CTAS, EVR_G_FMAX>
+static void k_launch(unsigned grid, size_t smem, cudaStream_t s, const KParams& p) {
+  EVR_K_KERNEL<<<grid, EVR_CTA_THREADS, smem, s>>>(p);
 }
 
-static void g_multi(unsigned grid, size_t smem, cudaStream_t s, const KParams* ps, const MItem* items, int n_items,
-                    int item_base, unsigned int* counter) {
-  hpsi_multi_kernel<EVR_G_CTAS, EVR_G_FMAX><<<grid, EVR_CTA_THREADS, smem, s>>>(ps, items, n_items, item_base, counter);
+#else
+
+#define EVR_K_CAP (EVR_KIND == 1 ? EVR_PB_SMALL : EVR_PB_LARGE)
+#define EVR_K_KERNEL hpsi_multi_kernel<EVR_G_CTAS, EVR_G_FMAX, EVR_K_CAP>
+static void k_launch(unsigned grid, size_t smem, cudaStream_t s, const ParamBlock<EVR_K_CAP>& P, const MItem* items,
+                     int n_items, int item_base, unsigned int* counter) {
+  EVR_K_KERNEL<<<grid, EVR_CTA_THREADS, smem, s>>>(P, items, n_items, item_base, counter);
 }
 
-static cudaError_t g_static_smem(size_t* batched, size_t* multi) {
-  cudaFuncAttributes a, b;
-  cudaError_t e = cudaFuncGetAttributes(&a, hpsi_batched_kernel<EVR_G_CTAS, EVR_G_FMAX>);
-  if (e == cudaSuccess) e = cudaFuncGetAttributes(&b, hpsi_multi_kernel<EVR_G_CTAS, EVR_G_FMAX>);
-  if (e != cudaSuccess) return e;
-  *batched = a.sharedSizeBytes;
-  *multi = b.sharedSizeBytes;
-  return cudaSuccess;
-}
+#endif
 
-static cudaError_t g_set_smem(int bytes) {
-  cudaError_t e = cudaFuncSetAttribute(hpsi_batched_kernel<EVR_G_CTAS, EVR_G_FMAX>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(hpsi_multi_kernel<EVR_G_CTAS, EVR_G_FMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             bytes);
+static cudaError_t k_static_smem(size_t* bytes) {
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, EVR_K_KERNEL);
+  if (e == cudaSuccess) *bytes = a.sharedSizeBytes;
   return e;
 }
 
-const GeoKernels EVR_G_TABLE = {EVR_G_CTAS, g_batched, g_multi, g_static_smem, g_set_smem};
+static cudaError_t k_set_smem(int bytes) {
+  return cudaFuncSetAttribute(EVR_K_KERNEL, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+#if EVR_KIND == 0
+#if EVR_GEO == 0
+const BatchedEntry batched_wide = {k_launch, k_static_smem, k_set_smem};
+#elif EVR_GEO == 1
+const BatchedEntry batched_narrow = {k_launch, k_static_smem, k_set_smem};
+#else
+const BatchedEntry batched_mid = {k_launch, k_static_smem, k_set_smem};
+#endif
+#elif EVR_KIND == 1
+#if EVR_GEO == 0
+const MultiEntry<EVR_PB_SMALL> multi_small_wide = {k_launch, k_static_smem, k_set_smem};
+#elif EVR_GEO == 1
+const MultiEntry<EVR_PB_SMALL> multi_small_narrow = {k_launch, k_static_smem, k_set_smem};
+#else
+const MultiEntry<EVR_PB_SMALL> multi_small_mid = {k_launch, k_static_smem, k_set_smem};
+#endif
+#else
+#if EVR_GEO == 0
+const MultiEntry<EVR_PB_LARGE> multi_large_wide = {k_launch, k_static_smem, k_set_smem};
+#elif EVR_GEO == 1
+const MultiEntry<EVR_PB_LARGE> multi_large_narrow = {k_launch, k_static_smem, k_set_smem};
+#else
+const MultiEntry<EVR_PB_LARGE> multi_large_mid = {k_launch, k_static_smem, k_set_smem};
+#endif
+#endif
 
 }  // namespace evr

@@ -934,12 +934,25 @@ __global__ void __launch_bounds__(EVR_CTA_THREADS, MINB) hpsi_batched_kernel(KPa
   }
 }
 
-// Items of several contexts in one launch: each item names its context,
-// whose parameter block is copied to shared memory before the item runs.
+// The parameter blocks of a merged launch, passed by value: EVR_PB_SMALL
+// contexts (the per-term path, the field-driven pairs) or EVR_PB_LARGE (the
+// multi-context plans split their contexts into launches of at most this
+// many).  17.5 KB at the larger size, inside the 32 KB kernel-parameter limit.
+enum { EVR_PB_SMALL = 2, EVR_PB_LARGE = 64 };
+template <int CAP>
+struct ParamBlock {
+  KParams p[CAP];
+};
+
+// Items of several contexts in one launch: each item names its context's slot
+// in the parameter block.  The block is a __grid_constant__ kernel parameter,
+// so a context's fields are read from the constant bank in place, as the
+// single-context kernel reads its own (a copy in registers spilled to local
+// memory: 3 % slower on the 64-instance draw, 17 % on its small contexts).
 // With a counter the CTAs pull items until the list is empty; without one
 // (the per-term path) CTA b runs item item_base + b.
-template <int MINB, int FMAX>
-__global__ void __launch_bounds__(EVR_CTA_THREADS, MINB) hpsi_multi_kernel(const KParams* __restrict__ ps,
+template <int MINB, int FMAX, int CAP>
+__global__ void __launch_bounds__(EVR_CTA_THREADS, MINB) hpsi_multi_kernel(const __grid_constant__ ParamBlock<CAP> P,
                                                               const MItem* __restrict__ items, int n_items,
                                                               int item_base, unsigned int* counter) {
   extern __shared__ double smem[];
@@ -952,26 +965,28 @@ __global__ void __launch_bounds__(EVR_CTA_THREADS, MINB) hpsi_multi_kernel(const
     __syncthreads();
     if (idx >= n_items) break;
     const MItem m = items[idx];
-    // a private copy of the context's parameters: the compiler keeps the
-    // fields it needs in registers, which no store to the shared work arrays
-    // can alias (a copy in shared memory was reloaded in the inner loops:
-    // 1 % slower RK4, 1.5 % slower 64-instance draw)
-    const KParams p = ps[m.ctx];
-    run_item<FMAX>(p, it, smem, m.term, m.rhs0);
+    run_item<FMAX>(P.p[m.ctx], it, smem, m.term, m.rhs0);
   }
 }
 
-
-// The kernels of one launch geometry, compiled in their own translation unit
-// (sg4_items.cu with EVR_GEO = 0 wide, 1 narrow, 2 mid).
-struct GeoKernels {
-  int ctas;  // resident CTAs per SM
-  void (*batched)(unsigned grid, size_t smem, cudaStream_t s, const KParams& p);
-  void (*multi)(unsigned grid, size_t smem, cudaStream_t s, const KParams* ps, const MItem* items, int n_items,
-                int item_base, unsigned int* counter);
-  cudaError_t (*static_smem)(size_t* batched, size_t* multi);  // static shared bytes of the two kernels
-  cudaError_t (*set_smem)(int bytes);                           // their dynamic shared-memory limit
+// One kernel of one launch geometry, each compiled in its own translation
+// unit (sg4_items.cu with EVR_GEO = 0 wide, 1 narrow, 2 mid and EVR_KIND = 0
+// single context, 1 and 2 merged with the small and large parameter blocks);
+// the host code in sg4_device.cu assembles them per geometry.
+struct BatchedEntry {
+  void (*launch)(unsigned grid, size_t smem, cudaStream_t s, const KParams& p);
+  cudaError_t (*static_smem)(size_t* bytes);  // static shared bytes
+  cudaError_t (*set_smem)(int bytes);         // the dynamic shared-memory limit
 };
-extern const GeoKernels geo_kernels_wide, geo_kernels_narrow, geo_kernels_mid;
+template <int CAP>
+struct MultiEntry {
+  void (*launch)(unsigned grid, size_t smem, cudaStream_t s, const ParamBlock<CAP>& P, const MItem* items,
+                 int n_items, int item_base, unsigned int* counter);
+  cudaError_t (*static_smem)(size_t* bytes);
+  cudaError_t (*set_smem)(int bytes);
+};
+extern const BatchedEntry batched_wide, batched_narrow, batched_mid;
+extern const MultiEntry<EVR_PB_SMALL> multi_small_wide, multi_small_narrow, multi_small_mid;
+extern const MultiEntry<EVR_PB_LARGE> multi_large_wide, multi_large_narrow, multi_large_mid;
 
 }  // namespace evr

@@ -100,6 +100,19 @@ def test_multi_two_launch_groups():
     torch.cuda.synchronize()
     assert plan.last_launches() == 1 + 2 * 2
     assert torch.equal(outs2[0], ref[0]) and torch.equal(outs2[2], ref[2]) and torch.all(outs2[1] == 7.0)
+    groups = plan.groups()
+    assert len(groups) == 2 and groups[0][0] == 1 and all(n > 0 for _, n in groups)
+    # a geometry named on every context of a group is the group's; same bits in each
+    for geo in (0, 2):
+        ops[1].set_plan(geo)
+        p2 = MultiOp(ops, nrhs)
+        assert p2.groups()[1][0] == geo and p2.groups()[0][0] == 1
+        outs3 = [torch.full_like(P, float("nan")) for P in psis]
+        p2.hpsi(psis, outs3)
+        torch.cuda.synchronize()
+        for k in range(3):
+            assert torch.equal(outs3[k], ref[k]), (geo, k)
+    ops[1].set_plan(-1)
 
 
 def test_multi_skips_null_contexts_and_leaves_contexts_usable():
