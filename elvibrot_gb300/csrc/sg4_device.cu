@@ -100,23 +100,17 @@ namespace evr {
 // The kernels of launch geometry geo (0 wide, 1 narrow, 2 mid).
 struct GeoKernels {
   int ctas;  // resident CTAs per SM
-  const BatchedEntry* batched;
-  const MultiEntry<EVR_PB_SMALL>* multi_small;
-  const MultiEntry<EVR_PB_LARGE>* multi_large;
+  const MultiEntry<EVR_PB_SMALL>* small;
+  const MultiEntry<EVR_PB_LARGE>* large;
 };
 static const GeoKernels& geo_kernels(int geo) {
-  static const GeoKernels t[3] = {
-      {EVR_WIDE_CTAS, &batched_wide, &multi_small_wide, &multi_large_wide},
-      {EVR_NARROW_CTAS, &batched_narrow, &multi_small_narrow, &multi_large_narrow},
-      {EVR_MID_CTAS, &batched_mid, &multi_small_mid, &multi_large_mid}};
+  static const GeoKernels t[3] = {{EVR_WIDE_CTAS, &multi_small_wide, &multi_large_wide},
+                                  {EVR_NARROW_CTAS, &multi_small_narrow, &multi_large_narrow},
+                                  {EVR_MID_CTAS, &multi_small_mid, &multi_large_mid}};
   return t[geo == 1 ? 1 : (geo == 2 ? 2 : 0)];
 }
 
-static void launch_batched(int geo, unsigned grid, size_t smem, cudaStream_t s, const KParams& p) {
-  geo_kernels(geo).batched->launch(grid, smem, s, p);
-}
-
-// A merged launch over n_ctx <= EVR_PB_LARGE contexts whose parameters are
+// A launch over n_ctx <= EVR_PB_LARGE contexts whose parameters are
 // ps[0..n_ctx) (host memory; items name their slot).  The launch copies the
 // block, so ps may change as soon as this returns, and a CUDA graph that
 // records the launch keeps the values of the recording.
@@ -125,33 +119,37 @@ static void launch_multi(int geo, unsigned grid, size_t smem, cudaStream_t s, co
   if (n_ctx <= EVR_PB_SMALL) {
     ParamBlock<EVR_PB_SMALL> P;
     std::copy(ps, ps + n_ctx, P.p);
-    geo_kernels(geo).multi_small->launch(grid, smem, s, P, items, n_items, item_base, counter);
+    geo_kernels(geo).small->launch(grid, smem, s, P, items, n_items, item_base, counter);
   } else {
-    static thread_local ParamBlock<EVR_PB_LARGE> P;  // 17.5 KB: not on the stack
+    static thread_local ParamBlock<EVR_PB_LARGE> P;  // 16 KB: not on the stack
     std::copy(ps, ps + n_ctx, P.p);
-    geo_kernels(geo).multi_large->launch(grid, smem, s, P, items, n_items, item_base, counter);
+    geo_kernels(geo).large->launch(grid, smem, s, P, items, n_items, item_base, counter);
   }
+}
+
+// One context's persistent launch: the CTAs pull items[0..n_items) through
+// the counter (zeroed by the caller).
+static void launch_single(int geo, unsigned grid, size_t smem, cudaStream_t s, const KParams& p, const MItem* items,
+                          int n_items, unsigned int* counter) {
+  launch_multi(geo, grid, smem, s, &p, 1, items, n_items, 0, counter);
 }
 
 static int geo_ctas(int geo) { return geo_kernels(geo).ctas; }
 
 // Static shared memory plus the 1 KB the driver reserves per CTA, rounded up
-// to 256 bytes (queried once): the largest of a geometry's three item kernels,
-// so each of them keeps the geometry's CTAs per SM (sized for the
-// single-context kernel alone, a wide merged launch once kept three CTAs per
-// SM instead of four and the RK4 forward ran 8 % slower).
+// to 256 bytes (queried once): the larger of a geometry's two kernels, so
+// both keep the geometry's CTAs per SM.
 static int smem_slack(int geo) {
   static const std::vector<int> slack = [] {
     std::vector<int> v(3, 4096);
     for (int g = 0; g < 3; ++g) {
-      size_t b = 0, ms = 0, ml = 0;
+      size_t a = 0, b = 0;
       const GeoKernels& k = geo_kernels(g);
-      if (k.batched->static_smem(&b) != cudaSuccess || k.multi_small->static_smem(&ms) != cudaSuccess ||
-          k.multi_large->static_smem(&ml) != cudaSuccess) {
+      if (k.small->static_smem(&a) != cudaSuccess || k.large->static_smem(&b) != cudaSuccess) {
         cudaGetLastError();
         continue;
       }
-      v[g] = (int)((std::max(b, std::max(ms, ml)) + 1024 + 255) / 256 * 256);
+      v[g] = (int)((std::max(a, b) + 1024 + 255) / 256 * 256);
     }
     return v;
   }();
@@ -169,9 +167,8 @@ static cudaError_t set_smem_attributes() {
   for (int g = 0; g < 3 && e == cudaSuccess; ++g) {
     const GeoKernels& k = geo_kernels(g);
     const int bytes = geo_smem_bytes(g);
-    e = k.batched->set_smem(bytes);
-    if (e == cudaSuccess) e = k.multi_small->set_smem(bytes);
-    if (e == cudaSuccess) e = k.multi_large->set_smem(bytes);
+    e = k.small->set_smem(bytes);
+    if (e == cudaSuccess) e = k.large->set_smem(bytes);
   }
   return e;
 }
@@ -398,7 +395,7 @@ struct evr_sg4_ctx {
   double* d_x = nullptr;
   int* d_x_off = nullptr;
   TermInfo* d_terms = nullptr;
-  Item* d_items = nullptr;
+  MItem* d_items = nullptr;          // the plan's items, decreasing cost (slot 0)
   MItem* d_plain_items = nullptr;    // term-ordered (context 0) items for the per-term path
   size_t items_cap = 0;
   int items_nrhs = -1;               // items built for this virtual nrhs
@@ -922,6 +919,13 @@ static void plan_items(evr_sg4_ctx* c, int nrhs_v, std::vector<Item>& items, std
   c->grid = geo_ctas(geo) * c->num_sms;
 }
 
+// a single context's device work list: every item in slot 0
+static std::vector<MItem> slot0_items(const std::vector<Item>& items) {
+  std::vector<MItem> out(items.size());
+  for (size_t k = 0; k < items.size(); ++k) out[k] = MItem{0, items[k].term, items[k].rhs0, 0};
+  return out;
+}
+
 static int build_items(evr_sg4_ctx* c, int nrhs_v) {
   if (c->items_nrhs == nrhs_v) return EVR_OK;
   std::vector<Item> items, sorted;
@@ -952,13 +956,15 @@ static int build_items(evr_sg4_ctx* c, int nrhs_v) {
   if (need > c->items_cap) {
     if (c->d_items) cudaFree(c->d_items);
     c->d_items = nullptr;
-    CUDA_TRY(cudaMalloc(&c->d_items, need * sizeof(Item)));
+    CUDA_TRY(cudaMalloc(&c->d_items, need * sizeof(MItem)));
     c->items_cap = need;
   }
-  CUDA_TRY(cudaMemcpy(c->d_items, sorted.data(), sorted.size() * sizeof(Item), cudaMemcpyHostToDevice));
   {
-    std::vector<MItem> pl(items.size());
-    for (size_t k = 0; k < items.size(); ++k) pl[k] = MItem{0, items[k].term, items[k].rhs0, 0};
+    const std::vector<MItem> ms = slot0_items(sorted);
+    CUDA_TRY(cudaMemcpy(c->d_items, ms.data(), ms.size() * sizeof(MItem), cudaMemcpyHostToDevice));
+  }
+  {
+    const std::vector<MItem> pl = slot0_items(items);
     if (c->d_plain_items) cudaFree(c->d_plain_items);
     c->d_plain_items = nullptr;
     CUDA_TRY(cudaMalloc(&c->d_plain_items, std::max<size_t>(1, pl.size()) * sizeof(MItem)));
@@ -1019,8 +1025,6 @@ static KParams make_params(evr_sg4_ctx* c, int nrhs_v, int cshift, const double*
   p.nrhs_v = nrhs_v;
   p.cshift = cshift;
   p.terms = c->d_terms;
-  p.n_items = c->n_items;
-  p.counter = c->d_counter;
   p.map = c->d_map;
   p.mats = c->d_mats;
   p.mat_off = c->d_mat_off;
@@ -1088,17 +1092,15 @@ static int hpsi_common(evr_sg4_ctx* c, int nrhs, int cshift, const double* psi, 
       if ((rc = eval_fields(c, g0, g1, c->V_nterms > 0, c->d_G1 || c->d_G0, s))) return rc;
       CUDA_TRY(cudaMemsetAsync(c->d_counter, 0, sizeof(unsigned int), s));
       KParams q = p;
-      q.items = c->d_items + c->slice_item[k];
-      q.n_items = c->slice_item[k + 1] - c->slice_item[k];
       q.fbase = g0;
-      launch_batched(c->geo, c->grid, smem, s, q);
+      launch_single(c->geo, c->grid, smem, s, q, c->d_items + c->slice_item[k],
+                    c->slice_item[k + 1] - c->slice_item[k], c->d_counter);
       CUDA_TRY(cudaGetLastError());
       launches += 2;
     }
   } else if (!plain) {
     CUDA_TRY(cudaMemsetAsync(c->d_counter, 0, sizeof(unsigned int), s));
-    p.items = c->d_items;
-    launch_batched(c->geo, c->grid, smem, s, p);
+    launch_single(c->geo, c->grid, smem, s, p, c->d_items, c->n_items, c->d_counter);
     CUDA_TRY(cudaGetLastError());
     launches = 1;
   } else {
@@ -1330,7 +1332,7 @@ extern "C" int evr_probe_fp64_pipes(double* dfma_tflops, double* dmma_tflops, do
 // memory budget (a host program whose allocator owns every device byte and
 // forbids allocations behind its back), or a real-time loop that must stay
 // out of the driver's allocator, whose calls can synchronise the device.
-// evr_sg4_hpsi_noalloc gives them the batched kernel with all of its scratch
+// evr_sg4_hpsi_noalloc gives them the persistent kernel with all of its scratch
 // -- the work counter, the term table of this call's plan, the work list,
 // the per-term contributions, the chunk partials of the ordered accumulation
 // and the per-CTA slabs for terms larger than shared memory -- carved from
@@ -1400,7 +1402,7 @@ extern "C" int evr_sg4_hpsi_noalloc(evr_sg4_ctx* c, int nrhs, const double* psi,
   auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
   const size_t off_terms = 256;
   const size_t off_items = off_terms + up(terms.size() * sizeof(TermInfo));
-  const size_t off_contrib = off_items + up(sorted.size() * sizeof(Item));
+  const size_t off_contrib = off_items + up(sorted.size() * sizeof(MItem));
   const size_t off_part = off_contrib + up((size_t)c->z.sum_nb * nrhs_v * 8);
   const size_t off_slabs = off_part + up((size_t)c->n_chunks * nrhs_v * 16);
   const long long per_cta = max_need > smem_doubles ? max_need : 0;
@@ -1419,18 +1421,17 @@ extern "C" int evr_sg4_hpsi_noalloc(evr_sg4_ctx* c, int nrhs, const double* psi,
   // returns, so they may go out of scope when this call does
   CUDA_TRY(cudaMemcpyAsync(base + off_terms, terms.data(), terms.size() * sizeof(TermInfo), cudaMemcpyHostToDevice,
                            s));
-  CUDA_TRY(cudaMemcpyAsync(base + off_items, sorted.data(), sorted.size() * sizeof(Item), cudaMemcpyHostToDevice, s));
+  const std::vector<MItem> ms = slot0_items(sorted);
+  CUDA_TRY(cudaMemcpyAsync(base + off_items, ms.data(), ms.size() * sizeof(MItem), cudaMemcpyHostToDevice, s));
   CUDA_TRY(cudaMemsetAsync(base, 0, sizeof(unsigned int), s));
   KParams p = make_params(c, nrhs_v, 0, psi, ldpsi, hpsi, ldh, 1.0);
   p.terms = (const TermInfo*)(base + off_terms);
-  p.items = (const Item*)(base + off_items);
-  p.n_items = (int)sorted.size();
-  p.counter = (unsigned int*)base;
   p.smem_doubles = smem_doubles;
   p.contrib = (double*)(base + off_contrib);
   p.gscratch = per_cta ? (double*)(base + off_slabs) : nullptr;
   p.scratch_per_cta = per_cta;
-  launch_batched(geo, grid, (size_t)smem_doubles * 8, s, p);
+  launch_single(geo, grid, (size_t)smem_doubles * 8, s, p, (const MItem*)(base + off_items), (int)ms.size(),
+                (unsigned int*)base);
   CUDA_TRY(cudaGetLastError());
   int rc = launch_reduce(c, p.contrib, (double2*)(base + off_part), nrhs_v, 0, psi, ldpsi, hpsi, ldh, E0, Esc, s);
   if (rc) return rc;
@@ -1705,8 +1706,6 @@ extern "C" int evr_sg4_multi_hpsi(evr_sg4_multi* m, const double* const* psi, co
     p.contrib = m->d_contrib[k];
     p.gscratch = m->d_scratch;
     p.scratch_per_cta = g.scratch_per_cta;
-    p.counter = nullptr;
-    p.items = nullptr;
     ++active;
   }
   if (active == 0) return set_error(EVR_ERR_ARG, "multi_hpsi: every context is skipped");
@@ -1763,8 +1762,6 @@ int evr::multi_bind(evr_sg4_multi* m, int slot, const double* const* psi, double
     p.contrib = m->d_contrib[k];
     p.gscratch = m->d_scratch;
     p.scratch_per_cta = g.scratch_per_cta;
-    p.counter = nullptr;
-    p.items = nullptr;
   }
   m->pslot[slot].swap(params);
   return EVR_OK;
@@ -1820,10 +1817,10 @@ extern "C" int evr_sg4_hpsi_multi(int n, evr_sg4_ctx* const* ctxs, const int* nr
 // ------------------------------------------------------------------------
 struct evr::BoundApply {
   evr_sg4_ctx* c = nullptr;
-  KParams p{};                  // the plan's parameters (items, terms, counter, scratch of its own)
-  int geo = 0, grid = 0, nrhs_v = 0;
+  KParams p{};                  // the plan's parameters (terms, scratch of its own)
+  int geo = 0, grid = 0, nrhs_v = 0, n_items = 0;
   TermInfo* d_terms = nullptr;
-  Item* d_items = nullptr;
+  MItem* d_items = nullptr;
   unsigned int* d_counter = nullptr;
   double* d_contrib = nullptr;
   double* d_part = nullptr;
@@ -1833,7 +1830,7 @@ struct evr::BoundApply {
   long long ld = 0;
 };
 
-// The same work list, geometry and batched kernel as evr_sg4_apply's plan for
+// The same work list, geometry and kernel as evr_sg4_apply's plan for
 // nrhs columns (plan_sorted), in buffers of its own.
 int evr::bound_apply_create(evr_sg4_ctx* c, int nrhs, int transpose, const double* psi, double* hpsi,
                             BoundApply** out) {
@@ -1860,21 +1857,20 @@ int evr::bound_apply_create(evr_sg4_ctx* c, int nrhs, int transpose, const doubl
     return set_error(EVR_ERR_CUDA, "bound apply: %s", what);
   };
   if (cudaMalloc(&b->d_terms, terms.size() * sizeof(TermInfo)) != cudaSuccess ||
-      cudaMalloc(&b->d_items, std::max<size_t>(1, sorted.size()) * sizeof(Item)) != cudaSuccess ||
+      cudaMalloc(&b->d_items, std::max<size_t>(1, sorted.size()) * sizeof(MItem)) != cudaSuccess ||
       cudaMalloc(&b->d_counter, sizeof(unsigned int)) != cudaSuccess ||
       cudaMalloc(&b->d_contrib, (size_t)c->z.sum_nb * b->nrhs_v * 8) != cudaSuccess ||
       cudaMalloc(&b->d_part, (size_t)c->n_chunks * b->nrhs_v * 16) != cudaSuccess ||
       (per_cta && cudaMalloc(&b->d_scratch, (size_t)per_cta * b->grid * 8) != cudaSuccess))
     return fail("device allocation failed");
   if (cudaMemcpy(b->d_terms, terms.data(), terms.size() * sizeof(TermInfo), cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(b->d_items, sorted.data(), sorted.size() * sizeof(Item), cudaMemcpyHostToDevice) != cudaSuccess)
+      cudaMemcpy(b->d_items, slot0_items(sorted).data(), sorted.size() * sizeof(MItem), cudaMemcpyHostToDevice) !=
+          cudaSuccess)
     return fail("upload failed");
+  b->n_items = (int)sorted.size();
   KParams p = make_params(c, b->nrhs_v, 0, psi, b->ld, hpsi, b->ld, 1.0);
   p.transpose = transpose ? 1 : 0;
   p.terms = b->d_terms;
-  p.items = b->d_items;
-  p.n_items = (int)sorted.size();
-  p.counter = b->d_counter;
   p.smem_doubles = smem_doubles;
   p.contrib = b->d_contrib;
   p.gscratch = b->d_scratch;
@@ -1895,7 +1891,7 @@ void evr::bound_apply_destroy(BoundApply* b) {
 int evr::bound_apply_launch(BoundApply* b, void* stream) {
   cudaStream_t s = (cudaStream_t)stream;
   CUDA_TRY(cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned int), s));
-  launch_batched(b->geo, b->grid, (size_t)b->p.smem_doubles * 8, s, b->p);
+  launch_single(b->geo, b->grid, (size_t)b->p.smem_doubles * 8, s, b->p, b->d_items, b->n_items, b->d_counter);
   CUDA_TRY(cudaGetLastError());
   return launch_reduce(b->c, b->d_contrib, (double2*)b->d_part, b->nrhs_v, 0, b->psi, b->ld, b->hpsi, b->ld, 0.0,
                        1.0, s);
@@ -1976,8 +1972,6 @@ int evr::field_pair_create(evr_sg4_ctx* a, evr_sg4_ctx* b, int transpose, int nr
     ps[k].contrib = m->d_contrib[k];
     ps[k].gscratch = m->d_scratch;
     ps[k].scratch_per_cta = g.scratch_per_cta;
-    ps[k].counter = nullptr;
-    ps[k].items = nullptr;
   }
   if (cudaMemset(g.d_counter, 0, sizeof(unsigned int)) != cudaSuccess) {
     cudaGetLastError();

@@ -47,7 +47,7 @@ int field_pair_apply(FieldPair* f, void* stream);
 FieldPairView field_pair_view(const FieldPair* f);
 // One context applied to fixed device buffers (nrhs real columns, ld nb0*N,
 // E0 = 0, Esc = 1) with a plan and scratch of its own (the work list and
-// batched kernel evr_sg4_apply would use): a launch enqueues kernels and a
+// kernel evr_sg4_apply would use): a launch enqueues kernels and a
 // memset only (graph-recordable).
 struct BoundApply;
 int bound_apply_create(evr_sg4_ctx* c, int nrhs, int transpose, const double* psi, double* hpsi, BoundApply** out);

@@ -1,15 +1,16 @@
-// sg4_items.cu -- one persistent H.psi kernel of one launch geometry.
-// Compiled once per (geometry, kind), in parallel: EVR_GEO = 0 wide, 1 narrow,
-// 2 mid; EVR_KIND = 0 the single-context kernel, 1 and 2 the merged kernel
-// with the small and the large parameter block.  The host code in
-// sg4_device.cu reaches them through the entries defined here.
+// sg4_items.cu -- the persistent H.psi kernel of one launch geometry and one
+// parameter-block size.  Compiled once per (geometry, block), in parallel:
+// EVR_GEO = 0 wide, 1 narrow, 2 mid; EVR_KIND = 0 the small block (one
+// context, or the field-driven pairs), 1 the large block (multi-context
+// plans).  The host code in sg4_device.cu reaches them through the entries
+// defined here.
 #include "sg4_items.cuh"
 
 #ifndef EVR_GEO
 #error "compile with -DEVR_GEO=0 (wide), 1 (narrow) or 2 (mid)"
 #endif
 #ifndef EVR_KIND
-#error "compile with -DEVR_KIND=0 (single context), 1 (merged, small block) or 2 (merged, large block)"
+#error "compile with -DEVR_KIND=0 (small parameter block) or 1 (large parameter block)"
 #endif
 
 namespace evr {
@@ -25,23 +26,13 @@ namespace evr {
 #define EVR_G_FMAX EVR_MID_FMAX
 #endif
 
-#if EVR_KIND == 0
+#define EVR_K_CAP (EVR_KIND == 0 ? EVR_PB_SMALL : EVR_PB_LARGE)
+#define EVR_K_KERNEL hpsi_items_kernel<EVR_G_CTAS, EVR_G_FMAX, EVR_K_CAP>
 
-#define EVR_K_KERNEL hpsi_batched_kernel<EVR_G_CTAS, EVR_G_FMAX>
-static void k_launch(unsigned grid, size_t smem, cudaStream_t s, const KParams& p) {
-  EVR_K_KERNEL<<<grid, EVR_CTA_THREADS, smem, s>>>(p);
-}
-
-#else
-
-#define EVR_K_CAP (EVR_KIND == 1 ? EVR_PB_SMALL : EVR_PB_LARGE)
-#define EVR_K_KERNEL hpsi_multi_kernel<EVR_G_CTAS, EVR_G_FMAX, EVR_K_CAP>
 static void k_launch(unsigned grid, size_t smem, cudaStream_t s, const ParamBlock<EVR_K_CAP>& P, const MItem* items,
                      int n_items, int item_base, unsigned int* counter) {
   EVR_K_KERNEL<<<grid, EVR_CTA_THREADS, smem, s>>>(P, items, n_items, item_base, counter);
 }
-
-#endif
 
 static cudaError_t k_static_smem(size_t* bytes) {
   cudaFuncAttributes a;
@@ -55,14 +46,6 @@ static cudaError_t k_set_smem(int bytes) {
 }
 
 #if EVR_KIND == 0
-#if EVR_GEO == 0
-const BatchedEntry batched_wide = {k_launch, k_static_smem, k_set_smem};
-#elif EVR_GEO == 1
-const BatchedEntry batched_narrow = {k_launch, k_static_smem, k_set_smem};
-#else
-const BatchedEntry batched_mid = {k_launch, k_static_smem, k_set_smem};
-#endif
-#elif EVR_KIND == 1
 #if EVR_GEO == 0
 const MultiEntry<EVR_PB_SMALL> multi_small_wide = {k_launch, k_static_smem, k_set_smem};
 #elif EVR_GEO == 1

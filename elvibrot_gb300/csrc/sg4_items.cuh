@@ -85,12 +85,14 @@ static inline void mode_order(const int* nb, const int* nq, int D, int* ord) {
   }
 }
 
+// a work item (host plans)
 struct Item {
   int term;
   int rhs0;
 };
 
-// a work item of a launch over several contexts (context index first)
+// a work item of a launch: the context's slot in the launch's parameter
+// block, the Smolyak term and the first right-hand side of the block
 struct MItem {
   int ctx, term, rhs0, pad;
 };
@@ -113,10 +115,6 @@ struct KParams {
   int nrhs_v;                // virtual right-hand sides (2*nrhs for complex)
   int cshift;                // 1 for interleaved complex, else 0
   const TermInfo* terms;
-  const Item* items;
-  int n_items;
-  int item_base;             // plain path: items [item_base, item_base+gridDim.x)
-  unsigned int* counter;     // batched path: global work counter
   const int* map;
   const double* mats;
   const int* mat_off;        // [D*Lp1*8]: forward set, then transposed set
@@ -918,41 +916,28 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ter
   store_contrib(p, it, yb);
 }
 
-template <int MINB, int FMAX>
-__global__ void __launch_bounds__(EVR_CTA_THREADS, MINB) hpsi_batched_kernel(KParams p) {
-  extern __shared__ double smem[];
-  __shared__ ItemShared it;
-  __shared__ int next;
-  for (;;) {
-    if (threadIdx.x == 0) next = (int)atomicAdd(p.counter, 1u);
-    __syncthreads();
-    int idx = next;
-    __syncthreads();
-    if (idx >= p.n_items) break;
-    const Item itm = p.items[idx];
-    run_item<FMAX>(p, it, smem, itm.term, itm.rhs0);
-  }
-}
-
-// The parameter blocks of a merged launch, passed by value: EVR_PB_SMALL
-// contexts (the per-term path, the field-driven pairs) or EVR_PB_LARGE (the
+// The parameter blocks of a launch, passed by value: EVR_PB_SMALL contexts
+// (a single context, the field-driven pairs) or EVR_PB_LARGE (the
 // multi-context plans split their contexts into launches of at most this
-// many).  17.5 KB at the larger size, inside the 32 KB kernel-parameter limit.
+// many; 16 KB, inside the 32 KB kernel-parameter limit).
 enum { EVR_PB_SMALL = 2, EVR_PB_LARGE = 64 };
 template <int CAP>
 struct ParamBlock {
   KParams p[CAP];
 };
 
-// Items of several contexts in one launch: each item names its context's slot
-// in the parameter block.  The block is a __grid_constant__ kernel parameter,
-// so a context's fields are read from the constant bank in place, as the
-// single-context kernel reads its own (a copy in registers spilled to local
-// memory: 3 % slower on the 64-instance draw, 17 % on its small contexts).
+// The persistent H.psi kernel: every work item of a launch, of one or several
+// contexts; each item names its context's slot in the parameter block.  The
+// block is a __grid_constant__ kernel parameter, so a context's fields are
+// read in place from the constant bank.  Measured against the alternatives
+// (same bits): a copy of the context's parameters in registers spilled to
+// local memory (3 % slower on the 64-instance draw, 17 % on its small
+// contexts), and a kernel taking one context's parameters as a plain kernel
+// argument was 1.3 % slower on the 6-D benchmark (more spill code).
 // With a counter the CTAs pull items until the list is empty; without one
 // (the per-term path) CTA b runs item item_base + b.
 template <int MINB, int FMAX, int CAP>
-__global__ void __launch_bounds__(EVR_CTA_THREADS, MINB) hpsi_multi_kernel(const __grid_constant__ ParamBlock<CAP> P,
+__global__ void __launch_bounds__(EVR_CTA_THREADS, MINB) hpsi_items_kernel(const __grid_constant__ ParamBlock<CAP> P,
                                                               const MItem* __restrict__ items, int n_items,
                                                               int item_base, unsigned int* counter) {
   extern __shared__ double smem[];
@@ -971,21 +956,15 @@ __global__ void __launch_bounds__(EVR_CTA_THREADS, MINB) hpsi_multi_kernel(const
 
 // One kernel of one launch geometry, each compiled in its own translation
 // unit (sg4_items.cu with EVR_GEO = 0 wide, 1 narrow, 2 mid and EVR_KIND = 0
-// single context, 1 and 2 merged with the small and large parameter blocks);
-// the host code in sg4_device.cu assembles them per geometry.
-struct BatchedEntry {
-  void (*launch)(unsigned grid, size_t smem, cudaStream_t s, const KParams& p);
-  cudaError_t (*static_smem)(size_t* bytes);  // static shared bytes
-  cudaError_t (*set_smem)(int bytes);         // the dynamic shared-memory limit
-};
+// the small, 1 the large parameter block); the host code in sg4_device.cu
+// assembles them per geometry.
 template <int CAP>
 struct MultiEntry {
   void (*launch)(unsigned grid, size_t smem, cudaStream_t s, const ParamBlock<CAP>& P, const MItem* items,
                  int n_items, int item_base, unsigned int* counter);
-  cudaError_t (*static_smem)(size_t* bytes);
-  cudaError_t (*set_smem)(int bytes);
+  cudaError_t (*static_smem)(size_t* bytes);  // static shared bytes
+  cudaError_t (*set_smem)(int bytes);         // the dynamic shared-memory limit
 };
-extern const BatchedEntry batched_wide, batched_narrow, batched_mid;
 extern const MultiEntry<EVR_PB_SMALL> multi_small_wide, multi_small_narrow, multi_small_mid;
 extern const MultiEntry<EVR_PB_LARGE> multi_large_wide, multi_large_narrow, multi_large_mid;
 
