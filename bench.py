@@ -5,7 +5,9 @@ Q-dependent-G (type 10) SG4 Hamiltonian (seeded synthetic data, see
 elvibrot_gb300/configs.py).  value = right-hand-side H.psi applications per
 second with psi resident in HBM; e2e = the same through the host-pointer C
 ABI (pinned host psi copied in and H.psi copied out every step).  L2 is
-flushed (256 MB write) before every timed step.
+flushed (256 MB write) before every timed step.  The launch plan is the
+autotuner's, chosen before the warm-up (--no-tune: the automatic plan;
+--plan G,R,S: a given one); the automatic plan is timed beside it.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -146,8 +148,8 @@ class ClockSampler:
 
 
 def profile_traffic():
-    """Per-launch DRAM traffic of the batched kernel from the committed ncu summary, if present."""
-    p = os.path.join(ROOT, "profiles", "hpsi_batched_6d_l8_20rhs.txt")
+    """Per-launch DRAM traffic of the H.psi kernel from the committed ncu summary, if present."""
+    p = os.path.join(ROOT, "profiles", "hpsi_items_6d_l8_20rhs.txt")
     if not os.path.exists(p):
         return None
     m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", open(p).read())
@@ -582,6 +584,15 @@ def run_ours(args, ws, rank, local):
     def step():
         op.hpsi_dev(psi, out, stream=sh)
 
+    # the autotuner picks the launch plan before anything is timed, as the
+    # reference runs Tune_SG4threads_HPsi before its propagations and
+    # diagonalisations (SRC/sub_main/vib.f90:370,583); --no-tune keeps the
+    # automatic plan
+    tr = None
+    if args.plan:
+        op.set_plan(*[int(x) for x in args.plan.split(",")])
+    elif not args.no_tune:
+        tr = op.tune_plan(nrhs)
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -625,6 +636,23 @@ def run_ours(args, ws, rank, local):
     np.testing.assert_allclose(hh.numpy(), out.cpu().numpy(), rtol=0, atol=1e-12 * float(out.abs().max()))
     e2e_value = ws * args.steps * nrhs / e2e_t
 
+    # the automatic plan on the same workload and protocol, for comparison
+    auto = None
+    if tr is not None or args.plan:
+        op.set_plan(-1, 32, 0)
+        step()  # untimed: the first call under a new plan builds its work list
+        torch.cuda.synchronize()
+        ta = 0.0
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            step()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ta += a.elapsed_time(b) / 1e3
+        auto = {"value": ws * args.steps * nrhs / ta, "unit": UNIT, "ms_per_step": 1e3 * ta / args.steps}
+
     # plain per-term path (one launch per Smolyak term) on the same workload
     plain_steps = max(2, min(5, args.steps))
     op.hpsi_dev(psi, out, plain=True)
@@ -639,26 +667,6 @@ def run_ours(args, ws, rank, local):
         torch.cuda.synchronize()
         pt += a.elapsed_time(b) / 1e3
     plain_value = plain_steps * nrhs / pt
-
-    # the autotuner's plan for this workload (same bits; the headline keeps the automatic plan)
-    tuned = None
-    if not args.no_tune:
-        tr = op.tune_plan(nrhs)
-        op.hpsi_dev(psi, out, stream=sh)  # untimed: the first call under a new plan builds its work list
-        torch.cuda.synchronize()
-        tt = 0.0
-        for k in range(plain_steps):
-            flush.fill_(float(k))
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            op.hpsi_dev(psi, out, stream=sh)
-            b.record(stream)
-            torch.cuda.synchronize()
-            tt += a.elapsed_time(b) / 1e3
-        tuned = {"value": ws * plain_steps * nrhs / tt, "unit": UNIT, "ms_per_step": 1e3 * tt / plain_steps,
-                 "plan": {"geo": tr["geo"], "rmax": tr["rmax"], "split": tr["split"]},
-                 "tuner_best_ms": tr["ms"], "tuner_automatic_ms": tr["default_ms"]}
-        op.set_plan(-1, 32, 0)
 
     # callers of the path: Davidson on the same operator, OC gradient on the 4-D L=7 system
     extras = {}
@@ -726,8 +734,17 @@ def run_ours(args, ws, rank, local):
             "clocks": {"sm_mhz": clocks["sm_mhz"], "sm_max_mhz": clocks["sm_max_mhz"], "reasons": clocks["reasons"]},
             "gpu_launches": launches,
         }
-        if tuned:
-            result["tuned"] = tuned
+        if tr is not None:
+            result["plan"] = {"source": "autotuner (evr_sg4_tune_plan), before the warm-up", "geo": tr["geo"],
+                              "rmax": tr["rmax"], "split": tr["split"], "tuner_best_ms": tr["ms"],
+                              "tuner_automatic_ms": tr["default_ms"]}
+            result["automatic_plan"] = auto
+        elif args.plan:
+            g, r, sp = [int(x) for x in args.plan.split(",")]
+            result["plan"] = {"source": "given (--plan)", "geo": g, "rmax": r, "split": sp}
+            result["automatic_plan"] = auto
+        else:
+            result["plan"] = {"source": "automatic (--no-tune)"}
         result.update(extras)
     return result
 
@@ -769,7 +786,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-extras", action="store_true", help="skip the timings of the callers")
-    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner's plan")
+    ap.add_argument("--no-tune", action="store_true", help="keep the automatic launch plan (no autotuner)")
+    ap.add_argument("--plan", default="", help="a fixed launch plan 'geo,rmax,split' instead of the autotuner's "
+                                                "(geo 0 wide, 1 narrow, 2 mid; for reproducible profiles)")
     ap.add_argument("--extras", default="config0,davidson,oc,uneven,graph,stream12",
                     help="callers to time: config0 (the 3-D L=6 workload), davidson, oc (optimal-control gradient), "
                          "uneven (64-instance batching), "
