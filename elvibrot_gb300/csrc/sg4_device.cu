@@ -1653,10 +1653,10 @@ extern "C" int evr_sg4_multi_create(int n, evr_sg4_ctx* const* ctxs, const int* 
   return EVR_OK;
 }
 
-extern "C" int evr_sg4_multi_groups(const evr_sg4_multi* m, int* n_groups, int* geo, long long* n_items) {
-  if (!m || !n_groups) return set_error(EVR_ERR_ARG, "multi_groups: NULL argument");
+extern "C" int evr_sg4_multi_groups(const evr_sg4_multi* m, int cap, int* n_groups, int* geo, long long* n_items) {
+  if (!m || !n_groups || cap < 0) return set_error(EVR_ERR_ARG, "multi_groups: NULL argument or cap < 0");
   *n_groups = (int)m->groups.size();
-  for (size_t g = 0; g < m->groups.size(); ++g) {
+  for (size_t g = 0; g < m->groups.size() && (int)g < cap; ++g) {
     if (geo) geo[g] = m->groups[g].geo;
     if (n_items) n_items[g] = (long long)m->groups[g].sorted.size();
   }

@@ -140,7 +140,7 @@ def _declare(L):
         "evr_sg4_multi_hpsi": [vp, ctypes.POINTER(vp), ctypes.POINTER(ll), ctypes.POINTER(vp), ctypes.POINTER(ll),
                                dp, dp, vp],
         "evr_sg4_multi_last_launches": [vp, ctypes.POINTER(ll)],
-        "evr_sg4_multi_groups": [vp, ip, ip, ctypes.POINTER(ll)],
+        "evr_sg4_multi_groups": [vp, ctypes.c_int, ip, ip, ctypes.POINTER(ll)],
         "evr_sg4_multi_destroy": [vp],
         "evr_sg4_multi_cheby_propagate": [vp, ctypes.POINTER(ChebyOpts), ctypes.POINTER(vp), ctypes.POINTER(vp),
                                           ctypes.POINTER(ctypes.c_int), vp],
@@ -597,9 +597,10 @@ class MultiOp:
     def groups(self):
         """[(geometry, work items)] per launch group (0 wide, 1 narrow, 2 mid)."""
         n = ctypes.c_int()
-        geo = (ctypes.c_int * 2)()
-        items = (ctypes.c_longlong * 2)()
-        check(lib().evr_sg4_multi_groups(self._h, ctypes.byref(n), geo, items))
+        check(lib().evr_sg4_multi_groups(self._h, 0, ctypes.byref(n), None, None))
+        geo = (ctypes.c_int * max(1, n.value))()
+        items = (ctypes.c_longlong * max(1, n.value))()
+        check(lib().evr_sg4_multi_groups(self._h, n.value, ctypes.byref(n), geo, items))
         return [(geo[g], items[g]) for g in range(n.value)]
 
     def cheby_propagate(self, psis, Hmin, Hmax, dt: float, npoly: int, nsteps: int, stream: int = 0,

@@ -363,17 +363,19 @@ int evr_sg4_cheby_propagate(evr_sg4_ctx* c, const evr_cheby_opts* o, int nrhs, d
  * stream at a time.
  * Launch groups: the contexts with D <= 6 run narrow in a launch of their
  * own when their items fill enough waves and other contexts exist; else one
- * launch takes every context.  A group's geometry is automatic unless every
- * context in it names the same one through evr_sg4_set_plan before
- * evr_sg4_multi_create.  evr_sg4_multi_groups reports the groups (at most 2):
- * their count, and per group the geometry (0 wide, 1 narrow, 2 mid) and the
- * number of work items (geo and n_items may be NULL). */
+ * launch takes every context; a group of more than 64 contexts is split into
+ * launches of at most 64 (the contexts' parameters travel by value in the
+ * launch).  A group's geometry is automatic unless every context in it names
+ * the same one through evr_sg4_set_plan before evr_sg4_multi_create.
+ * evr_sg4_multi_groups reports the launch groups: their count, and for the
+ * first min(count, cap) the geometry (0 wide, 1 narrow, 2 mid) and the number
+ * of work items (geo and n_items may be NULL). */
 typedef struct evr_sg4_multi evr_sg4_multi;
 int evr_sg4_multi_create(int n, evr_sg4_ctx* const* ctxs, const int* nrhs, int flags, evr_sg4_multi** out);
 int evr_sg4_multi_hpsi(evr_sg4_multi* m, const double* const* psi, const long long* ldpsi, double* const* hpsi,
                        const long long* ldh, const double* E0, const double* Esc, void* stream);
 int evr_sg4_multi_last_launches(const evr_sg4_multi* m, long long* n);
-int evr_sg4_multi_groups(const evr_sg4_multi* m, int* n_groups, int* geo, long long* n_items);
+int evr_sg4_multi_groups(const evr_sg4_multi* m, int cap, int* n_groups, int* geo, long long* n_items);
 int evr_sg4_multi_destroy(evr_sg4_multi* m);
 /* Chebyshev propagation (evr_sg4_cheby_propagate's fixed-order form) of the
  * packets of every context of a plan created with EVR_APPLY_COMPLEX, in

@@ -115,6 +115,36 @@ def test_multi_two_launch_groups():
     ops[1].set_plan(-1)
 
 
+def test_multi_more_contexts_than_one_parameter_block():
+    """70 contexts: more than one launch's parameter block holds (64), so the
+    plan runs them in two launches; every context gets the bits of its own
+    launch, also with contexts of both launches skipped."""
+    need_cuda()
+    ops = [make_model(2 + k % 3, 3 + k % 4, 1 if k % 2 else 10, 200 + k).operator() for k in range(70)]
+    nrhs = [1 + k % 3 for k in range(70)]
+    psis = [_rand(op, r, False, 300 + k) for k, (op, r) in enumerate(zip(ops, nrhs))]
+    ref = []
+    for op, P in zip(ops, psis):
+        O = torch.empty_like(P)
+        op.hpsi_dev(P, O)
+        ref.append(O)
+    plan = MultiOp(ops, nrhs)
+    groups = plan.groups()
+    assert len(groups) == 2 and all(n > 0 for _, n in groups)
+    outs = [torch.full_like(P, float("nan")) for P in psis]
+    plan.hpsi(psis, outs)
+    torch.cuda.synchronize()
+    assert plan.last_launches() == 2 + 2 * 70
+    for k in range(70):
+        assert torch.equal(outs[k], ref[k]), f"context {k}"
+    skip = {3, 40, 65, 69}
+    outs2 = [torch.full_like(P, 7.0) for P in psis]
+    plan.hpsi([None if k in skip else P for k, P in enumerate(psis)], outs2)
+    torch.cuda.synchronize()
+    for k in range(70):
+        assert torch.all(outs2[k] == 7.0) if k in skip else torch.equal(outs2[k], ref[k]), f"context {k}"
+
+
 def test_multi_skips_null_contexts_and_leaves_contexts_usable():
     need_cuda()
     ops = _uneven_ops()[:4]
