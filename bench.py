@@ -639,7 +639,7 @@ def run_ours(args, ws, rank, local):
     # the automatic plan on the same workload and protocol, for comparison
     auto = None
     if tr is not None or args.plan:
-        op.set_plan(-1, 32, 0)
+        op.set_plan()
         step()  # untimed: the first call under a new plan builds its work list
         torch.cuda.synchronize()
         ta = 0.0

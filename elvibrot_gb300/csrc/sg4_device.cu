@@ -95,6 +95,16 @@ int desc_sizes(const evr_sg4_desc* d, DescSizes* z) {
 
 #include "sg4_items.cuh"
 
+// The automatic launch plan's knobs (evr_sg4_set_plan): the most right-hand
+// sides per work item, and the mode-pass thread mapping (0 chosen per pass,
+// 1 one thread per fibre, 2 one thread per output element).
+#ifndef EVR_AUTO_RMAX
+#define EVR_AUTO_RMAX 32
+#endif
+#ifndef EVR_AUTO_SPLIT
+#define EVR_AUTO_SPLIT 0
+#endif
+
 namespace evr {
 
 // The kernels of launch geometry geo (0 wide, 1 narrow, 2 mid).
@@ -417,9 +427,9 @@ struct evr_sg4_ctx {
   int grid = 0;
   int smem_doubles = 0;
   int geo = 0;                       // launch geometry (1: narrow, D <= EVR_NARROW_FMAX)
-  int rmax = 32;                     // most right-hand sides per work item (plan knob)
+  int rmax = EVR_AUTO_RMAX;          // most right-hand sides per work item (plan knob)
   int geo_override = -1;             // launch geometry (plan knob; -1 automatic)
-  int split = 0;                     // mode-pass thread mapping (plan knob)
+  int split = EVR_AUTO_SPLIT;        // mode-pass thread mapping (plan knob)
   // operator
   bool have_op = false;
   int type = -1;
@@ -2228,6 +2238,8 @@ extern "C" int evr_sg4_set_plan(evr_sg4_ctx* c, int geo, int rmax, int split) {
   if (geo < -1 || geo > 2) return set_error(EVR_ERR_ARG, "set_plan: geometry %d not in {-1, 0, 1, 2}", geo);
   if (geo == 1 && c->D > EVR_NARROW_FMAX)
     return set_error(EVR_ERR_ARG, "set_plan: the narrow geometry takes D <= %d (D = %d)", EVR_NARROW_FMAX, c->D);
+  if (rmax == 0) rmax = EVR_AUTO_RMAX;
+  if (split == -1) split = EVR_AUTO_SPLIT;
   if (rmax < 1 || rmax > 32) return set_error(EVR_ERR_ARG, "set_plan: rmax %d not in [1, 32]", rmax);
   if (split < 0 || split > 2) return set_error(EVR_ERR_ARG, "set_plan: split %d not in {0, 1, 2}", split);
   c->geo_override = geo;
@@ -2256,7 +2268,7 @@ static std::string tune_key(const evr_sg4_ctx* c, int nrhs, int flags) {
 }
 
 struct TuneEntry {
-  int geo = -1, rmax = 32, split = 0;
+  int geo = -1, rmax = EVR_AUTO_RMAX, split = EVR_AUTO_SPLIT;
   double ms = 0.0, default_ms = 0.0;
 };
 
@@ -2376,7 +2388,7 @@ extern "C" int evr_sg4_tune_plan(evr_sg4_ctx* c, int nrhs, int flags, const char
     return rc;
   };
   TuneEntry best;
-  int rc = time_plan(-1, 32, 0, &best.default_ms);  // the automatic plan first
+  int rc = time_plan(-1, EVR_AUTO_RMAX, EVR_AUTO_SPLIT, &best.default_ms);  // the automatic plan first
   if (!rc) {
     best.ms = best.default_ms;
     best.geo = auto_geo_of(c, nrhs, flags);
@@ -2398,11 +2410,12 @@ extern "C" int evr_sg4_tune_plan(evr_sg4_ctx* c, int nrhs, int flags, const char
   // confirmation: the minimum over many candidates favours a lucky timing, so
   // the winner and the automatic plan are timed again, alternately, five
   // times each; the winner stays only if its median is more than 1 % faster
-  if (!rc && !(best.geo == -1 || (best.rmax == 32 && best.split == 0 && best.geo == auto_geo_of(c, nrhs, flags)))) {
+  if (!rc && !(best.geo == -1 || (best.rmax == EVR_AUTO_RMAX && best.split == EVR_AUTO_SPLIT &&
+                                   best.geo == auto_geo_of(c, nrhs, flags)))) {
     std::vector<double> ta, tb;
     for (int k = 0; k < 5 && !rc; ++k) {
       double ms = 0.0;
-      if (!(rc = time_plan(-1, 32, 0, &ms))) ta.push_back(ms);
+      if (!(rc = time_plan(-1, EVR_AUTO_RMAX, EVR_AUTO_SPLIT, &ms))) ta.push_back(ms);
       if (!rc && !(rc = time_plan(best.geo, best.rmax, best.split, &ms))) tb.push_back(ms);
     }
     if (!rc) {
@@ -2410,8 +2423,8 @@ extern "C" int evr_sg4_tune_plan(evr_sg4_ctx* c, int nrhs, int flags, const char
       std::sort(tb.begin(), tb.end());
       if (!(tb[2] < 0.99 * ta[2])) {
         best.geo = auto_geo_of(c, nrhs, flags);
-        best.rmax = 32;
-        best.split = 0;
+        best.rmax = EVR_AUTO_RMAX;
+        best.split = EVR_AUTO_SPLIT;
         best.ms = ta[2];
       } else {
         best.ms = tb[2];

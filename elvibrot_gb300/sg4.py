@@ -345,7 +345,8 @@ class ParamOp:
         return {"geo": r.geo, "rmax": r.rmax, "split": r.split, "ms": r.ms, "default_ms": r.default_ms,
                 "from_cache": bool(r.from_cache)}
 
-    def set_plan(self, geo: int = -1, rmax: int = 32, split: int = 0):
+    def set_plan(self, geo: int = -1, rmax: int = 0, split: int = -1):
+        """Plan knobs (evr_sg4_set_plan); no arguments: the automatic plan."""
         check(lib().evr_sg4_set_plan(self._h, int(geo), int(rmax), int(split)))
 
     def get_plan(self):

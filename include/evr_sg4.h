@@ -233,9 +233,12 @@ int evr_sg4_field_slices(const evr_sg4_ctx* c, long long* nslices);
  * Tune_SG4threads_HPsi, SRC/sub_main/vib.f90:2013-2123):
  *   geo   : launch geometry, -1 automatic (per work plan), 0 wide (4 CTAs
  *           per SM), 1 narrow (8 per SM, D <= 6 only), 2 mid (6 per SM);
- *   rmax  : most right-hand sides one work item carries, 1..32;
+ *   rmax  : most right-hand sides one work item carries, 1..32 (0: the
+ *           automatic plan's value);
  *   split : mode passes, 0 thread mapping chosen per pass, 1 one thread per
- *           fibre, 2 one thread per output element.
+ *           fibre, 2 one thread per output element (-1: the automatic
+ *           plan's value).
+ * evr_sg4_set_plan(c, -1, 0, -1) restores the automatic plan.
  * Results do not depend on them: every setting runs the same arithmetic per
  * Smolyak term and right-hand side (the same bits). */
 int evr_sg4_set_plan(evr_sg4_ctx* c, int geo, int rmax, int split);

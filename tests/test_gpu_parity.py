@@ -321,7 +321,7 @@ def test_plan_tuner_every_plan_same_bits_and_cached(tmp_path):
             op.hpsi_dev(P, out)
             torch.cuda.synchronize()
             assert torch.equal(out, ref), (geo, rmax, split)
-    op.set_plan(-1, 32, 0)
+    op.set_plan()
     cache = str(tmp_path / "tune.json")
     r = op.tune_plan(20, cache_path=cache)
     assert not r["from_cache"] and r["ms"] <= r["default_ms"]
