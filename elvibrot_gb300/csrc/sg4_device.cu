@@ -97,12 +97,18 @@ int desc_sizes(const evr_sg4_desc* d, DescSizes* z) {
 
 // The automatic launch plan's knobs (evr_sg4_set_plan): the most right-hand
 // sides per work item, and the mode-pass thread mapping (0 chosen per pass,
-// 1 one thread per fibre, 2 one thread per output element).
+// 1 one thread per fibre, 2 one thread per output element).  Four columns per
+// item and one thread per output element were the autotuner's choice for the
+// 6-D benchmark and for 55 of the 64 uneven instances; as the automatic plan
+// they measured faster than (32, per-pass choice) on every timed path: the
+// benchmark 1.8 %, the RK4 stage 4.2 %, the OC gradient 3.8 %, Chebyshev 3 %,
+// the 64-instance draw 1.6 %, the per-term path 2-5 %, Davidson 0.5 %, the
+// streamed 12-D operator 0.2 % (same bits).
 #ifndef EVR_AUTO_RMAX
-#define EVR_AUTO_RMAX 32
+#define EVR_AUTO_RMAX 4
 #endif
 #ifndef EVR_AUTO_SPLIT
-#define EVR_AUTO_SPLIT 0
+#define EVR_AUTO_SPLIT 2
 #endif
 
 namespace evr {
