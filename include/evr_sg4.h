@@ -161,7 +161,7 @@ int evr_sg4_hpsi(evr_sg4_ctx* c, int nrhs, const double* psi, long long ldpsi, d
                  long long ldh, double E0, double Esc, void* stream);
 
 /* Same result through one kernel launch per Smolyak term (the "plain"
- * per-term GPU path, kept as the baseline the batched kernel is measured
+ * per-term GPU path, kept as the baseline the one-launch path is measured
  * against; it mirrors the reference's per-term loop). */
 int evr_sg4_hpsi_plain(evr_sg4_ctx* c, int nrhs, const double* psi, long long ldpsi,
                        double* hpsi, long long ldh, void* stream);
@@ -196,7 +196,7 @@ int evr_sg4_hpsi_host(evr_sg4_ctx* c, int nrhs, const double* psi, long long ldp
 /* H.psi that allocates no device memory (no counterpart in the reference).
  * For callers that cannot call cudaMalloc -- a host program whose own
  * allocator owns the device memory, a real-time loop that must stay out of
- * the driver's allocator -- this runs the same batched kernel as
+ * the driver's allocator -- this runs the same persistent kernel as
  * evr_sg4_hpsi with its scratch (work counter, work list, per-term
  * contributions, slabs for terms larger than shared memory) carved from one
  * fixed file-scope device array of EVR_SG4_NOALLOC_SCRATCH_BYTES, which every

@@ -112,7 +112,7 @@ def test_hpsi_matches_oracle(D, L, type_op, nrhs):
     check_against_oracle(same_inputs_op(O, kw), O, kw, psi, f"{D}-D L={L} type {type_op} (oracle tables)")
     op = m.operator()   # product tables + device-evaluated fields
     check_against_oracle(op, O, kw, psi, f"{D}-D L={L} type {type_op} (product tables)")
-    assert op.last_launches == 3   # batched kernel + the two ordered-accumulation kernels
+    assert op.last_launches == 3   # the item kernel + the two ordered-accumulation kernels
 
 
 def test_type0_and_fields_from_grids():
