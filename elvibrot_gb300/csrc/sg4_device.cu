@@ -116,13 +116,16 @@ namespace evr {
 // The kernels of launch geometry geo (0 wide, 1 narrow, 2 mid).
 struct GeoKernels {
   int ctas;  // resident CTAs per SM
+  int fmax;  // largest D of its fused passes
   const MultiEntry<EVR_PB_SMALL>* small;
   const MultiEntry<EVR_PB_LARGE>* large;
+  const MultiEntry<EVR_PB_SMALL>* small10;  // type 10 with D <= fmax only
 };
 static const GeoKernels& geo_kernels(int geo) {
-  static const GeoKernels t[3] = {{EVR_WIDE_CTAS, &multi_small_wide, &multi_large_wide},
-                                  {EVR_NARROW_CTAS, &multi_small_narrow, &multi_large_narrow},
-                                  {EVR_MID_CTAS, &multi_small_mid, &multi_large_mid}};
+  static const GeoKernels t[3] = {
+      {EVR_WIDE_CTAS, EVR_WIDE_FMAX, &multi_small_wide, &multi_large_wide, &multi_small10_wide},
+      {EVR_NARROW_CTAS, EVR_NARROW_FMAX, &multi_small_narrow, &multi_large_narrow, &multi_small10_narrow},
+      {EVR_MID_CTAS, EVR_MID_FMAX, &multi_small_mid, &multi_large_mid, &multi_small10_mid}};
   return t[geo == 1 ? 1 : (geo == 2 ? 2 : 0)];
 }
 
@@ -132,14 +135,17 @@ static const GeoKernels& geo_kernels(int geo) {
 // records the launch keeps the values of the recording.
 static void launch_multi(int geo, unsigned grid, size_t smem, cudaStream_t s, const KParams* ps, int n_ctx,
                          const MItem* items, int n_items, int item_base, unsigned int* counter) {
+  const GeoKernels& k = geo_kernels(geo);
   if (n_ctx <= EVR_PB_SMALL) {
     ParamBlock<EVR_PB_SMALL> P;
     std::copy(ps, ps + n_ctx, P.p);
-    geo_kernels(geo).small->launch(grid, smem, s, P, items, n_items, item_base, counter);
+    bool t10 = true;  // every context type 10 within the fused passes: the kernel compiled for them
+    for (int j = 0; j < n_ctx; ++j) t10 = t10 && ps[j].type == 10 && ps[j].D <= k.fmax;
+    (t10 ? k.small10 : k.small)->launch(grid, smem, s, P, items, n_items, item_base, counter);
   } else {
     static thread_local ParamBlock<EVR_PB_LARGE> P;  // 16 KB: not on the stack
     std::copy(ps, ps + n_ctx, P.p);
-    geo_kernels(geo).large->launch(grid, smem, s, P, items, n_items, item_base, counter);
+    k.large->launch(grid, smem, s, P, items, n_items, item_base, counter);
   }
 }
 
@@ -153,19 +159,20 @@ static void launch_single(int geo, unsigned grid, size_t smem, cudaStream_t s, c
 static int geo_ctas(int geo) { return geo_kernels(geo).ctas; }
 
 // Static shared memory plus the 1 KB the driver reserves per CTA, rounded up
-// to 256 bytes (queried once): the larger of a geometry's two kernels, so
-// both keep the geometry's CTAs per SM.
+// to 256 bytes (queried once): the largest of a geometry's kernels, so all
+// of them keep the geometry's CTAs per SM.
 static int smem_slack(int geo) {
   static const std::vector<int> slack = [] {
     std::vector<int> v(3, 4096);
     for (int g = 0; g < 3; ++g) {
-      size_t a = 0, b = 0;
+      size_t a = 0, b = 0, c = 0;
       const GeoKernels& k = geo_kernels(g);
-      if (k.small->static_smem(&a) != cudaSuccess || k.large->static_smem(&b) != cudaSuccess) {
+      if (k.small->static_smem(&a) != cudaSuccess || k.large->static_smem(&b) != cudaSuccess ||
+          k.small10->static_smem(&c) != cudaSuccess) {
         cudaGetLastError();
         continue;
       }
-      v[g] = (int)((std::max(a, b) + 1024 + 255) / 256 * 256);
+      v[g] = (int)((std::max(a, std::max(b, c)) + 1024 + 255) / 256 * 256);
     }
     return v;
   }();
@@ -185,6 +192,7 @@ static cudaError_t set_smem_attributes() {
     const int bytes = geo_smem_bytes(g);
     e = k.small->set_smem(bytes);
     if (e == cudaSuccess) e = k.large->set_smem(bytes);
+    if (e == cudaSuccess) e = k.small10->set_smem(bytes);
   }
   return e;
 }

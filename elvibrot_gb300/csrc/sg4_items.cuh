@@ -685,7 +685,10 @@ static __device__ void store_contrib(const KParams& p, const ItemShared& it, con
   __syncthreads();
 }
 
-template <int FMAX>
+// OPK: 0 every operator type; 10 only type 10 with D <= FMAX (the fused
+// passes), for launches whose contexts are all such (the other branches are
+// not compiled in).
+template <int FMAX, int OPK>
 __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int term, int rhs0) {
   if (threadIdx.x == 0) {
     const TermInfo& T = p.terms[term];
@@ -764,7 +767,7 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ter
   double* y;
   const long long oq = it.off_nq;
 
-  if (p.type == 0) {
+  if (OPK != 10 && p.type == 0) {
     // CASE 0: y = V.x
     if (p.nb0 == 1) {
       for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
@@ -777,7 +780,7 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ter
       for (int e = threadIdx.x; e < NQR; e += blockDim.x) y[e] = p.V ? vmat_apply(p, x, e, nqt, oq, it.rhs0) : 0.0;
     }
     __syncthreads();
-  } else if (p.type == 1) {
+  } else if (OPK != 10 && p.type == 1) {
     // CASE 1 through the fused grid passes in the wide and mid kernels (x in
     // X, O in T, then U_1..U_{D-1}); the narrow kernel keeps the term-by-term
     // passes: compiled into it, the fused code shifted its register
@@ -816,7 +819,7 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ter
       }
       y = Y;
     }
-  } else if (D <= FMAX) {
+  } else if (OPK == 10 || D <= FMAX) {
     // CASE 10 through the fused grid passes; x is in X.  Without Jac and rho
     // (D + 1 arrays) U_1..U_D follow X and pass B writes O = V.x + c.sum over
     // x itself (each point is read and written by one thread; the -1/2 of
@@ -934,9 +937,12 @@ struct ParamBlock {
 // local memory (3 % slower on the 64-instance draw, 17 % on its small
 // contexts), and a kernel taking one context's parameters as a plain kernel
 // argument was 1.3 % slower on the 6-D benchmark (more spill code).
+// OPK 10 compiles only the fused type-10 path (launches whose contexts are
+// all type 10 with D <= FMAX): less code and fewer spills, 1.2 % faster on
+// the 6-D benchmark than the kernel for every type.
 // With a counter the CTAs pull items until the list is empty; without one
 // (the per-term path) CTA b runs item item_base + b.
-template <int MINB, int FMAX, int CAP>
+template <int MINB, int FMAX, int CAP, int OPK>
 __global__ void __launch_bounds__(EVR_CTA_THREADS, MINB) hpsi_items_kernel(const __grid_constant__ ParamBlock<CAP> P,
                                                               const MItem* __restrict__ items, int n_items,
                                                               int item_base, unsigned int* counter) {
@@ -950,14 +956,14 @@ __global__ void __launch_bounds__(EVR_CTA_THREADS, MINB) hpsi_items_kernel(const
     __syncthreads();
     if (idx >= n_items) break;
     const MItem m = items[idx];
-    run_item<FMAX>(P.p[m.ctx], it, smem, m.term, m.rhs0);
+    run_item<FMAX, OPK>(P.p[m.ctx], it, smem, m.term, m.rhs0);
   }
 }
 
 // One kernel of one launch geometry, each compiled in its own translation
 // unit (sg4_items.cu with EVR_GEO = 0 wide, 1 narrow, 2 mid and EVR_KIND = 0
-// the small, 1 the large parameter block); the host code in sg4_device.cu
-// assembles them per geometry.
+// the small, 1 the large parameter block, 2 the small block for type 10
+// only); the host code in sg4_device.cu assembles them per geometry.
 template <int CAP>
 struct MultiEntry {
   void (*launch)(unsigned grid, size_t smem, cudaStream_t s, const ParamBlock<CAP>& P, const MItem* items,
@@ -966,6 +972,7 @@ struct MultiEntry {
   cudaError_t (*set_smem)(int bytes);         // the dynamic shared-memory limit
 };
 extern const MultiEntry<EVR_PB_SMALL> multi_small_wide, multi_small_narrow, multi_small_mid;
+extern const MultiEntry<EVR_PB_SMALL> multi_small10_wide, multi_small10_narrow, multi_small10_mid;
 extern const MultiEntry<EVR_PB_LARGE> multi_large_wide, multi_large_narrow, multi_large_mid;
 
 }  // namespace evr
