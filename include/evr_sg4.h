@@ -202,8 +202,8 @@ int evr_sg4_hpsi_host(evr_sg4_ctx* c, int nrhs, const double* psi, long long ldp
  * fixed file-scope device array of EVR_SG4_NOALLOC_SCRATCH_BYTES, which every
  * GPU that loads the library holds until the process exits.  Sizes that need
  * more scratch are rejected with EVR_ERR_ARG.  The first call on a device
- * looks up the array's device address (cudaGetSymbolAddress); make that first
- * call before any stream capture.  All calls share the array: calls that
+ * looks up the array's device address (cudaGetSymbolAddress).  All calls
+ * share the array: calls that
  * overlap on the GPU (two streams or two threads) race.  Real psi only;
  * device pointers; same result as evr_sg4_hpsi. */
 #define EVR_SG4_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
