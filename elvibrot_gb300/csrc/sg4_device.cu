@@ -456,6 +456,10 @@ struct evr_sg4_ctx {
   double* d_F1 = nullptr;
   double F2[EVR_MAXD * EVR_MAXD] = {0};
   double F1[EVR_MAXD] = {0};
+  int n_t1 = 0;                       // type-1 terms with coefficient grids (0: constant F2 / F1)
+  std::vector<T1Term> t1_terms;       // host copy
+  T1Term* d_t1terms = nullptr;
+  double* d_t1grid = nullptr;
   // streamed operator fields: analytic V / G kept as coefficients and
   // evaluated per slice of Smolyak terms just before the slice's items run
   long long field_budget = 0;         // bytes; 0: fields stay resident
@@ -509,7 +513,7 @@ static void free_ctx(evr_sg4_ctx* c) {
                   c->d_inv_idx, c->d_contrib, c->d_chunk_q, c->d_fun_chunk, c->d_part,
                   c->d_scratch, c->d_V, c->d_G, c->d_Jac, c->d_cfac,
                   c->d_sqRho, c->d_F2, c->d_F1, c->d_io, c->d_Vcoef, c->d_Vfac, c->d_G0, c->d_G1,
-                  c->d_pt_start};
+                  c->d_pt_start, c->d_t1terms, c->d_t1grid};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete c;
@@ -743,11 +747,15 @@ extern "C" int evr_sg4_set_operator(evr_sg4_ctx* c, const evr_sg4_op_desc* op) {
   const int D = c->D;
   const long long snq = c->z.sum_nq;
   for (double** p : {&c->d_V, &c->d_G, &c->d_Jac, &c->d_sqRho, &c->d_cfac, &c->d_F2, &c->d_F1, &c->d_Vcoef, &c->d_G0,
-                     &c->d_G1})
+                     &c->d_G1, &c->d_t1grid})
     if (*p) {
       cudaFree(*p);
       *p = nullptr;
     }
+  if (c->d_t1terms) cudaFree(c->d_t1terms);
+  c->d_t1terms = nullptr;
+  c->n_t1 = 0;
+  c->t1_terms.clear();
   if (c->d_Vfac) cudaFree(c->d_Vfac);
   if (c->d_pt_start) cudaFree(c->d_pt_start);
   c->d_Vfac = nullptr;
@@ -778,7 +786,8 @@ extern "C" int evr_sg4_set_operator(evr_sg4_ctx* c, const evr_sg4_op_desc* op) {
     }
   }
   // fields given in analytic form are streamed per term slice when they exceed the budget
-  const bool grids = op->V_grid || (op->type == 10 && (op->G_grid || op->Jac_grid || op->sqRho_grid));
+  const bool grids = op->V_grid || (op->type == 10 && (op->G_grid || op->Jac_grid || op->sqRho_grid)) ||
+                     (op->type == 1 && (op->F2_grid || op->F1_grid));
   const double bpp = 8.0 * (polyV ? 1 : 0) + 8.0 * D * D * (affG ? 1 : 0);  // bytes per grid point
   const bool stream = c->field_budget > 0 && !grids && (polyV || affG) && bpp * (double)snq > (double)c->field_budget;
   if (stream && c->nb0 > 1)
@@ -842,6 +851,47 @@ extern "C" int evr_sg4_set_operator(evr_sg4_ctx* c, const evr_sg4_op_desc* op) {
         for (int j = i; j < D; ++j) c->F2[i * D + j] = op->F2[i * D + j];
     if (op->F1)
       for (int i = 0; i < D; ++i) c->F1[i] = op->F1[i];
+  }
+  if (op->type == 1 && (op->F2_grid || op->F1_grid)) {
+    // Q-dependent coefficients: the term list in Init_TypeOp order, (i, j >= i)
+    // then (i, 0); a grid that is zero everywhere is skipped (grid_zero), a
+    // term without a grid keeps its constant
+    std::vector<T1Term> tl;
+    std::vector<const double*> src;
+    auto add = [&](int i, int j, const double* g, double cst) -> int {
+      if (g) {
+        bool zero = true;
+        for (long long k = 0; k < snq; ++k) {
+          if (!std::isfinite(g[k])) return set_error(EVR_ERR_NUMERIC, "type-1 coefficient grid (%d, %d) is not finite", i, j);
+          if (g[k] != 0.0) zero = false;
+        }
+        if (zero) return EVR_OK;
+        tl.push_back(T1Term{i, j, (long long)src.size() * snq, 0.0});
+        src.push_back(g);
+      } else if (cst != 0.0) {
+        tl.push_back(T1Term{i, j, -1, cst});
+      }
+      return EVR_OK;
+    };
+    for (int i = 0; i < D; ++i)
+      for (int j = i; j < D; ++j)
+        if ((rc = add(i, j, op->F2_grid ? op->F2_grid + (size_t)(i * D + j) * snq : nullptr, c->F2[i * D + j])))
+          return rc;
+    for (int i = 0; i < D; ++i)
+      if ((rc = add(i, -1, op->F1_grid ? op->F1_grid + (size_t)i * snq : nullptr, c->F1[i]))) return rc;
+    memset(c->F2, 0, sizeof(c->F2));  // every term is in the list
+    memset(c->F1, 0, sizeof(c->F1));
+    if (!src.empty()) {
+      CUDA_TRY(cudaMalloc(&c->d_t1grid, src.size() * (size_t)snq * 8));
+      for (size_t k = 0; k < src.size(); ++k)
+        CUDA_TRY(cudaMemcpy(c->d_t1grid + k * snq, src[k], (size_t)snq * 8, cudaMemcpyHostToDevice));
+    }
+    if (!tl.empty()) {
+      CUDA_TRY(cudaMalloc(&c->d_t1terms, tl.size() * sizeof(T1Term)));
+      CUDA_TRY(cudaMemcpy(c->d_t1terms, tl.data(), tl.size() * sizeof(T1Term), cudaMemcpyHostToDevice));
+    }
+    c->n_t1 = (int)tl.size();  // 0: every term zero, V alone remains (the constant path)
+    c->t1_terms = tl;
   }
   if ((rc = upload(&c->d_F2, c->F2, (size_t)D * D)) || (rc = upload(&c->d_F1, c->F1, (size_t)D))) return rc;
   if (polyV || affG) {  // the analytic forms stay on the device (evaluated again per slice when streamed)
@@ -1066,6 +1116,9 @@ static KParams make_params(evr_sg4_ctx* c, int nrhs_v, int cshift, const double*
   p.F2 = c->d_F2;
   p.F1 = c->d_F1;
   p.t1_mixed = c->type == 1 && t1_mixed(c) ? 1 : 0;
+  p.n_t1 = c->type == 1 ? c->n_t1 : 0;
+  p.t1terms = c->d_t1terms;
+  p.t1grid = c->d_t1grid;
   p.split = c->split;
   p.type = c->type;
   p.nbuf = nbuf_for(c);
@@ -1228,6 +1281,10 @@ extern "C" int evr_sg4_flops_per_rhs(const evr_sg4_ctx* c, double* flops) {
     const double vq = c->d_V ? (c->nb0 > 1 ? 2.0 * c->nb0 * q : q) : 0.0;
     if (c->type == 0) {
       f += vq;
+    } else if (c->type == 1 && c->n_t1 > 0) {  // term by term: derivative passes, then coefficient x result
+      f += vq;
+      for (const T1Term& t : c->t1_terms)
+        f += 2.0 * q * nq[t.i] + (t.j > t.i ? 2.0 * q * nq[t.j] : 0.0) + 2.0 * q;
     } else if (c->type == 1) {  // the fused passes (type1_fused; the same for a diagonal F2 term by term)
       f += vq;
       for (int i = 0; i < D; ++i)
@@ -2155,7 +2212,7 @@ __global__ void __launch_bounds__(128) diag_kernel(KParams p, const int* __restr
 extern "C" int evr_sg4_diagonal(evr_sg4_ctx* c, double* diag, void* stream) {
   if (!c || !diag) return set_error(EVR_ERR_ARG, "diagonal: NULL argument");
   if (!c->have_op) return set_error(EVR_ERR_STATE, "diagonal: set_operator was not called");
-  if (c->nb0 > 1 || c->streamed || c->d_Jac || c->d_sqRho)
+  if (c->nb0 > 1 || c->streamed || c->d_Jac || c->d_sqRho || c->n_t1 > 0)
     return evr_sg4_diagonal_by_apply(c, diag, stream);
   cudaStream_t s = (cudaStream_t)stream;
   const int D = c->D;

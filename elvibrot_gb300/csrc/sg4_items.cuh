@@ -110,6 +110,15 @@ struct OpFields {
   double F1[EVR_MAXD];
 };
 
+// A type-1 derivative term with its coefficient (CASE 1 with Q-dependent
+// coefficients): coefficient * d_i d_j x, or * d_i x when j < 0; the
+// coefficient is the grid t1grid[goff + point] or, when goff < 0, c.
+struct T1Term {
+  int i, j;
+  long long goff;
+  double c;
+};
+
 struct KParams {
   int D, Lp1;
   int nrhs_v;                // virtual right-hand sides (2*nrhs for complex)
@@ -145,6 +154,9 @@ struct KParams {
   long long Nfun;            // packed basis functions per channel
   long long vstride;         // V[(a*nb0 + b)*vstride + point] for nb0 > 1
   int t1_mixed;              // type 1: some F2_ij (i < j) or F1_i is non-zero
+  int n_t1;                  // type 1 with coefficient grids: its terms (else 0)
+  const T1Term* t1terms;     // [n_t1]
+  const double* t1grid;      // their grids, sum_nq each
   int split;                 // mode passes: 0 per-pass choice, 1 one thread per fibre, 2 per output
 };
 
@@ -685,6 +697,60 @@ static __device__ void store_contrib(const KParams& p, const ItemShared& it, con
   __syncthreads();
 }
 
+// CASE 1 with Q-dependent coefficients, term by term as the reference
+// (sub_OpPsi_SG4.f90:1497-1520): each term's derivatives of x
+// (DerivOp_TO_RDP_OF_SmolaykRep), then times its coefficient grid, added
+// into Y; the terms act on every channel alike.  For H^T a term is
+// (g d_i d_j)^T = d_i^T d_j^T g (the transposed matrices of the item): the
+// coefficient first, then the derivatives.  Buffers: x (X or T), Y = T + NQR,
+// C = T + 2 NQR and the other of X / T.  (Not inlined, the call made the mid
+// kernel keep a 888-byte stack frame; inlined it adds some spill code to the
+// kernels for every operator type, not to the type-10 one.)
+static __device__ __forceinline__ double* type1_grid_terms(const KParams& p, const ItemShared& it, double* x, double* X,
+                                                        double* T, int NQR) {
+  const int nqt = it.nq_t;
+  const long long oq = it.off_nq;
+  double* Y = T + NQR;
+  double* C = T + 2 * NQR;
+  double* C2 = (x == X) ? T : X;
+  for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
+    const int q = e % nqt;
+    Y[e] = !p.V ? 0.0 : (p.nb0 == 1 ? __ldg(p.V + oq + q) * x[e] : vmat_apply(p, x, e, nqt, oq, it.rhs0));
+  }
+  __syncthreads();
+  for (int t = 0; t < p.n_t1; ++t) {
+    const T1Term tt = p.t1terms[t];
+    const double* g = tt.goff >= 0 ? p.t1grid + tt.goff + oq : nullptr;
+    if (!p.transpose) {
+      if (tt.j < 0) {
+        grid_deriv(p, it, tt.i, M_D1, x, C2, false, 1.0);
+      } else if (tt.j == tt.i) {
+        grid_deriv(p, it, tt.i, M_D2, x, C2, false, 1.0);
+      } else {
+        grid_deriv(p, it, tt.j, M_D1, x, C, false, 1.0);
+        __syncthreads();
+        grid_deriv(p, it, tt.i, M_D1, C, C2, false, 1.0);
+      }
+      __syncthreads();
+      for (int e = threadIdx.x; e < NQR; e += blockDim.x) Y[e] = fma(g ? __ldg(g + e % nqt) : tt.c, C2[e], Y[e]);
+    } else {
+      for (int e = threadIdx.x; e < NQR; e += blockDim.x) C[e] = (g ? __ldg(g + e % nqt) : tt.c) * x[e];
+      __syncthreads();
+      if (tt.j < 0) {
+        grid_deriv(p, it, tt.i, M_D1, C, Y, true, 1.0);
+      } else if (tt.j == tt.i) {
+        grid_deriv(p, it, tt.i, M_D2, C, Y, true, 1.0);
+      } else {
+        grid_deriv(p, it, tt.j, M_D1, C, C2, false, 1.0);
+        __syncthreads();
+        grid_deriv(p, it, tt.i, M_D1, C2, Y, true, 1.0);
+      }
+    }
+    __syncthreads();
+  }
+  return Y;
+}
+
 // OPK: 0 every operator type; 10 only type 10 with D <= FMAX (the fused
 // passes), for launches whose contexts are all such (the other branches are
 // not compiled in).
@@ -780,6 +846,8 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ter
       for (int e = threadIdx.x; e < NQR; e += blockDim.x) y[e] = p.V ? vmat_apply(p, x, e, nqt, oq, it.rhs0) : 0.0;
     }
     __syncthreads();
+  } else if (OPK != 10 && p.type == 1 && p.n_t1 > 0) {
+    y = type1_grid_terms(p, it, x, X, T, NQR);
   } else if (OPK != 10 && p.type == 1) {
     // CASE 1 through the fused grid passes in the wide and mid kernels (x in
     // X, O in T, then U_1..U_{D-1}); the narrow kernel keeps the term-by-term

@@ -95,7 +95,8 @@ class OpDesc(ctypes.Structure):
                 ("V_expo", ctypes.POINTER(ctypes.c_int)), ("G_grid", ctypes.POINTER(ctypes.c_double)),
                 ("G0", ctypes.POINTER(ctypes.c_double)), ("G1", ctypes.POINTER(ctypes.c_double)),
                 ("Jac_grid", ctypes.POINTER(ctypes.c_double)), ("sqRho_grid", ctypes.POINTER(ctypes.c_double)),
-                ("F2", ctypes.POINTER(ctypes.c_double)), ("F1", ctypes.POINTER(ctypes.c_double))]
+                ("F2", ctypes.POINTER(ctypes.c_double)), ("F1", ctypes.POINTER(ctypes.c_double)),
+                ("F2_grid", ctypes.POINTER(ctypes.c_double)), ("F1_grid", ctypes.POINTER(ctypes.c_double))]
 
 
 def _declare(L):
@@ -287,7 +288,8 @@ class Polynomial:
 class ParamOp:
     """SG4 operator on the GPU (param_Op with its Save_MemGrid grids).
 
-    type_op 0 : V;  1 : V + sum F2_ij d_i d_j + sum F1_i d_i (constant F);
+    type_op 0 : V;  1 : V + sum F2_ij d_i d_j + sum F1_i d_i (F constant, or
+    Q-dependent grids F2_grid [D, D, sum_nq] / F1_grid [D, sum_nq]);
     10 : -1/2 sum d_i Jac G_ji d_j s / (Jac s) + V with G grid or affine G(Q).
     """
 
@@ -295,7 +297,8 @@ class ParamOp:
                  V_poly: Optional[Polynomial] = None, G: Optional[np.ndarray] = None,
                  G0: Optional[np.ndarray] = None, G1: Optional[np.ndarray] = None,
                  Jac: Optional[np.ndarray] = None, sqRho: Optional[np.ndarray] = None,
-                 F2: Optional[np.ndarray] = None, F1: Optional[np.ndarray] = None, field_budget: int = 0):
+                 F2: Optional[np.ndarray] = None, F1: Optional[np.ndarray] = None, field_budget: int = 0,
+                 F2_grid: Optional[np.ndarray] = None, F1_grid: Optional[np.ndarray] = None):
         self.basis = basis
         self.type_op = int(type_op)
         h = ctypes.c_void_p()
@@ -303,12 +306,19 @@ class ParamOp:
         self._h = h
         if field_budget:
             check(lib().evr_sg4_set_field_budget(h, int(field_budget)))
-        self.set_operator(V=V, V_poly=V_poly, G=G, G0=G0, G1=G1, Jac=Jac, sqRho=sqRho, F2=F2, F1=F1)
+        self.set_operator(V=V, V_poly=V_poly, G=G, G0=G0, G1=G1, Jac=Jac, sqRho=sqRho, F2=F2, F1=F1,
+                          F2_grid=F2_grid, F1_grid=F1_grid)
 
-    def set_operator(self, V=None, V_poly=None, G=None, G0=None, G1=None, Jac=None, sqRho=None, F2=None, F1=None):
+    def set_operator(self, V=None, V_poly=None, G=None, G0=None, G1=None, Jac=None, sqRho=None, F2=None, F1=None,
+                     F2_grid=None, F1_grid=None):
         D = self.basis.D
         c = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float64).ravel()
-        keep = dict(V=c(V), G=c(G), G0=c(G0), G1=c(G1), Jac=c(Jac), sqRho=c(sqRho), F2=c(F2), F1=c(F1))
+        keep = dict(V=c(V), G=c(G), G0=c(G0), G1=c(G1), Jac=c(Jac), sqRho=c(sqRho), F2=c(F2), F1=c(F1),
+                    F2_grid=c(F2_grid), F1_grid=c(F1_grid))
+        snq = self.basis.sum_nq
+        for name, n in (("F2_grid", D * D * snq), ("F1_grid", D * snq)):
+            if keep[name] is not None and keep[name].size != n:
+                raise EVRError(1, f"{name}: {keep[name].size} values, expected {n}")
         coef = expo = None
         nterms = 0
         if V_poly is not None and V is None:
@@ -321,7 +331,7 @@ class ParamOp:
             coef = coef.ravel()
         op = OpDesc(self.type_op, _dp(keep["V"]), nterms, _dp(coef), _ip(expo), _dp(keep["G"]),
                     _dp(keep["G0"]), _dp(keep["G1"]), _dp(keep["Jac"]), _dp(keep["sqRho"]),
-                    _dp(keep["F2"]), _dp(keep["F1"]))
+                    _dp(keep["F2"]), _dp(keep["F1"]), _dp(keep["F2_grid"]), _dp(keep["F1_grid"]))
         check(lib().evr_sg4_set_operator(self._h, ctypes.byref(op)))
 
     def __del__(self):

@@ -130,6 +130,14 @@ int evr_sg4_destroy(evr_sg4_ctx* c);
  * or the affine form G_ij(Q) = G0_ij + sum_k G1_ijk Q_k ([D*D], [D*D*D],
  * row-major ijk); neither = identity.  Jac / sqRho grids: NULL = 1.
  * F2 [D*D] row-major (entries i<=j used) and F1 [D]: constant coefficients.
+ * F2_grid [D*D*sum_nq] (term (i, j), i <= j, at [(i*D + j)*sum_nq + point])
+ * and F1_grid [D*sum_nq] (term i at [i*sum_nq + point]): Q-dependent
+ * coefficients of the type-1 derivative terms (OpGrid(iterm)%Grid when it is
+ * not grid_cte); when given they replace F2 / F1.  Then every derivative
+ * term is applied on its own, its derivatives first and its coefficient grid
+ * after, in Init_TypeOp order ((i, j >= i), then (i, 0)), and a term whose
+ * grid is zero everywhere is skipped (grid_zero); the terms act on every
+ * channel alike.  Such grids stay resident.
  * All pointers are host pointers; the fields are built once on the device
  * (the equivalent of Save_MemGrid).
  * ---------------------------------------------------------------------- */
@@ -146,6 +154,8 @@ typedef struct {
   const double* sqRho_grid;
   const double* F2;
   const double* F1;
+  const double* F2_grid;
+  const double* F1_grid;
 } evr_sg4_op_desc;
 
 int evr_sg4_set_operator(evr_sg4_ctx* c, const evr_sg4_op_desc* op);
@@ -319,8 +329,8 @@ int evr_sg4_davidson(evr_sg4_ctx* c, const evr_davidson_opts* o, const double* g
  * term: each Smolyak term's diagonal is a grid->basis transform of its
  * fields with per-mode matrices (RBGwrho.D o (D.RGB)^T), one transform per
  * field term, then the weighted, term-ordered accumulation of H.psi.  Type 10
- * with Jac or rho grids, several channels and streamed fields use
- * evr_sg4_diagonal_by_apply. */
+ * with Jac or rho grids, type 1 with coefficient grids, several channels and
+ * streamed fields use evr_sg4_diagonal_by_apply. */
 int evr_sg4_diagonal(evr_sg4_ctx* c, double* diag, void* stream);
 /* The same diagonal from H applied to blocks of 64 unit vectors (N/64 H.psi
  * calls): valid for every operator, and the check of the term-wise form. */

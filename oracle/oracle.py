@@ -68,7 +68,8 @@ class _OrcOp(ctypes.Structure):
                 ("sqRho", ctypes.POINTER(ctypes.c_double)), ("F2", ctypes.POINTER(ctypes.c_double)),
                 ("F1", ctypes.POINTER(ctypes.c_double)), ("V_nterms", ctypes.c_int),
                 ("V_coef", ctypes.POINTER(ctypes.c_double)), ("V_expo", ctypes.POINTER(ctypes.c_int)),
-                ("G0", ctypes.POINTER(ctypes.c_double)), ("G1", ctypes.POINTER(ctypes.c_double))]
+                ("G0", ctypes.POINTER(ctypes.c_double)), ("G1", ctypes.POINTER(ctypes.c_double)),
+                ("F2_grid", ctypes.POINTER(ctypes.c_double)), ("F1_grid", ctypes.POINTER(ctypes.c_double))]
 
 
 def gauss_hermite(nq: int):
@@ -133,12 +134,13 @@ class OracleSG4:
         return Q.reshape(self.sum_nq, self.D)
 
     def hpsi(self, psi, type_op=10, V=None, G=None, Jac=None, sqRho=None, F2=None, F1=None, nthreads=0,
-             extended=False, V_poly=None, G0=None, G1=None):
+             extended=False, V_poly=None, G0=None, G1=None, F2_grid=None, F1_grid=None):
         """psi: (N,) or (N, nrhs) float64, column-major per RHS.
 
         V / G are grids; alternatively V_poly = (coef[nt], expo[nt, D]) and the
         affine G0[D, D], G1[D, D, D] are evaluated term by term at the grid
-        points.  extended=True runs the same algorithm with long-double
+        points.  Type 1: F2[D, D] / F1[D] constant, or the grids
+        F2_grid[D, D, sum_nq] / F1_grid[D, sum_nq] (Q-dependent coefficients).  extended=True runs the same algorithm with long-double
         intermediates (the accuracy yardstick); the result is rounded to double."""
         psi = np.asarray(psi, dtype=np.float64)
         one = psi.ndim == 1
@@ -153,8 +155,9 @@ class OracleSG4:
             expo = np.ascontiguousarray(V_poly[1], dtype=np.int32).reshape(len(coef), self.D)
         g0 = None if G0 is None else np.ascontiguousarray(G0, dtype=np.float64)
         g1 = None if G1 is None else np.ascontiguousarray(G1, dtype=np.float64)
+        fg = [None if a is None else np.ascontiguousarray(a, dtype=np.float64).ravel() for a in (F2_grid, F1_grid)]
         op = _OrcOp(type_op, *[_dp(a) for a in keep], 0 if coef is None else len(coef), _dp(coef), _ip(expo),
-                    _dp(g0), _dp(g1))
+                    _dp(g0), _dp(g1), _dp(fg[0]), _dp(fg[1]))
         fn = lib().orc_hpsi_ld if extended else lib().orc_hpsi
         rc = fn(self.h, ctypes.byref(op), nrhs, _dp(Pc), _dp(H), int(nthreads))
         if rc != 0:

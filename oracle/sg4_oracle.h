@@ -57,7 +57,11 @@ void orc_grid_points(const orc_sg4* s, double* Q);
  *  type 0 : y = V.x
  *  type 1 : y = sum_terms F_t Der_t x, terms (0,0),(i<=j),(i,0) in the
  *           reference order; F2[D*D] (i,j)-> constant coefficient of d_i d_j
- *           (row-major, i<=j used), F1[D] constant coefficient of d_i.
+ *           (row-major, i<=j used), F1[D] constant coefficient of d_i;
+ *           F2_grid[D*D*sum_nq] (term (i,j) at [(i*D+j)*sum_nq + point]) and
+ *           F1_grid[D*sum_nq], when given, replace them with Q-dependent
+ *           coefficients (OpGrid(iterm)%Grid), a grid zero everywhere being
+ *           a grid_zero term.
  *  type 10: y = -1/2 sum_i d_i (Jac sum_j G_ji d_j (s x)) / (Jac s) + V x,
  *           s = sqRhoOVERJac.  G[sum_nq*D*D] per term laid out (iq, j, i) with
  *           iq fastest (GGiq), NULL = identity; Jac, sqRho NULL = 1.
@@ -83,6 +87,8 @@ typedef struct {
   const int* V_expo;
   const double* G0;
   const double* G1;
+  const double* F2_grid; /* type 1: Q-dependent coefficients, replace F2 / F1 when given */
+  const double* F1_grid;
 } orc_op;
 
 /* hpsi[N*nrhs] = H psi[N*nrhs] (column-major, ld = N).  nthreads <= 0 = all. */

@@ -335,3 +335,89 @@ def test_plan_tuner_every_plan_same_bits_and_cached(tmp_path):
     assert r2["from_cache"] and (r2["geo"], r2["rmax"], r2["split"]) == (r["geo"], r["rmax"], r["split"])
     import json
     assert len(json.load(open(cache))) == 1
+
+
+def _type1_grids(Q, D, rng, nonzero_pairs=None):
+    """Q-dependent type-1 coefficients on the grid points Q[sum_nq, D]:
+    F2_ij(Q) = a_ij (1 + 0.2 sin(Q_i + Q_j)), F1_i(Q) = b_i (1 + 0.1 Q_i^2),
+    i <= j; one pair left zero everywhere (a grid_zero term)."""
+    snq = Q.shape[0]
+    F2g = np.zeros((D, D, snq))
+    for i in range(D):
+        for j in range(i, D):
+            if nonzero_pairs is None or (i, j) in nonzero_pairs:
+                F2g[i, j] = rng.normal() * (1.0 + 0.2 * np.sin(Q[:, i] + Q[:, j]))
+    F2g[0, D - 1] = 0.0
+    F1g = rng.normal(size=(D, 1)) * (1.0 + 0.1 * Q.T ** 2)
+    return F2g, F1g
+
+
+@pytest.mark.parametrize("D,L,nrhs", [(3, 5, 2), (5, 7, 20), (7, 5, 20)])
+def test_type1_coefficient_grids_match_oracle(D, L, nrhs):
+    """CASE 1 with Q-dependent coefficient grids (OpGrid(iterm)%Grid that is
+    not grid_cte): GPU term by term vs the oracle, in the wide, narrow
+    (5-D, 20 RHS) and mid (7-D, 20 RHS) launch geometries; H^T against the
+    dense transpose; a grid that is constant gives the constant-coefficient
+    operator."""
+    need_cuda()
+    sq = np.full(D, 0.45)
+    b = SG4Basis(D, L, scaleQ=sq)
+    O = OracleSG4(D, L, L, 1, 1, 2, 1, scaleQ=sq)
+    rng = np.random.default_rng(40 + D)
+    Q = O.grid_points()
+    V = rng.normal(size=b.sum_nq)
+    F2g, F1g = _type1_grids(Q, D, rng)
+    op = ParamOp(b, 1, V=V, F2_grid=F2g, F1_grid=F1g)
+    psi = random_psi(b.N, nrhs, 7 + D)
+    ref = O.hpsi(psi, type_op=1, V=V, F2_grid=F2g, F1_grid=F1g)
+    assert rel_err(gpu_apply(op, psi), ref) <= TOL
+    lng = O.hpsi(psi, type_op=1, V=V, F2_grid=F2g, F1_grid=F1g, extended=True)
+    assert rel_err(gpu_apply(op, psi), lng) <= TOL
+    if D == 3:
+        H = O.hpsi(np.eye(O.N), type_op=1, V=V, F2_grid=F2g, F1_grid=F1g)
+        P = torch.from_numpy(np.ascontiguousarray(psi.T)).cuda()
+        out = torch.empty_like(P)
+        op.hpsi_dev(P, out, transpose=True)
+        torch.cuda.synchronize()
+        assert rel_err(out.cpu().numpy().T, H.T @ psi) <= TOL
+        pc = random_psi(O.N, 2, 3, complex_=True)
+        Pc = torch.from_numpy(np.ascontiguousarray(pc.T)).cuda()
+        oc = torch.empty_like(Pc)
+        op.hpsi_dev(Pc, oc, transpose=True)
+        torch.cuda.synchronize()
+        assert rel_err(oc.cpu().numpy().T, H.T @ pc) <= TOL
+        op.hpsi_dev(Pc, oc)
+        torch.cuda.synchronize()
+        assert rel_err(oc.cpu().numpy().T, H @ pc) <= TOL
+    # constant grids: the constant-coefficient operator (other passes, same operator)
+    F2 = np.triu(rng.normal(size=(D, D)))
+    F1 = rng.normal(size=D)
+    opg = ParamOp(b, 1, V=V, F2_grid=np.repeat(F2[:, :, None], b.sum_nq, axis=2),
+                  F1_grid=np.repeat(F1[:, None], b.sum_nq, axis=1))
+    opc = ParamOp(b, 1, V=V, F2=F2, F1=F1)
+    assert rel_err(gpu_apply(opg, psi), gpu_apply(opc, psi)) <= TOL
+
+
+def test_type1_coefficient_grids_in_a_multi_context_plan():
+    """A context with coefficient grids merged with others: the bits of its own launch."""
+    need_cuda()
+    from elvibrot_gb300 import MultiOp
+    D, L = 4, 6
+    b = SG4Basis(D, L, scaleQ=np.full(D, 0.5))
+    rng = np.random.default_rng(3)
+    F2g, F1g = _type1_grids(b.grid_points(), D, rng)
+    opg = ParamOp(b, 1, V=rng.normal(size=b.sum_nq), F2_grid=F2g, F1_grid=F1g)
+    ops = [opg, make_model(5, 5, 10, 9).operator(), make_model(3, 6, 1, 8).operator()]
+    nrhs = [4, 3, 2]
+    psis = [torch.from_numpy(np.ascontiguousarray(random_psi(op.basis.N, r, 20 + k).T)).cuda()
+            for k, (op, r) in enumerate(zip(ops, nrhs))]
+    ref = []
+    for op, P in zip(ops, psis):
+        O = torch.empty_like(P)
+        op.hpsi_dev(P, O)
+        ref.append(O)
+    outs = [torch.empty_like(P) for P in psis]
+    MultiOp(ops, nrhs).hpsi(psis, outs)
+    torch.cuda.synchronize()
+    for k in range(3):
+        assert torch.equal(outs[k], ref[k]), k

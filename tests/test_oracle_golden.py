@@ -169,3 +169,38 @@ def test_oracle_analytic_fields_match_grid_fields():
     r1 = O1.hpsi(psi1, type_op=1, V=m1.V(O1.grid_points()), F2=m1.F2.ravel())
     g1 = O1.hpsi(psi1, type_op=1, V_poly=(m1.V.coef, m1.V.expo), F2=m1.F2.ravel())
     assert np.max(np.abs(g1 - r1)) <= 1e-13 * np.max(np.abs(r1))
+
+
+def test_oracle_type1_coefficient_grids():
+    """Type-1 coefficients given as grids (OpGrid(iterm)%Grid): a grid equal
+    to the constant everywhere gives the constant-coefficient operator bit
+    for bit, a grid zero everywhere drops its term (grid_zero), and a
+    Q-dependent grid multiplies its term's derivatives point by point.  One
+    thread: the reference's atomic scatter makes the sum order, and so the
+    last bits, depend on the thread schedule."""
+    D, L = 3, 4
+    O = OracleSG4(D, L, L, 1, 1, 2, 1, scaleQ=np.full(D, 0.5))
+    rng = np.random.default_rng(12)
+    snq = O.sum_nq
+    V = rng.normal(size=snq)
+    F2 = np.triu(rng.normal(size=(D, D)))
+    F1 = rng.normal(size=D)
+    psi = rng.normal(size=(O.N, 2))
+    ref = O.hpsi(psi, type_op=1, V=V, F2=F2.ravel(), F1=F1, nthreads=1)
+    F2g = np.repeat(F2[:, :, None], snq, axis=2)
+    F1g = np.repeat(F1[:, None], snq, axis=1)
+    assert np.array_equal(O.hpsi(psi, type_op=1, V=V, F2_grid=F2g, F1_grid=F1g, nthreads=1), ref)
+    F2z = F2.copy()
+    F2z[0, 1] = 0.0
+    F2gz = F2g.copy()
+    F2gz[0, 1] = 0.0
+    assert np.array_equal(O.hpsi(psi, type_op=1, V=V, F2_grid=F2gz, F1_grid=F1g, nthreads=1),
+                          O.hpsi(psi, type_op=1, V=V, F2=F2z.ravel(), F1=F1, nthreads=1))
+    # a coefficient that is a sum of two grids: the operator is linear in it
+    g1 = rng.normal(size=snq)
+    g2 = rng.normal(size=snq)
+    def one(g):
+        G = np.zeros((D, D, snq))
+        G[1, 2] = g
+        return O.hpsi(psi, type_op=1, F2_grid=G)
+    np.testing.assert_allclose(one(g1 + g2), one(g1) + one(g2), rtol=0, atol=1e-12 * np.abs(one(g1 + g2)).max())
