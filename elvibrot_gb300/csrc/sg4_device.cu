@@ -8,18 +8,20 @@
 //   sub_TabOpPsi_OF_ONEDP_FOR_SGtype4) -> grid->basis (GDP_TO_BDP) ->
 //   weighted atomic scatter (tabR_AT_iG_TO_tabPackedBasis).
 // Here one persistent kernel runs every (term, block of right-hand sides)
-// work item of one H.psi: CTAs pull items from a cost-sorted list through a
-// global atomic counter, keep the whole term in shared memory (a per-CTA
-// slab of global scratch when a term does not fit), apply the 1-D matrices
-// mode by mode with one thread per fibre, and write each term's weighted
+// work item of one H.psi, of one context or of several: CTAs pull items from
+// a cost-sorted list through a global atomic counter, keep the term in
+// shared memory (x in shared memory and the rest in a per-CTA slab of global
+// scratch when a term does not fit), apply the 1-D matrices mode by mode
+// (fused grid passes for the operators), and write each term's weighted
 // result to a contribution buffer that two small kernels then sum per packed
 // function in Smolyak-term order (compensated, deterministic, no atomics).
-// GB300's FP64 pipe (~1.2 TFLOP/s measured) is the binding resource, so the
-// kernel is organised to keep it busy: several CTAs per SM (four, or eight
-// for D <= 6) so some compute while the others gather or synchronise,
-// right-hand sides batched per item so the 1-D matrices and the operator
-// fields are loaded once per point, and no FP64 work spent on anything but
-// the algorithm's own multiply-adds.
+// The contexts' parameters travel by value in the launch (a __grid_constant__
+// block).  GB300's FP64 pipe (~1.25 TFLOP/s measured) is the binding
+// resource, so the kernel is organised to keep it busy: several CTAs per SM
+// (four, six, or eight for D <= 6) so some compute while the others gather or
+// synchronise, right-hand sides grouped per item so the 1-D matrices and the
+// operator fields are loaded once per point for the group, and no FP64 work
+// spent on anything but the algorithm's own multiply-adds.
 #include <cuda_runtime.h>
 
 #include <algorithm>

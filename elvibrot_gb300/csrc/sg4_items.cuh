@@ -27,8 +27,9 @@ namespace evr {
 //   mid (2), D > 6: six CTAs per SM (35.75 KB, 80 registers, fused passes up
 //     to D = 12): 4-7 % on the 12-D streamed operator and the uneven
 //     multi-instance draw.
-// Each geometry's kernels are compiled in their own translation unit
-// (sg4_items.cu built with EVR_GEO = 0, 1, 2), in parallel.
+// Each geometry's kernels are compiled in their own translation units
+// (sg4_items.cu built with EVR_GEO = 0, 1, 2 and EVR_KIND = 0, 1, 2), in
+// parallel.
 #ifndef EVR_CTA_THREADS
 #define EVR_CTA_THREADS 128
 #endif

@@ -1377,7 +1377,7 @@ extern "C" int evr_sg4_oc_gradient(evr_sg4_ctx* H0, evr_sg4_ctx* mu, const evr_r
 
 // ------------------------------------------------------------------------
 // Chebyshev propagation of every context of a complex multi-context plan in
-// lock-step (the batched uneven-instance workload): each expansion order is
+// lock-step (the uneven-instance workload): each expansion order is
 // ONE evr_sg4_multi_hpsi over all contexts still in their step, with each
 // context's own (E0, Esc) fused, followed by the per-context recurrence
 // update.  Per context the arithmetic is that of evr_sg4_cheby_propagate
