@@ -856,31 +856,39 @@ extern "C" int evr_sg4_set_operator(evr_sg4_ctx* c, const evr_sg4_op_desc* op) {
   }
   if (op->type == 1 && (op->F2_grid || op->F1_grid)) {
     // Q-dependent coefficients: the term list in Init_TypeOp order, (i, j >= i)
-    // then (i, 0); a grid that is zero everywhere is skipped (grid_zero), a
-    // term without a grid keeps its constant
+    // then (i, 0), with the channel pairs (a, b) of each term inside (several
+    // channels: one grid per pair, GridOp(:,a,b,iterm)); a grid that is zero
+    // everywhere is skipped (grid_zero), a term without a grid keeps its
+    // constant on every channel alike
+    const int nc = c->nb0 * c->nb0;
     std::vector<T1Term> tl;
     std::vector<const double*> src;
     auto add = [&](int i, int j, const double* g, double cst) -> int {
-      if (g) {
+      if (!g) {
+        if (cst != 0.0) tl.push_back(T1Term{i, j, -1, -1, -1, cst});
+        return EVR_OK;
+      }
+      for (int ab = 0; ab < nc; ++ab) {
+        const double* ga = g + (size_t)ab * snq;
         bool zero = true;
         for (long long k = 0; k < snq; ++k) {
-          if (!std::isfinite(g[k])) return set_error(EVR_ERR_NUMERIC, "type-1 coefficient grid (%d, %d) is not finite", i, j);
-          if (g[k] != 0.0) zero = false;
+          if (!std::isfinite(ga[k]))
+            return set_error(EVR_ERR_NUMERIC, "type-1 coefficient grid (%d, %d) is not finite", i, j);
+          if (ga[k] != 0.0) zero = false;
         }
-        if (zero) return EVR_OK;
-        tl.push_back(T1Term{i, j, (long long)src.size() * snq, 0.0});
-        src.push_back(g);
-      } else if (cst != 0.0) {
-        tl.push_back(T1Term{i, j, -1, cst});
+        if (zero) continue;
+        tl.push_back(T1Term{i, j, c->nb0 > 1 ? ab / c->nb0 : -1, c->nb0 > 1 ? ab % c->nb0 : -1,
+                            (long long)src.size() * snq, 0.0});
+        src.push_back(ga);
       }
       return EVR_OK;
     };
     for (int i = 0; i < D; ++i)
       for (int j = i; j < D; ++j)
-        if ((rc = add(i, j, op->F2_grid ? op->F2_grid + (size_t)(i * D + j) * snq : nullptr, c->F2[i * D + j])))
+        if ((rc = add(i, j, op->F2_grid ? op->F2_grid + (size_t)(i * D + j) * nc * snq : nullptr, c->F2[i * D + j])))
           return rc;
     for (int i = 0; i < D; ++i)
-      if ((rc = add(i, -1, op->F1_grid ? op->F1_grid + (size_t)i * snq : nullptr, c->F1[i]))) return rc;
+      if ((rc = add(i, -1, op->F1_grid ? op->F1_grid + (size_t)i * nc * snq : nullptr, c->F1[i]))) return rc;
     memset(c->F2, 0, sizeof(c->F2));  // every term is in the list
     memset(c->F1, 0, sizeof(c->F1));
     if (!src.empty()) {
@@ -1285,8 +1293,13 @@ extern "C" int evr_sg4_flops_per_rhs(const evr_sg4_ctx* c, double* flops) {
       f += vq;
     } else if (c->type == 1 && c->n_t1 > 0) {  // term by term: derivative passes, then coefficient x result
       f += vq;
-      for (const T1Term& t : c->t1_terms)
-        f += 2.0 * q * nq[t.i] + (t.j > t.i ? 2.0 * q * nq[t.j] : 0.0) + 2.0 * q;
+      int pi = -2, pj = -2;
+      for (const T1Term& t : c->t1_terms) {
+        if (t.i != pi || t.j != pj) f += 2.0 * q * nq[t.i] + (t.j > t.i ? 2.0 * q * nq[t.j] : 0.0);
+        pi = t.i;
+        pj = t.j;
+        f += t.a < 0 ? 2.0 * q : 2.0 * q / c->nb0;  // per column: a channel-pair grid acts on one channel of nb0
+      }
     } else if (c->type == 1) {  // the fused passes (type1_fused; the same for a diagonal F2 term by term)
       f += vq;
       for (int i = 0; i < D; ++i)

@@ -113,9 +113,11 @@ struct OpFields {
 
 // A type-1 derivative term with its coefficient (CASE 1 with Q-dependent
 // coefficients): coefficient * d_i d_j x, or * d_i x when j < 0; the
-// coefficient is the grid t1grid[goff + point] or, when goff < 0, c.
+// coefficient is the grid t1grid[goff + point] or, when goff < 0, c.  With
+// a >= 0 it couples channel b into channel a (GridOp(:,a,b,iterm)); a < 0:
+// it acts on every channel alike.
 struct T1Term {
-  int i, j;
+  int i, j, a, b;
   long long goff;
   double c;
 };
@@ -701,41 +703,55 @@ static __device__ void store_contrib(const KParams& p, const ItemShared& it, con
 // CASE 1 with Q-dependent coefficients, term by term as the reference
 // (sub_OpPsi_SG4.f90:1497-1520): each term's derivatives of x
 // (DerivOp_TO_RDP_OF_SmolaykRep), then times its coefficient grid, added
-// into Y; the terms act on every channel alike.  For H^T a term is
-// (g d_i d_j)^T = d_i^T d_j^T g (the transposed matrices of the item): the
-// coefficient first, then the derivatives.  Buffers: x (X or T), Y = T + NQR,
-// C = T + 2 NQR and the other of X / T.  (Not inlined, the call made the mid
-// kernel keep a 888-byte stack frame; inlined it adds some spill code to the
-// kernels for every operator type, not to the type-10 one.)
+// into Y, on every channel alike or from channel b into channel a
+// (OpPsi(:,a) += GridOp(:,a,b,iterm) * Psi_ch(:,b)); consecutive entries of
+// one term reuse its derivatives.  Channel c of the item's column k is
+// ((rhs0 + k) >> cshift) % nb0 (items hold whole channel groups), so channel
+// b of the same right-hand side is (b - a) << cshift columns away.  For H^T
+// an entry is (g d_i d_j)^T = d_i^T d_j^T g from channel a into channel b
+// (the transposed matrices of the item): the coefficient first, then the
+// derivatives.  Buffers: x (X or T), Y = T + NQR, C = T + 2 NQR and the
+// other of X / T.  (Not inlined, the call made the mid kernel keep a
+// 888-byte stack frame; inlined it adds some spill code to the kernels for
+// every operator type, not to the type-10 one.)
 static __device__ __forceinline__ double* type1_grid_terms(const KParams& p, const ItemShared& it, double* x, double* X,
-                                                        double* T, int NQR) {
+                                                           double* T, int NQR) {
   const int nqt = it.nq_t;
   const long long oq = it.off_nq;
   double* Y = T + NQR;
   double* C = T + 2 * NQR;
   double* C2 = (x == X) ? T : X;
+  auto chan = [&](int e) { return ((it.rhs0 + e / nqt) >> p.cshift) % p.nb0; };
   for (int e = threadIdx.x; e < NQR; e += blockDim.x) {
     const int q = e % nqt;
     Y[e] = !p.V ? 0.0 : (p.nb0 == 1 ? __ldg(p.V + oq + q) * x[e] : vmat_apply(p, x, e, nqt, oq, it.rhs0));
   }
   __syncthreads();
+  int pi = -2, pj = -2;  // the term whose derivatives C2 holds
   for (int t = 0; t < p.n_t1; ++t) {
     const T1Term tt = p.t1terms[t];
     const double* g = tt.goff >= 0 ? p.t1grid + tt.goff + oq : nullptr;
+    const int shift = (tt.a >= 0 ? tt.b - tt.a : 0) << p.cshift;  // columns from channel a to channel b
     if (!p.transpose) {
-      if (tt.j < 0) {
-        grid_deriv(p, it, tt.i, M_D1, x, C2, false, 1.0);
-      } else if (tt.j == tt.i) {
-        grid_deriv(p, it, tt.i, M_D2, x, C2, false, 1.0);
-      } else {
-        grid_deriv(p, it, tt.j, M_D1, x, C, false, 1.0);
+      if (tt.i != pi || tt.j != pj) {
+        if (tt.j < 0) {
+          grid_deriv(p, it, tt.i, M_D1, x, C2, false, 1.0);
+        } else if (tt.j == tt.i) {
+          grid_deriv(p, it, tt.i, M_D2, x, C2, false, 1.0);
+        } else {
+          grid_deriv(p, it, tt.j, M_D1, x, C, false, 1.0);
+          __syncthreads();
+          grid_deriv(p, it, tt.i, M_D1, C, C2, false, 1.0);
+        }
         __syncthreads();
-        grid_deriv(p, it, tt.i, M_D1, C, C2, false, 1.0);
+        pi = tt.i;
+        pj = tt.j;
       }
-      __syncthreads();
-      for (int e = threadIdx.x; e < NQR; e += blockDim.x) Y[e] = fma(g ? __ldg(g + e % nqt) : tt.c, C2[e], Y[e]);
+      for (int e = threadIdx.x; e < NQR; e += blockDim.x)
+        if (tt.a < 0 || chan(e) == tt.a) Y[e] = fma(g ? __ldg(g + e % nqt) : tt.c, C2[e + shift * nqt], Y[e]);
     } else {
-      for (int e = threadIdx.x; e < NQR; e += blockDim.x) C[e] = (g ? __ldg(g + e % nqt) : tt.c) * x[e];
+      for (int e = threadIdx.x; e < NQR; e += blockDim.x)
+        C[e] = (tt.a < 0 || chan(e) == tt.b) ? (g ? __ldg(g + e % nqt) : tt.c) * x[e - shift * nqt] : 0.0;
       __syncthreads();
       if (tt.j < 0) {
         grid_deriv(p, it, tt.i, M_D1, C, Y, true, 1.0);

@@ -289,7 +289,8 @@ class ParamOp:
     """SG4 operator on the GPU (param_Op with its Save_MemGrid grids).
 
     type_op 0 : V;  1 : V + sum F2_ij d_i d_j + sum F1_i d_i (F constant, or
-    Q-dependent grids F2_grid [D, D, sum_nq] / F1_grid [D, sum_nq]);
+    Q-dependent grids F2_grid [D, D, nb0*nb0, sum_nq] / F1_grid [D, nb0*nb0,
+    sum_nq], channel pair (a, b) at a*nb0 + b);
     10 : -1/2 sum d_i Jac G_ji d_j s / (Jac s) + V with G grid or affine G(Q).
     """
 
@@ -316,7 +317,8 @@ class ParamOp:
         keep = dict(V=c(V), G=c(G), G0=c(G0), G1=c(G1), Jac=c(Jac), sqRho=c(sqRho), F2=c(F2), F1=c(F1),
                     F2_grid=c(F2_grid), F1_grid=c(F1_grid))
         snq = self.basis.sum_nq
-        for name, n in (("F2_grid", D * D * snq), ("F1_grid", D * snq)):
+        nc = self.basis.nb0 ** 2
+        for name, n in (("F2_grid", D * D * nc * snq), ("F1_grid", D * nc * snq)):
             if keep[name] is not None and keep[name].size != n:
                 raise EVRError(1, f"{name}: {keep[name].size} values, expected {n}")
         coef = expo = None

@@ -130,14 +130,17 @@ int evr_sg4_destroy(evr_sg4_ctx* c);
  * or the affine form G_ij(Q) = G0_ij + sum_k G1_ijk Q_k ([D*D], [D*D*D],
  * row-major ijk); neither = identity.  Jac / sqRho grids: NULL = 1.
  * F2 [D*D] row-major (entries i<=j used) and F1 [D]: constant coefficients.
- * F2_grid [D*D*sum_nq] (term (i, j), i <= j, at [(i*D + j)*sum_nq + point])
- * and F1_grid [D*sum_nq] (term i at [i*sum_nq + point]): Q-dependent
- * coefficients of the type-1 derivative terms (OpGrid(iterm)%Grid when it is
- * not grid_cte); when given they replace F2 / F1.  Then every derivative
- * term is applied on its own, its derivatives first and its coefficient grid
- * after, in Init_TypeOp order ((i, j >= i), then (i, 0)), and a term whose
- * grid is zero everywhere is skipped (grid_zero); the terms act on every
- * channel alike.  Such grids stay resident.
+ * F2_grid [D*D*nb0*nb0*sum_nq] (term (i, j), i <= j, channel pair (a, b) at
+ * [((i*D + j)*nb0*nb0 + a*nb0 + b)*sum_nq + point]) and F1_grid
+ * [D*nb0*nb0*sum_nq] (term i at [(i*nb0*nb0 + a*nb0 + b)*sum_nq + point]):
+ * Q-dependent coefficients of the type-1 derivative terms (OpGrid(iterm)%Grid
+ * when it is not grid_cte; element (a, b) couples channel b into channel a,
+ * OpPsi(:,a) += GridOp(:,a,b,iterm) * Psi_ch(:,b)); when given they replace
+ * F2 / F1.  Then every derivative term is applied on its own, its
+ * derivatives first and its coefficient grids after, in Init_TypeOp order
+ * ((i, j >= i), then (i, 0)), and a grid that is zero everywhere is skipped
+ * (grid_zero).  Such grids stay resident.  Constant F2 / F1 act on every
+ * channel alike.
  * All pointers are host pointers; the fields are built once on the device
  * (the equivalent of Save_MemGrid).
  * ---------------------------------------------------------------------- */

@@ -198,3 +198,40 @@ def test_channels_polynomial_v_matches_grid_v():
             assert err <= 1e-13
     with pytest.raises(EVRError):                                  # wrong number of coefficients
         ParamOp(basis, 1, V_poly=Polynomial(coef[0], expo), F2=-0.5 * np.eye(D))
+
+
+def test_channel_coupled_derivative_terms_match_oracle_blocks():
+    """Type-1 derivative terms whose coefficient grids couple channels
+    (GridOp(:,a,b,iterm) with a != b: non-adiabatic derivative couplings):
+    the dense GPU H, real and complex, H and H^T, against the oracle's
+    blocks H_ab = V_ab + sum_t GridOp_t(:,a,b) Der_t, each a one-channel
+    type-1 operator with coefficient grids."""
+    need_cuda()
+    D, L, nb0 = 3, 4, 2
+    basis = SG4Basis(D, L, L, 1, 1, 2, 1, nb0=nb0)
+    O = OracleSG4(D, L, L, 1, 1, 2, 1)
+    Q = O.grid_points()
+    snq = len(Q)
+    rng = np.random.default_rng(77)
+    Vm = np.empty((nb0, nb0, snq))
+    F2g = np.zeros((D, D, nb0, nb0, snq))
+    F1g = np.zeros((D, nb0, nb0, snq))
+    for a in range(nb0):
+        for b in range(nb0):
+            c = rng.normal(size=D + 1)
+            Vm[a, b] = c[0] + Q @ c[1:] + (0.5 * (Q * Q).sum(axis=1) if a == b else 0.0)
+            for i in range(D):
+                for j in range(i, D):
+                    if a == b or (i, j) == (0, 1):   # kinetic terms on each channel, one coupled mixed term
+                        F2g[i, j, a, b] = (-0.5 if i == j else 0.1) * rng.uniform(0.5, 1.5) * (1 + 0.1 * np.cos(Q[:, j]))
+            if a != b:                                # first-derivative couplings
+                F1g[:, a, b] = rng.normal(size=(D, 1)) * 0.2 * (1 + 0.1 * Q.T)
+    op = ParamOp(basis, 1, V=Vm.reshape(nb0 * nb0, -1), F2_grid=F2g.reshape(-1), F1_grid=F1g.reshape(-1))
+    I = np.eye(O.N)
+    Href = np.block([[O.hpsi(I, type_op=1, V=Vm[a, b], F2_grid=F2g[:, :, a, b], F1_grid=F1g[:, a, b])
+                      for b in range(nb0)] for a in range(nb0)])
+    scale = np.max(np.abs(Href))
+    for cplx, tr in ((False, False), (False, True), (True, False), (True, True)):
+        H = gpu_dense(op, basis.nvec, cplx, tr)
+        ref = Href.T if tr else Href
+        assert np.max(np.abs(H - ref)) / scale <= 1e-12, (cplx, tr)
