@@ -21,9 +21,10 @@ SOURCES = ["sg4_device.cu", "sg4_solvers.cu", "sg4_setup.cpp", "sg4_items.cu"]
 # translation units: (source, object, extra flags); each item kernel is its
 # own unit, per launch geometry (wide, narrow, mid) and kind (small parameter
 # block: one context or a field-driven pair; large: multi-context plans;
-# small, compiled for type-10 operators only)
+# small, compiled for type-10 operators only; small, with type-1
+# coefficient grids)
 UNITS = [("sg4_items.cu", f"sg4_items_g{g}_k{k}.o", [f"-DEVR_GEO={g}", f"-DEVR_KIND={k}"])
-         for g in range(3) for k in range(3)] + [
+         for g in range(3) for k in range(4)] + [
     ("sg4_device.cu", "sg4_device.o", []), ("sg4_solvers.cu", "sg4_solvers.o", []),
     ("sg4_setup.cpp", "sg4_setup.o", [])]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

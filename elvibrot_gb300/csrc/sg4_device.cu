@@ -122,12 +122,14 @@ struct GeoKernels {
   const MultiEntry<EVR_PB_SMALL>* small;
   const MultiEntry<EVR_PB_LARGE>* large;
   const MultiEntry<EVR_PB_SMALL>* small10;  // type 10 with D <= fmax only
+  const MultiEntry<EVR_PB_SMALL>* small1g;  // with type-1 coefficient grids
 };
 static const GeoKernels& geo_kernels(int geo) {
   static const GeoKernels t[3] = {
-      {EVR_WIDE_CTAS, EVR_WIDE_FMAX, &multi_small_wide, &multi_large_wide, &multi_small10_wide},
-      {EVR_NARROW_CTAS, EVR_NARROW_FMAX, &multi_small_narrow, &multi_large_narrow, &multi_small10_narrow},
-      {EVR_MID_CTAS, EVR_MID_FMAX, &multi_small_mid, &multi_large_mid, &multi_small10_mid}};
+      {EVR_WIDE_CTAS, EVR_WIDE_FMAX, &multi_small_wide, &multi_large_wide, &multi_small10_wide, &multi_small1g_wide},
+      {EVR_NARROW_CTAS, EVR_NARROW_FMAX, &multi_small_narrow, &multi_large_narrow, &multi_small10_narrow,
+       &multi_small1g_narrow},
+      {EVR_MID_CTAS, EVR_MID_FMAX, &multi_small_mid, &multi_large_mid, &multi_small10_mid, &multi_small1g_mid}};
   return t[geo == 1 ? 1 : (geo == 2 ? 2 : 0)];
 }
 
@@ -141,9 +143,12 @@ static void launch_multi(int geo, unsigned grid, size_t smem, cudaStream_t s, co
   if (n_ctx <= EVR_PB_SMALL) {
     ParamBlock<EVR_PB_SMALL> P;
     std::copy(ps, ps + n_ctx, P.p);
-    bool t10 = true;  // every context type 10 within the fused passes: the kernel compiled for them
-    for (int j = 0; j < n_ctx; ++j) t10 = t10 && ps[j].type == 10 && ps[j].D <= k.fmax;
-    (t10 ? k.small10 : k.small)->launch(grid, smem, s, P, items, n_items, item_base, counter);
+    bool t10 = true, grids = false;  // the kernel compiled for the contexts' operators
+    for (int j = 0; j < n_ctx; ++j) {
+      t10 = t10 && ps[j].type == 10 && ps[j].D <= k.fmax;
+      grids = grids || (ps[j].type == 1 && ps[j].n_t1 > 0);
+    }
+    (t10 ? k.small10 : (grids ? k.small1g : k.small))->launch(grid, smem, s, P, items, n_items, item_base, counter);
   } else {
     static thread_local ParamBlock<EVR_PB_LARGE> P;  // 16 KB: not on the stack
     std::copy(ps, ps + n_ctx, P.p);
@@ -167,14 +172,14 @@ static int smem_slack(int geo) {
   static const std::vector<int> slack = [] {
     std::vector<int> v(3, 4096);
     for (int g = 0; g < 3; ++g) {
-      size_t a = 0, b = 0, c = 0;
+      size_t a = 0, b = 0, c = 0, d = 0;
       const GeoKernels& k = geo_kernels(g);
       if (k.small->static_smem(&a) != cudaSuccess || k.large->static_smem(&b) != cudaSuccess ||
-          k.small10->static_smem(&c) != cudaSuccess) {
+          k.small10->static_smem(&c) != cudaSuccess || k.small1g->static_smem(&d) != cudaSuccess) {
         cudaGetLastError();
         continue;
       }
-      v[g] = (int)((std::max(a, std::max(b, c)) + 1024 + 255) / 256 * 256);
+      v[g] = (int)((std::max(std::max(a, b), std::max(c, d)) + 1024 + 255) / 256 * 256);
     }
     return v;
   }();
@@ -195,6 +200,7 @@ static cudaError_t set_smem_attributes() {
     e = k.small->set_smem(bytes);
     if (e == cudaSuccess) e = k.large->set_smem(bytes);
     if (e == cudaSuccess) e = k.small10->set_smem(bytes);
+    if (e == cudaSuccess) e = k.small1g->set_smem(bytes);
   }
   return e;
 }

@@ -768,9 +768,10 @@ static __device__ __forceinline__ double* type1_grid_terms(const KParams& p, con
   return Y;
 }
 
-// OPK: 0 every operator type; 10 only type 10 with D <= FMAX (the fused
-// passes), for launches whose contexts are all such (the other branches are
-// not compiled in).
+// OPK: 0 every operator type, without type-1 coefficient grids; 1 every
+// type, with them; 10 only type 10 with D <= FMAX (the fused passes), for
+// launches whose contexts are all such (the other branches are not compiled
+// in).  The host picks the kernel for the contexts of a launch.
 template <int FMAX, int OPK>
 __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int term, int rhs0) {
   if (threadIdx.x == 0) {
@@ -863,7 +864,7 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ter
       for (int e = threadIdx.x; e < NQR; e += blockDim.x) y[e] = p.V ? vmat_apply(p, x, e, nqt, oq, it.rhs0) : 0.0;
     }
     __syncthreads();
-  } else if (OPK != 10 && p.type == 1 && p.n_t1 > 0) {
+  } else if (OPK == 1 && p.type == 1 && p.n_t1 > 0) {
     y = type1_grid_terms(p, it, x, X, T, NQR);
   } else if (OPK != 10 && p.type == 1) {
     // CASE 1 through the fused grid passes in the wide and mid kernels (x in
@@ -1024,7 +1025,9 @@ struct ParamBlock {
 // argument was 1.3 % slower on the 6-D benchmark (more spill code).
 // OPK 10 compiles only the fused type-10 path (launches whose contexts are
 // all type 10 with D <= FMAX): less code and fewer spills, 1.2 % faster on
-// the 6-D benchmark than the kernel for every type.
+// the 6-D benchmark than the kernel for every type.  OPK 0 leaves out the
+// type-1 coefficient grids (with them the wide kernel spilled and an RK4
+// stage took 2 % longer); OPK 1 has them.
 // With a counter the CTAs pull items until the list is empty; without one
 // (the per-term path) CTA b runs item item_base + b.
 template <int MINB, int FMAX, int CAP, int OPK>
@@ -1047,8 +1050,10 @@ __global__ void __launch_bounds__(EVR_CTA_THREADS, MINB) hpsi_items_kernel(const
 
 // One kernel of one launch geometry, each compiled in its own translation
 // unit (sg4_items.cu with EVR_GEO = 0 wide, 1 narrow, 2 mid and EVR_KIND = 0
-// the small, 1 the large parameter block, 2 the small block for type 10
-// only); the host code in sg4_device.cu assembles them per geometry.
+// the small parameter block without type-1 coefficient grids, 1 the large
+// block, 2 the small block for type 10 only, 3 the small block with
+// coefficient grids); the host code in sg4_device.cu assembles them per
+// geometry.
 template <int CAP>
 struct MultiEntry {
   void (*launch)(unsigned grid, size_t smem, cudaStream_t s, const ParamBlock<CAP>& P, const MItem* items,
@@ -1058,6 +1063,7 @@ struct MultiEntry {
 };
 extern const MultiEntry<EVR_PB_SMALL> multi_small_wide, multi_small_narrow, multi_small_mid;
 extern const MultiEntry<EVR_PB_SMALL> multi_small10_wide, multi_small10_narrow, multi_small10_mid;
+extern const MultiEntry<EVR_PB_SMALL> multi_small1g_wide, multi_small1g_narrow, multi_small1g_mid;
 extern const MultiEntry<EVR_PB_LARGE> multi_large_wide, multi_large_narrow, multi_large_mid;
 
 }  // namespace evr
