@@ -150,7 +150,7 @@ static void launch_multi(int geo, unsigned grid, size_t smem, cudaStream_t s, co
     }
     (t10 ? k.small10 : (grids ? k.small1g : k.small))->launch(grid, smem, s, P, items, n_items, item_base, counter);
   } else {
-    static thread_local ParamBlock<EVR_PB_LARGE> P;  // 16 KB: not on the stack
+    static thread_local ParamBlock<EVR_PB_LARGE> P;  // 17.5 KB: not on the stack
     std::copy(ps, ps + n_ctx, P.p);
     k.large->launch(grid, smem, s, P, items, n_items, item_base, counter);
   }

@@ -1008,12 +1008,14 @@ __device__ void run_item(const KParams& p, ItemShared& it, double* smem, int ter
 // The parameter blocks of a launch, passed by value: EVR_PB_SMALL contexts
 // (a single context, the field-driven pairs) or EVR_PB_LARGE (the
 // multi-context plans split their contexts into launches of at most this
-// many; 16 KB, inside the 32 KB kernel-parameter limit).
+// many; 17.5 KB, inside the 32 KB kernel-parameter limit).
 enum { EVR_PB_SMALL = 2, EVR_PB_LARGE = 64 };
 template <int CAP>
 struct ParamBlock {
   KParams p[CAP];
 };
+// the launch's other arguments take 32 bytes of the 32,764-byte limit
+static_assert(sizeof(ParamBlock<EVR_PB_LARGE>) + 32 <= 32764, "parameter block beyond the kernel-parameter limit");
 
 // The persistent H.psi kernel: every work item of a launch, of one or several
 // contexts; each item names its context's slot in the parameter block.  The
